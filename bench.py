@@ -1,0 +1,387 @@
+#!/usr/bin/env python
+"""Benchmark of the Pauli-sum product H psi on GB300 (one JSON line).
+
+Workload (default): the 26-qubit Jordan-Wigner-style operator -- 8,000 pair
+terms (X/Y at i and j, Z strictly between) + 2,000 pure-Z terms on 1-4
+qubits, coefficients ~ N(0, 0.1), seed 20262 -- applied to one unit-norm
+2^26-amplitude state.  A step is one H psi over the whole state.
+Metric: term*amp/s = (input terms) * 2^n * states / seconds.
+
+Arms:
+  (default)          our sm_103a kernels through libqrusty_gpu's C ABI.
+                     `value` = compensated-complex64 kernel, device-resident
+                     inputs; `e2e` = the C-ABI host entry (qr_apply_host) with
+                     pinned host buffers, copies included; the plain complex128
+                     kernel is reported beside it.
+  --impl reference   the reference's CPU method (rowwise CSR build + chunked
+                     CSR*vector, restated in C in oracle/) on all host cores, on
+                     a bounded row sample of the same workload.
+
+Multi-GPU (torchrun, N > 1): replicas -- every rank applies the operator to
+its own state (weak scaling, no data-path collective); max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Pauli-sum H·ψ term·amp/s & %HBM peak; c64-compensated vs c128 at stated rel err"
+UNIT = "term*amp/s"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------------------- helpers
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the c64c apply kernel from the committed ncu
+    summary (profiles/ncu_traffic.json), scaled to the bench workload."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev_index: int):
+        self.dev = dev_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        import tempfile
+        fd, self.path = tempfile.mkstemp(prefix="qr_clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        load = sorted(sm)
+        return {"sm_mhz": statistics.median(load) if load else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- workloads
+def make_terms(args):
+    from qrusty_gb300 import workloads as W
+    if args.workload == "jw":
+        t = W.cfg2(n=args.n, npair=args.pairs, nz=args.zterms)
+        desc = ("jordan-wigner n=%d: %d pair terms + %d pure-Z terms (seed %d)"
+                % (args.n, args.pairs, args.zterms, W.SEED0 + 2))
+    elif args.workload == "chain":
+        t, _ = W.cfg1(with_state=False, n=args.n)
+        desc = "tfim+xxz open chain n=%d, %d terms (seed %d)" % (args.n, t.T, W.SEED0 + 1)
+    else:
+        raise SystemExit("unknown workload %s" % args.workload)
+    return t, desc
+
+
+# ----------------------------------------------------------------------------- CPU arm
+def cpu_reference(t, rows, reps, nthreads):
+    """Reference method on host cores: rowwise CSR build of a row sample,
+    then chunked CSR*vector (1024-row chunks) over it."""
+    from oracle import oracle as O
+    O.build()
+    N = 1 << t.n
+    rng = np.random.default_rng(5)
+    psi = np.empty(N, dtype=np.complex128)
+    psi.real = rng.standard_normal(N)
+    psi.imag = rng.standard_normal(N)
+    cp = O.make_params(t.phase, t.coeff)
+    t0 = time.perf_counter()
+    ip, ij, d = O.csr_build(t.n, t.x, t.z, cp, step=1024, nthreads=nthreads, rows=(0, rows))
+    t_build = time.perf_counter() - t0
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        O.spmv(ip, ij, d, psi, step=1024, nthreads=nthreads)
+        times.append(time.perf_counter() - t0)
+    return t_build, times
+
+
+def run_reference_arm(args, t, desc):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    rows = args.cpu_rows
+    t_build, times = cpu_reference(t, rows, args.warmup + args.steps, nthreads)
+    timed = times[args.warmup:]
+    ms = 1e3 * statistics.mean(timed)
+    units = t.T * rows
+    value = units / (ms / 1e3)
+    sample = ("rows [0, %d) of 2^%d: CSR build %.2f s (make_row, chunks of 1024), then one "
+              "CSR*vector per step; value = sample term*amp / SpMV time" % (rows, t.n, t_build))
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": desc, "n": t.n, "terms": t.T, "states": 1},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "csr_build_s": t_build,
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_gpu_arm(args, t, desc):
+    import torch
+    from qrusty_gb300 import PauliOperator, _lib
+    from qrusty_gb300 import workloads as W
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n, N, T = t.n, 1 << t.n, t.T
+    op = PauliOperator(n, t.x, t.z, t.phase, t.coeff)
+    info = op.info()
+    P = W.alg_blocks(t, 13)
+    g = torch.Generator(device=dev).manual_seed(1000 + rank)
+    psi128 = torch.complex(torch.randn(N, device=dev, dtype=torch.float64, generator=g),
+                           torch.randn(N, device=dev, dtype=torch.float64, generator=g))
+    psi128 /= torch.linalg.vector_norm(psi128)
+    psi64 = psi128.to(torch.complex64)
+    y64 = torch.empty_like(psi64)
+    y128 = torch.empty_like(psi128)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        barrier()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        l0 = _lib.launch_count()
+        e_all0 = torch.cuda.Event(enable_timing=True)
+        e_all1 = torch.cuda.Event(enable_timing=True)
+        e_all0.record(stream)
+        for a, b in evs:
+            a.record(stream)
+            fn()
+            b.record(stream)
+        e_all1.record(stream)
+        barrier()
+        launches = _lib.launch_count() - l0
+        per = [a.elapsed_time(b) for a, b in evs]
+        total = e_all0.elapsed_time(e_all1)
+        if ws > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([total], device=dev, dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            total = float(tt.item())
+        return total, per, launches
+
+    clocks = ClockSampler(dev.index if dev.index is not None else 0)
+
+    # --- compensated complex64 (headline)
+    f64c = lambda: op.apply(psi64, out=y64)
+    clocks.start() if rank == 0 and not args.quick else None
+    tot64, per64, launches = timed(f64c, args.steps, args.warmup)
+    clk = clocks.stop() if rank == 0 and not args.quick else None
+    op.sync_check()
+    ms64 = tot64 / args.steps
+
+    # --- plain complex128
+    s128 = max(1, args.steps // 10) if not args.quick else 1
+    f128 = lambda: op.apply(psi128, out=y128)
+    tot128, per128, _ = timed(f128, s128, max(1, min(args.warmup, 3)))
+    op.sync_check()
+    ms128 = tot128 / s128
+
+    # --- accuracy at full size: c64c against c128 (checked against the FP64
+    # oracle on sampled rows in the test suite)
+    rel64 = float(torch.linalg.vector_norm(y64.to(torch.complex128) - y128)
+                  / torch.linalg.vector_norm(y128))
+
+    # --- end to end through the C-ABI host entry (pinned host buffers)
+    e2e = None
+    if not args.quick:
+        h_in = torch.empty(N, dtype=torch.complex64, pin_memory=True)
+        h_out = torch.empty(N, dtype=torch.complex64, pin_memory=True)
+        h_in.copy_(psi64.cpu())
+        a_in, a_out = h_in.numpy(), h_out.numpy()
+        for _ in range(max(3, min(args.warmup, 5))):
+            op.apply(a_in, out=a_out)
+        e_steps = max(3, args.steps // 5)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e_steps):
+            op.apply(a_in, out=a_out)
+        barrier()
+        e_ms = 1e3 * (time.perf_counter() - t0) / e_steps
+        if ws > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([e_ms], device=dev, dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e_ms = float(tt.item())
+        e2e = {"value": ws * T * N / (e_ms / 1e3), "unit": UNIT, "ms_per_step": e_ms,
+               "h2d_bytes_per_step": N * 8, "d2h_bytes_per_step": N * 8,
+               "path": "qr_apply_host (C ABI), pinned host buffers"}
+
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    hbm, peak_kind = peaks()
+    alg64 = (P + 1) * N * 8
+    alg128 = (P + 1) * N * 16
+    mean_launch64 = statistics.mean(per64) / 1e3
+    mean_launch128 = statistics.mean(per128) / 1e3
+    ach64 = alg64 / mean_launch64 / 1e9
+    ach128 = alg128 / mean_launch128 / 1e9
+    tr = ncu_traffic()
+    traffic = None
+    if tr and tr.get("workload") == desc:
+        traffic = tr.get("bytes_per_launch")
+    out = {
+        "metric": METRIC, "value": ws * T * N / (ms64 / 1e3), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms64,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64c (fp32 + two-sum)", "data": "synthetic",
+        "config": {"workload": desc, "n": n, "terms": T, "states_per_gpu": 1,
+                   "groups": int(info["ngroups"]), "merged_strings": int(info["nmerged"]),
+                   "partner_tiles_P": P, "tile_bits": int(info["tile_bits"]),
+                   "l2": "inputs 2^%d amplitudes (%d MiB c64) > L2 129 MB; no flush"
+                         % (n, (N * 8) >> 20),
+                   "parallelism": "replicas x%d" % ws},
+        "roofline": {"bound": "hbm", "achieved": ach64, "peak": hbm, "unit": "GB/s",
+                     "frac": ach64 / hbm, "traffic": traffic,
+                     "alg_bytes_per_launch": alg64,
+                     "alg_bytes_rule": "(P+1)*2^n*8, P=%d distinct x>>13" % P,
+                     "peak_source": peak_kind},
+        "c128": {"value": ws * T * N / (ms128 / 1e3), "ms_per_step": ms128, "steps": s128,
+                 "hbm_achieved_gbs": ach128, "hbm_frac": ach128 / hbm},
+        "speedup_c64c_vs_c128": ms128 / ms64,
+        "rel_err": {"c64c_vs_c128_full": rel64},
+        "e2e": e2e,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "device": torch.cuda.get_device_name(dev),
+    }
+    if not args.no_cpu and not args.quick and ws == 1:
+        nthreads = os.cpu_count() or 1
+        t_build, times = cpu_reference(t, args.cpu_rows, 4, nthreads)
+        ms_cpu = 1e3 * statistics.median(times[1:])
+        cpu_val = T * args.cpu_rows / (ms_cpu / 1e3)
+        out["cpu_baseline"] = {
+            "value": cpu_val, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": ("rows [0, %d) of 2^%d; CSR build %.2f s, CSR*vector %.1f ms (median of 3)"
+                       % (args.cpu_rows, n, t_build, ms_cpu))}
+    print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__,
+                                 formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["jw", "chain"], default="jw")
+    ap.add_argument("--n", type=int, default=26)
+    ap.add_argument("--pairs", type=int, default=8000)
+    ap.add_argument("--zterms", type=int, default=2000)
+    ap.add_argument("--cpu-rows", type=int, default=1 << 16,
+                    help="row sample of the CPU reference arm / baseline")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--quick", action="store_true",
+                    help="no clock sampling, e2e or CPU baseline (profiling runs)")
+    args = ap.parse_args()
+    if args.warmup < 3 and not args.quick:
+        raise SystemExit("--warmup must be >= 3")
+    if args.workload == "chain" and args.n == 26:
+        args.n = 22
+    t, desc = make_terms(args)
+    if args.impl == "reference":
+        run_reference_arm(args, t, desc)
+    else:
+        run_gpu_arm(args, t, desc)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,133 @@
+/*
+ * qrusty_gpu.h -- C ABI of the GB300 (sm_103a) Pauli-operator hot path.
+ *
+ * Drop-in boundary for qrusty's rowwise SparsePauliOp -> CSR construction
+ * and for the Pauli-sum product H*psi.  Plain pointers and sizes only; no
+ * CUDA, C++ or torch types appear in the signatures (streams are passed as
+ * `void*` holding a cudaStream_t, NULL = the legacy default stream).
+ *
+ * Conventions
+ *  - Every function returns QR_OK (0) or a negative QR_E* code and never
+ *    aborts; qr_last_error() returns the message of the calling thread's
+ *    last failure.
+ *  - Terms are (x, z, phase, coeff) exactly as qrusty's make_params consumes
+ *    them (qrusty/src/accel.rs:141-157): bit q of x is set for X/Y on qubit
+ *    q, bit q of z for Y/Z, phase = (base_phase + #Y) mod 4 with base_phase
+ *    from the label prefix (qrusty/src/lib.rs:125-181).  Matrix entry
+ *    (r, r ^ x) of a term is c' * (-1)^popcount(r & z) with
+ *    c' = (1, -i, -1, +i)[phase] * coeff.
+ *  - Complex numbers are interleaved (re, im): complex128 = 2 doubles,
+ *    complex64 = 2 floats.
+ *  - Device pointers are raw CUDA allocations on the device the operator
+ *    was created on.  Host pointers may be pageable or pinned.
+ *  - A handle must not be used by two host threads at once.
+ *  - Calls taking a stream are asynchronous with respect to the host unless
+ *    stated otherwise.
+ */
+#ifndef QRUSTY_GPU_H
+#define QRUSTY_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    QR_OK = 0,
+    QR_EINVAL = -1,   /* bad argument (sizes, masks, phase, null pointer)   */
+    QR_ECUDA = -2,    /* a CUDA runtime call failed                         */
+    QR_ENOMEM = -3,   /* device or host allocation failed                   */
+    QR_EKERNEL = -4,  /* a kernel reported an error (bounded wait expired)  */
+    QR_ESTATE = -5    /* wrong device / handle state                        */
+};
+
+enum { QR_MEM_DEVICE = 0, QR_MEM_HOST = 1 };
+
+/* Arithmetic of qr_apply: plain complex128, or complex64 amplitudes with
+ * FP32 arithmetic and compensated (two-sum) accumulation. */
+enum { QR_C128 = 0, QR_C64C = 1 };
+
+typedef struct qr_op qr_op;
+
+typedef struct {
+    int32_t n;            /* qubits                                        */
+    int32_t tile_bits;    /* amplitude-tile width used by qr_apply         */
+    uint64_t nterms;      /* input terms, in input order                   */
+    uint64_t ngroups;     /* distinct x masks (= nnz per CSR row)          */
+    uint64_t nmerged;     /* distinct (x, z) strings after FP64 merging    */
+    uint64_t nblocks;     /* distinct partner tiles x >> tile_bits         */
+    uint64_t nfat;        /* groups evaluated term by term in qr_apply     */
+    int32_t has_diag;     /* x = 0 group held as a precomputed diagonal    */
+    int32_t device;       /* CUDA device the operator lives on             */
+} qr_op_info;
+
+/* Create an operator from T terms (replaces SparsePauliOp::new,
+ * qrusty/src/lib.rs:354-376, plus make_params, qrusty/src/accel.rs:141-157).
+ * Validates 1 <= n <= 63, T >= 1, masks within n bits, phase <= 3.
+ * Uploads the term tables to the current CUDA device (synchronous). */
+int qr_op_create(int32_t n, uint64_t nterms, const uint64_t *x, const uint64_t *z,
+                 const uint8_t *phase, const double *coeff, qr_op **out);
+
+/* Release the operator and its device memory (synchronous). */
+int qr_op_destroy(qr_op *op);
+
+int qr_op_get_info(const qr_op *op, qr_op_info *info);
+
+/* CSR size of the operator's matrix (replaces the nnz pass of
+ * make_unsafe_vectors_chunked, qrusty/src/accel.rs:309-319):
+ * nrows = 2^n, nnz = nrows * ngroups. */
+int qr_csr_size(const qr_op *op, uint64_t *nrows, uint64_t *nnz);
+
+/* Fill caller-owned CSR arrays: indptr[nrows+1], indices[nnz],
+ * data[2*nnz] (complex128).  Replaces make_unsafe_vectors_chunked
+ * (qrusty/src/accel.rs:267-336) / to_matrix_rowwise_unsafe_chunked
+ * (qrusty/src/lib.rs:558-571): per row, columns r ^ x ascending, values
+ * summed over equal columns in input-term order, explicit zeros kept.
+ * mem = QR_MEM_DEVICE: device pointers, asynchronous on `stream`.
+ * mem = QR_MEM_HOST: host pointers; built on the device and copied back,
+ * synchronous. */
+int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data,
+                 int32_t mem, void *stream);
+
+/* y = H psi (adjoint = 0) or y = H^dagger psi (adjoint = 1) for nstates
+ * state vectors stored back to back (state s at offset s * 2^n).
+ * Replaces CSR build + spmat_dot_densevec (qrusty/src/accel.rs:338-370)
+ * with a matrix-free kernel.  dtype = QR_C128 (double2) or QR_C64C
+ * (float2).  psi and y are device pointers and must not overlap. */
+int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates,
+             int32_t adjoint, void *stream);
+
+/* Synchronise `stream` and report any error a kernel of this operator
+ * recorded on the device (e.g. an expired bounded wait).  The error word is
+ * cleared after it is reported. */
+int qr_check(qr_op *op, void *stream);
+
+/* As qr_apply with HOST psi / y: copies psi to the device, applies, copies
+ * y back (synchronous).  Device staging buffers are owned by the operator
+ * and reused across calls. */
+int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host,
+                  int32_t nstates, int32_t adjoint);
+
+/* y = A v for a CSR matrix given by device arrays (replaces
+ * spmat_dot_densevec, qrusty/src/accel.rs:338-370, and its binding
+ * pyqrusty/src/lib.rs:476-491).  complex128; each row's products are summed
+ * by one warp (lane-strided partial sums, then a butterfly), so the result
+ * matches a storage-order sum to rounding, not bit for bit. */
+int qr_csr_spmv(uint64_t nrows, const uint64_t *indptr, const uint64_t *indices,
+                const double *data, const double *v, double *y, void *stream);
+
+/* Message of the calling thread's last failure ("" if none).  Copies at
+ * most len-1 bytes plus a terminating NUL; returns the full length. */
+int qr_last_error(char *buf, size_t len);
+
+/* Number of kernel launches this library has issued in the process (for
+ * launch accounting by callers and benchmarks). */
+uint64_t qr_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QRUSTY_GPU_H */

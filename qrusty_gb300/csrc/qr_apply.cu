@@ -1,0 +1,428 @@
+// qr_apply.cu -- matrix-free Pauli-sum product y = H psi on sm_103a.
+//
+// Replaces "build the CSR, then spmat_dot_densevec" of qrusty
+// (qrusty/src/accel.rs:171-210 row semantics, :338-370 SpMV): row r of H has
+// one entry per distinct x mask g, at column r ^ x_g, with value
+// D_g(r) = sum_{k in g} c'_k (-1)^popc(r & z_k).  So
+//     y[r] = sum_g D_g(r) * psi[r ^ x_g].
+//
+// Layout and schedule.  The state is cut into tiles of 2^b contiguous
+// amplitudes.  Output tile q needs, for every group g, the partner tile
+// q ^ (x_g >> b), permuted inside by XOR with lo_g = x_g & (2^b - 1).  Groups
+// are bucketed by partner tile ("blocks"); a persistent CTA walks its output
+// tiles and, per tile, every block: the partner tile is staged into shared
+// memory by a 1-D TMA bulk copy (cp.async.bulk + mbarrier, STAGES-deep ring)
+// and all groups of the block are applied from shared memory.  Thread t of
+// the CTA owns amplitudes r_lo = t + threads * m, m < AMPS, so a warp's XOR
+// partners stay inside one aligned 32-element run (conflict-free LDS).
+//
+// Diagonal factor per group: D_g(r) = (-1)^popc(r & z0) * T_g[pi(r)], with
+// pi(r) the parities of r against a GF(2) basis of the group's z
+// differences (rank d <= kDMax, table of 2^d entries precomputed in FP64 on
+// the host).  The parities split into a per-thread constant and a per-m part
+// read from a 32-entry Walsh table, so the common case costs one sign select
+// per amplitude.  The x = 0 group with a large z span is a precomputed
+// diagonal vector (FP64 Walsh-Hadamard transform per tile, diag_wht below).
+//
+// Precision.  QR_C128: double2 amplitudes, FP64 arithmetic.  QR_C64C: float2
+// amplitudes, FP32 products, each block's contributions summed in FP32 and
+// folded into the row's running sum with a two-sum (error-free transform):
+// the running value is an unevaluated (hi + lo) pair per component.
+#include "qr_common.cuh"
+
+namespace qr {
+
+// Walsh words: bit m of walsh_word(v) is popc(m & v) & 1, for m, v < 32.
+constexpr uint32_t walsh_word(uint32_t v) {
+    uint32_t w = 0;
+    for (uint32_t m = 0; m < 32; ++m) {
+        uint32_t x = m & v, p = 0;
+        while (x) { p ^= x & 1u; x >>= 1; }
+        if (p) w |= 1u << m;
+    }
+    return w;
+}
+__constant__ uint32_t c_walsh[32] = {
+    walsh_word(0),  walsh_word(1),  walsh_word(2),  walsh_word(3),  walsh_word(4),
+    walsh_word(5),  walsh_word(6),  walsh_word(7),  walsh_word(8),  walsh_word(9),
+    walsh_word(10), walsh_word(11), walsh_word(12), walsh_word(13), walsh_word(14),
+    walsh_word(15), walsh_word(16), walsh_word(17), walsh_word(18), walsh_word(19),
+    walsh_word(20), walsh_word(21), walsh_word(22), walsh_word(23), walsh_word(24),
+    walsh_word(25), walsh_word(26), walsh_word(27), walsh_word(28), walsh_word(29),
+    walsh_word(30), walsh_word(31)};
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t saddr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(saddr(dst)),
+        "l"(src), "r"(bytes), "r"(saddr(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(saddr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t gtimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait: gives up after ~limit_ns and reports false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = gtimer_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (gtimer_ns() - t0 > limit_ns) return false;
+    }
+    return true;
+}
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per stage
+constexpr int kMaxStages = 4;
+
+// ---------------------------------------------------------------- arithmetic
+template <typename Real>
+__device__ __forceinline__ void cmac(Cplx<Real> &acc, const Cplx<Real> &d, const Cplx<Real> &p) {
+    acc.re = fma(d.re, p.re, fma(-d.im, p.im, acc.re));
+    acc.im = fma(d.re, p.im, fma(d.im, p.re, acc.im));
+}
+__device__ __forceinline__ void two_sum_into(float &hi, float &lo, float b) {
+    const float s = __fadd_rn(hi, b);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+template <typename Real>
+__device__ __forceinline__ Cplx<Real> cneg_if(const Cplx<Real> &d, uint32_t s) {
+    Cplx<Real> r;
+    r.re = s ? -d.re : d.re;
+    r.im = s ? -d.im : d.im;
+    return r;
+}
+
+// ---------------------------------------------------------------- apply kernel
+// Real = float (compensated) or double (plain).  AMPS amplitudes per thread.
+template <typename Real, int AMPS, bool COMP>
+__global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyArgs a, int stages) {
+    using C = Cplx<Real>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const uint32_t threads = blockDim.x;
+    const uint32_t t = threadIdx.x;
+    const uint32_t tile = 1u << a.b;
+    const uint32_t tile_bytes = tile * (uint32_t)sizeof(C);
+    C *bufs = reinterpret_cast<C *>(smem_raw);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)stages * tile_bytes);
+
+    const C *psi = static_cast<const C *>(a.psi);
+    C *y = static_cast<C *>(a.y);
+    const C *tables = static_cast<const C *>(a.tables);
+    const C *fat_c = static_cast<const C *>(a.fat_c);
+    const C *diag = static_cast<const C *>(a.diag);
+    const uint32_t nb = a.nblocks;
+
+    const uint64_t first = blockIdx.x;
+    const uint64_t my_items =
+        a.nitems > first ? (a.nitems - first + gridDim.x - 1) / gridDim.x : 0;
+    const uint64_t total = my_items * nb;
+    if (total == 0) return;
+
+    if (t == 0) {
+        for (int s = 0; s < stages; ++s) mbar_init(&full[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](uint64_t L) {
+        const uint64_t k = L / nb;
+        const uint32_t j = (uint32_t)(L - k * nb);
+        const uint64_t item = first + k * gridDim.x;
+        const uint64_t st = item / a.ntiles;
+        const uint64_t q = item - st * a.ntiles;
+        const uint64_t src_tile = q ^ a.blk_hi[j];
+        const C *src = psi + st * a.N + (src_tile << a.b);
+        const int s = (int)(L % (uint64_t)stages);
+        mbar_expect_tx(&full[s], tile_bytes);
+        bulk_g2s(bufs + (size_t)s * tile, src, tile_bytes, &full[s]);
+    };
+    if (t == 0) {
+        const uint64_t pro = total < (uint64_t)stages ? total : (uint64_t)stages;
+        for (uint64_t L = 0; L < pro; ++L) issue(L);
+    }
+
+    C acc[AMPS];
+    C lo_acc[AMPS];
+    C bacc[AMPS];
+    const uint32_t amask = AMPS - 1;
+
+    for (uint64_t L = 0; L < total; ++L) {
+        const uint64_t k = L / nb;
+        const uint32_t j = (uint32_t)(L - k * nb);
+        const uint64_t item = first + k * gridDim.x;
+        const uint64_t st = item / a.ntiles;
+        const uint64_t q = item - st * a.ntiles;
+        const uint64_t rbase = (q << a.b) | t;
+        if (j == 0) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                acc[m].re = acc[m].im = Real(0);
+                lo_acc[m].re = lo_acc[m].im = Real(0);
+            }
+        }
+        const int s = (int)(L % (uint64_t)stages);
+        const uint32_t par = (uint32_t)((L / (uint64_t)stages) & 1ull);
+        const bool ok = mbar_wait_bounded(&full[s], par, kWaitLimitNs);
+        const C *buf = bufs + (size_t)s * tile;
+
+        if constexpr (COMP) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) bacc[m].re = bacc[m].im = Real(0);
+        }
+        C *tgt = COMP ? bacc : acc;
+
+        if ((int)j == a.diag_block && diag != nullptr) {
+            const C *dg = diag + (q << a.b);
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const uint32_t rl = t + threads * (uint32_t)m;
+                cmac(tgt[m], dg[rl], buf[rl]);
+            }
+        }
+
+        const uint32_t g1 = a.blk_g0[j + 1];
+        for (uint32_t g = a.blk_g0[j]; g < g1; ++g) {
+            const GroupDesc gd = a.groups[g];
+            const uint32_t lo_t = gd.lo & (threads - 1);
+            const uint32_t lo_m = gd.lo >> a.tb;
+            const C *src = buf + (t ^ lo_t);
+            if (gd.d != kFat) {
+                const uint32_t s0 = (uint32_t)__popcll(rbase & gd.z0) & 1u;
+                const uint32_t W0 = c_walsh[(gd.z0 >> a.tb) & amask];
+                uint32_t u = 0, anyW = 0;
+                uint32_t W[kDMax];
+#pragma unroll
+                for (int i = 0; i < kDMax; ++i) {
+                    W[i] = 0;
+                    if (i < (int)gd.d) {
+                        u |= ((uint32_t)__popcll(rbase & gd.beta[i]) & 1u) << i;
+                        W[i] = c_walsh[(gd.beta[i] >> a.tb) & amask];
+                        anyW |= W[i];
+                    }
+                }
+                if (anyW == 0) {
+                    const C D = tables[gd.off + u];
+                    C Dn;
+                    Dn.re = -D.re;
+                    Dn.im = -D.im;
+#pragma unroll
+                    for (int m = 0; m < AMPS; ++m) {
+                        const C p = src[((uint32_t)m ^ lo_m) << a.tb];
+                        const uint32_t sg = ((W0 >> m) ^ s0) & 1u;
+                        C Dm;
+                        Dm.re = sg ? Dn.re : D.re;
+                        Dm.im = sg ? Dn.im : D.im;
+                        cmac(tgt[m], Dm, p);
+                    }
+                } else {
+#pragma unroll
+                    for (int m = 0; m < AMPS; ++m) {
+                        uint32_t um = u;
+#pragma unroll
+                        for (int i = 0; i < kDMax; ++i) um ^= ((W[i] >> m) & 1u) << i;
+                        const C D = tables[gd.off + um];
+                        const C p = src[((uint32_t)m ^ lo_m) << a.tb];
+                        const uint32_t sg = ((W0 >> m) ^ s0) & 1u;
+                        cmac(tgt[m], cneg_if(D, sg), p);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int m = 0; m < AMPS; ++m) {
+                    const uint64_t r = rbase | ((uint64_t)m << a.tb);
+                    C D;
+                    D.re = D.im = Real(0);
+                    for (uint32_t kk = 0; kk < gd.cnt; ++kk) {
+                        const uint64_t zk = a.fat_z[gd.off + kk];
+                        const C ck = fat_c[gd.off + kk];
+                        const uint32_t sg = (uint32_t)__popcll(r & zk) & 1u;
+                        D.re += sg ? -ck.re : ck.re;
+                        D.im += sg ? -ck.im : ck.im;
+                    }
+                    const C p = src[((uint32_t)m ^ lo_m) << a.tb];
+                    cmac(tgt[m], D, p);
+                }
+            }
+        }
+
+        if constexpr (COMP) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                two_sum_into(acc[m].re, lo_acc[m].re, bacc[m].re);
+                two_sum_into(acc[m].im, lo_acc[m].im, bacc[m].im);
+            }
+        }
+
+        if (j == nb - 1) {
+            C *yo = y + st * a.N + (q << a.b);
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                C o;
+                if constexpr (COMP) {
+                    o.re = acc[m].re + lo_acc[m].re;
+                    o.im = acc[m].im + lo_acc[m].im;
+                } else {
+                    o = acc[m];
+                }
+                yo[t + threads * (uint32_t)m] = o;
+            }
+        }
+
+        // All threads are done with stage s (and agree on the wait outcome).
+        if (__syncthreads_or(ok ? 0 : 1)) {
+            if (t == 0) {
+                atomicExch(a.err, kErrMbarTimeout);
+                // Drain copies still in flight into this CTA's stages.
+                for (uint64_t L2 = L; L2 < total && L2 < L + (uint64_t)stages; ++L2) {
+                    const int s2 = (int)(L2 % (uint64_t)stages);
+                    mbar_wait_bounded(&full[s2], (uint32_t)((L2 / stages) & 1ull), kWaitLimitNs);
+                }
+            }
+            return;
+        }
+        if (t == 0 && L + (uint64_t)stages < total) issue(L + (uint64_t)stages);
+    }
+}
+
+template <typename Real, int AMPS, bool COMP>
+static cudaError_t launch_one(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
+    const uint32_t tile_bytes = (1u << a.b) * (uint32_t)sizeof(Cplx<Real>);
+    int stages = (int)((200u * 1024u) / tile_bytes);
+    if (stages > kMaxStages) stages = kMaxStages;
+    if (stages < 2) stages = 2;
+    const size_t smem = (size_t)stages * tile_bytes + kMaxStages * sizeof(uint64_t);
+    auto kern = apply_tiled<Real, AMPS, COMP>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    uint64_t grid = a.nitems < (uint64_t)nsm ? a.nitems : (uint64_t)nsm;
+    if (grid == 0) return cudaSuccess;
+    kern<<<(unsigned)grid, threads, smem, st>>>(a, stages);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename Real, bool COMP>
+static cudaError_t dispatch_amps(const ApplyArgs &a, int amps, int threads, int nsm,
+                                 cudaStream_t st) {
+    switch (amps) {
+        case 1: return launch_one<Real, 1, COMP>(a, threads, nsm, st);
+        case 2: return launch_one<Real, 2, COMP>(a, threads, nsm, st);
+        case 4: return launch_one<Real, 4, COMP>(a, threads, nsm, st);
+        case 8: return launch_one<Real, 8, COMP>(a, threads, nsm, st);
+        case 16: return launch_one<Real, 16, COMP>(a, threads, nsm, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_apply(int dtype, const ApplyArgs &a, int amps, int threads, int nsm,
+                         cudaStream_t st) {
+    if (dtype == 0) return dispatch_amps<double, false>(a, amps, threads, nsm, st);
+    return dispatch_amps<float, true>(a, amps, threads, nsm, st);
+}
+
+// ---------------------------------------------------------------- diagonal
+// D0[r] = sum_k c'_k (-1)^popc(r & z_k) over the x = 0 group, in FP64: per
+// tile of 2^db amplitudes, fold the tile-index bits of z_k into a sign, sum
+// each distinct low-bit pattern z_k & (2^db - 1) into a bin (terms of a bin
+// in input order), then an in-place Walsh-Hadamard transform over db bits.
+__global__ void __launch_bounds__(256) diag_wht(int db, uint64_t ntiles, const uint64_t *bin_zlo,
+                                                const uint32_t *bin_off, uint32_t nbins,
+                                                const uint64_t *tz, const double *tc, void *out,
+                                                int out_f32) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    double2 *W = reinterpret_cast<double2 *>(smem_raw);
+    const uint32_t sz = 1u << db;
+    for (uint64_t q = blockIdx.x; q < ntiles; q += gridDim.x) {
+        for (uint32_t i = threadIdx.x; i < sz; i += blockDim.x) W[i] = make_double2(0.0, 0.0);
+        __syncthreads();
+        const uint64_t qhi = q << db;
+        for (uint32_t bi = threadIdx.x; bi < nbins; bi += blockDim.x) {
+            double wr = 0.0, wi = 0.0;
+            for (uint32_t k = bin_off[bi]; k < bin_off[bi + 1]; ++k) {
+                const bool neg = (__popcll(qhi & tz[k]) & 1) != 0;
+                const double cr = tc[2 * k], ci = tc[2 * k + 1];
+                if (k == bin_off[bi]) {
+                    wr = neg ? -cr : cr;
+                    wi = neg ? -ci : ci;
+                } else {
+                    wr = neg ? wr - cr : wr + cr;
+                    wi = neg ? wi - ci : wi + ci;
+                }
+            }
+            W[bin_zlo[bi]] = make_double2(wr, wi);
+        }
+        __syncthreads();
+        for (int l = 0; l < db; ++l) {
+            const uint32_t h = 1u << l;
+            for (uint32_t i = threadIdx.x; i < sz / 2; i += blockDim.x) {
+                const uint32_t ia = ((i >> l) << (l + 1)) | (i & (h - 1));
+                const uint32_t ib = ia | h;
+                const double2 u = W[ia], v = W[ib];
+                W[ia] = make_double2(u.x + v.x, u.y + v.y);
+                W[ib] = make_double2(u.x - v.x, u.y - v.y);
+            }
+            __syncthreads();
+        }
+        if (out_f32) {
+            float2 *o = static_cast<float2 *>(out) + qhi;
+            for (uint32_t i = threadIdx.x; i < sz; i += blockDim.x)
+                o[i] = make_float2((float)W[i].x, (float)W[i].y);
+        } else {
+            double2 *o = static_cast<double2 *>(out) + qhi;
+            for (uint32_t i = threadIdx.x; i < sz; i += blockDim.x) o[i] = W[i];
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_diag(int dtype, int n, int db, uint64_t ntiles, const uint64_t *bin_zlo,
+                        const uint32_t *bin_off, uint32_t nbins, const uint64_t *tz,
+                        const double *tc, void *out, cudaStream_t st) {
+    (void)n;
+    const size_t smem = ((size_t)1 << db) * sizeof(double2);
+    cudaError_t e = cudaFuncSetAttribute(diag_wht, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)(ntiles < 4096 ? ntiles : 4096);
+    diag_wht<<<grid, 256, smem, st>>>(db, ntiles, bin_zlo, bin_off, nbins, tz, tc, out,
+                                      dtype == 1);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace qr

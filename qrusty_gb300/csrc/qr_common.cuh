@@ -1,0 +1,86 @@
+// qr_common.cuh -- internal types shared by the host layer and the kernels
+// of libqrusty_gpu (not part of the public C ABI in include/qrusty_gpu.h).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace qr {
+
+// Largest rank of a group's z-difference span that qr_apply evaluates with
+// a 2^d-entry table; groups above it are evaluated term by term ("fat").
+constexpr int kDMax = 4;
+constexpr uint32_t kFat = 0xffffffffu;
+
+// One x-group of the apply plan.  All terms of the group share the x mask;
+// their z masks are z0 ^ delta_k with delta_k in span(beta[0..d)).  The
+// group's diagonal factor at row r is
+//   D(r) = (-1)^popc(r & z0) * table[off + pi(r)],  pi(r)_i = popc(r & beta_i) & 1.
+// Fat groups (d == kFat) list their cnt terms at fat_z/fat_c[off ...].
+struct alignas(16) GroupDesc {
+    uint64_t z0;
+    uint64_t beta[kDMax];
+    uint32_t lo;    // x & (tile - 1): XOR partner inside the partner tile
+    uint32_t d;     // rank, or kFat
+    uint32_t off;   // table offset (entries) or fat-term offset
+    uint32_t cnt;   // fat-term count
+};
+
+template <typename Real> struct Cplx;
+template <> struct alignas(8) Cplx<float> { float re, im; };
+template <> struct alignas(16) Cplx<double> { double re, im; };
+
+struct ApplyArgs {
+    const void *psi;
+    void *y;
+    uint64_t N;             // 2^n amplitudes per state
+    int n;
+    int b;                  // tile bits
+    int tb;                 // log2(threads)
+    int nstates;
+    uint64_t ntiles;        // N >> b
+    uint64_t nitems;        // nstates * ntiles
+    const GroupDesc *groups;
+    const void *tables;     // Cplx<Real>
+    const uint64_t *fat_z;
+    const void *fat_c;      // Cplx<Real>
+    const uint64_t *blk_hi; // partner-tile XOR per block
+    const uint32_t *blk_g0; // groups of block j: [blk_g0[j], blk_g0[j+1])
+    uint32_t nblocks;
+    const void *diag;       // Cplx<Real>[N] or null (only read in block hi == 0)
+    int diag_block;         // index of the hi == 0 block, or -1
+    int *err;               // device error word
+};
+
+// Device error codes written to the error word.
+enum : int { kErrNone = 0, kErrMbarTimeout = 1 };
+
+// Per-process launch counter (all launches issued through this library).
+void count_launch(uint64_t k = 1);
+
+// Kernel launchers (qr_apply.cu / qr_csr.cu).
+cudaError_t launch_apply(int dtype, const ApplyArgs &a, int amps, int threads, int nsm,
+                         cudaStream_t st);
+cudaError_t launch_diag(int dtype, int n, int db, uint64_t ntiles, const uint64_t *bin_zlo,
+                        const uint32_t *bin_off, uint32_t nbins, const uint64_t *tz,
+                        const double *tc, void *out, cudaStream_t st);
+
+struct CsrArgs {
+    uint64_t N, G;
+    const uint64_t *gx;       // G, ascending
+    const uint32_t *goff;     // G+1
+    const uint64_t *tz;       // terms in group-stable order
+    const double *tc;         // 2 doubles per term
+    const uint32_t *eoff;     // G+1: trie entries per group
+    const uint8_t *ebit;
+    const int64_t *esig;
+    uint64_t *indptr, *indices;
+    double *data;
+    uint64_t row0, nrows;     // rows to fill
+};
+cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st);
+cudaError_t launch_csr_spmv(uint64_t nrows, const uint64_t *indptr, const uint64_t *indices,
+                            const double *data, const double *v, double *y, int nsm,
+                            cudaStream_t st);
+
+}  // namespace qr

@@ -1,0 +1,737 @@
+// qr_host.cu -- C ABI of libqrusty_gpu (declared in include/qrusty_gpu.h).
+//
+// Host half of the GB300 Pauli-operator hot path: validates the terms,
+// computes c'_k in FP64, groups the terms by x mask, prepares the CSR and
+// apply tables, owns the operator's device memory and launches the kernels
+// of qr_csr.cu / qr_apply.cu.  No CPU fallback exists: every numeric result
+// is computed on the GPU.
+//
+// Compiled with -ffp-contract=off: c'_k = m(phase) * c_k must round exactly
+// as num-complex's (ar*br - ai*bi, ar*bi + ai*br) does in qrusty's
+// make_params (qrusty/src/accel.rs:141-157).
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "../../include/qrusty_gpu.h"
+#include "qr_common.cuh"
+
+namespace qr {
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launch(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+static int cuda_fail(cudaError_t e, const char *what) {
+    return fail(QR_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define QR_CUDA(call, what)                          \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+struct cd {
+    double re, im;
+};
+
+// Device buffer with RAII release.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t alloc(size_t b) {
+        release();
+        if (b == 0) b = 16;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        else p = nullptr;
+        return e;
+    }
+    template <typename T>
+    cudaError_t upload(const std::vector<T> &v) {
+        cudaError_t e = alloc(v.size() * sizeof(T));
+        if (e != cudaSuccess) return e;
+        if (!v.empty()) e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+        return e;
+    }
+    template <typename T>
+    T *as() const { return static_cast<T *>(p); }
+};
+
+struct Plan {
+    bool built = false;
+    int b = 0, tb = 0, threads = 0, amps = 0;
+    uint32_t nblocks = 0;
+    uint64_t ngroups = 0, nfat = 0;
+    int diag_block = -1;
+    bool has_diag = false;
+    DevBuf groups, tables, fat_z, fat_c, blk_hi, blk_g0, diag;
+};
+
+}  // namespace qr
+
+using namespace qr;
+
+struct qr_op {
+    int n = 0;
+    uint64_t N = 0, T = 0;
+    int device = 0;
+    int nsm = 0;
+    // input terms (input order)
+    std::vector<uint64_t> x, z;
+    std::vector<cd> cp;  // c'_k
+    // CSR tables: groups by x ascending, terms stable within group
+    uint64_t G = 0;
+    std::vector<uint64_t> gx;
+    std::vector<uint32_t> goff;
+    std::vector<uint64_t> tz;
+    std::vector<cd> tc;
+    std::vector<uint32_t> eoff;
+    std::vector<uint8_t> ebit;
+    std::vector<int64_t> esig;
+    bool csr_uploaded = false;
+    DevBuf d_gx, d_goff, d_tz, d_tc, d_eoff, d_ebit, d_esig;
+    // merged terms (FP64 simplification) for qr_apply
+    std::vector<uint64_t> mx, mz;
+    std::vector<cd> mc;
+    Plan plans[2][2];  // [dtype][adjoint]
+    DevBuf d_err;
+    // host-call staging
+    cudaStream_t hstream = nullptr;
+    DevBuf stage_in, stage_out;
+};
+
+namespace {
+
+// ---------------------------------------------------------------- CSR trie
+// Recursive split of the ascending x masks [lo, hi) at bit `bit`: records,
+// for every element, its sibling-subtree size at each branching bit.
+void build_trie(const std::vector<uint64_t> &gx, size_t lo, size_t hi, int bit,
+                std::vector<std::vector<std::pair<uint8_t, int64_t>>> &ent) {
+    while (bit >= 0 && hi - lo > 1) {
+        const uint64_t m = 1ull << bit;
+        // first index in [lo, hi) with bit set (sorted ascending, common prefix above bit)
+        size_t mid = lo;
+        while (mid < hi && !(gx[mid] & m)) ++mid;
+        if (mid > lo && mid < hi) {
+            const int64_t s0 = (int64_t)(mid - lo), s1 = (int64_t)(hi - mid);
+            for (size_t i = lo; i < mid; ++i) ent[i].push_back({(uint8_t)bit, +s1});
+            for (size_t i = mid; i < hi; ++i) ent[i].push_back({(uint8_t)bit, -s0});
+            build_trie(gx, lo, mid, bit - 1, ent);
+            lo = mid;  // continue with the 1-side iteratively
+        }
+        --bit;
+    }
+}
+
+int prepare_csr_tables(qr_op *op) {
+    const uint64_t T = op->T;
+    std::vector<uint64_t> order(T);
+    for (uint64_t k = 0; k < T; ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint64_t a, uint64_t b) { return op->x[a] < op->x[b]; });
+    op->gx.clear();
+    op->goff.clear();
+    op->tz.resize(T);
+    op->tc.resize(T);
+    for (uint64_t i = 0; i < T; ++i) {
+        const uint64_t k = order[i];
+        if (i == 0 || op->x[k] != op->gx.back()) {
+            op->gx.push_back(op->x[k]);
+            op->goff.push_back((uint32_t)i);
+        }
+        op->tz[i] = op->z[k];
+        op->tc[i] = op->cp[k];
+    }
+    op->goff.push_back((uint32_t)T);
+    op->G = op->gx.size();
+    std::vector<std::vector<std::pair<uint8_t, int64_t>>> ent(op->G);
+    build_trie(op->gx, 0, op->G, op->n - 1, ent);
+    op->eoff.assign(1, 0);
+    op->ebit.clear();
+    op->esig.clear();
+    for (uint64_t g = 0; g < op->G; ++g) {
+        for (auto &e : ent[g]) {
+            op->ebit.push_back(e.first);
+            op->esig.push_back(e.second);
+        }
+        op->eoff.push_back((uint32_t)op->ebit.size());
+    }
+    return QR_OK;
+}
+
+int upload_csr_tables(qr_op *op) {
+    if (op->csr_uploaded) return QR_OK;
+    QR_CUDA(op->d_gx.upload(op->gx), "upload gx");
+    QR_CUDA(op->d_goff.upload(op->goff), "upload goff");
+    QR_CUDA(op->d_tz.upload(op->tz), "upload tz");
+    QR_CUDA(op->d_tc.upload(op->tc), "upload tc");
+    QR_CUDA(op->d_eoff.upload(op->eoff), "upload eoff");
+    QR_CUDA(op->d_ebit.upload(op->ebit), "upload ebit");
+    QR_CUDA(op->d_esig.upload(op->esig), "upload esig");
+    op->csr_uploaded = true;
+    return QR_OK;
+}
+
+// ---------------------------------------------------------------- merging
+void merge_terms(qr_op *op) {
+    struct H {
+        size_t operator()(const std::pair<uint64_t, uint64_t> &p) const {
+            return std::hash<uint64_t>()(p.first * 0x9E3779B97F4A7C15ull ^ p.second);
+        }
+    };
+    std::unordered_map<std::pair<uint64_t, uint64_t>, size_t, H> idx;
+    idx.reserve(op->T * 2);
+    op->mx.clear();
+    op->mz.clear();
+    op->mc.clear();
+    for (uint64_t k = 0; k < op->T; ++k) {
+        auto key = std::make_pair(op->x[k], op->z[k]);
+        auto it = idx.find(key);
+        if (it == idx.end()) {
+            idx.emplace(key, op->mx.size());
+            op->mx.push_back(op->x[k]);
+            op->mz.push_back(op->z[k]);
+            op->mc.push_back(op->cp[k]);
+        } else {
+            cd &c = op->mc[it->second];
+            c.re += op->cp[k].re;
+            c.im += op->cp[k].im;
+        }
+    }
+}
+
+// GF(2) span of the z differences of one group: basis (pivot = msb, unique)
+// and the coordinates of every term's difference in that basis.
+struct Span {
+    std::vector<uint64_t> basis;
+    std::vector<uint32_t> coord;  // per term
+    bool overflow = false;
+};
+Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
+    Span sp;
+    const uint64_t z0 = zs[0];
+    sp.coord.resize(zs.size());
+    for (size_t k = 0; k < zs.size(); ++k) {
+        uint64_t v = zs[k] ^ z0;
+        uint32_t c = 0;
+        // basis kept in order of insertion; reduce by descending pivot
+        std::vector<size_t> ord(sp.basis.size());
+        for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+        std::sort(ord.begin(), ord.end(),
+                  [&](size_t a, size_t b) { return sp.basis[a] > sp.basis[b]; });
+        for (size_t i : ord) {
+            const uint64_t bv = sp.basis[i];
+            const int piv = 63 - __builtin_clzll(bv);
+            if ((v >> piv) & 1ull) {
+                v ^= bv;
+                c |= 1u << i;
+            }
+        }
+        if (v != 0) {
+            if (sp.basis.size() >= dmax) {
+                sp.overflow = true;
+                return sp;
+            }
+            c |= 1u << sp.basis.size();
+            sp.basis.push_back(v);
+        }
+        sp.coord[k] = c;
+    }
+    return sp;
+}
+
+template <typename Real>
+void push_cplx(std::vector<unsigned char> &buf, cd v) {
+    Cplx<Real> c;
+    c.re = (Real)v.re;
+    c.im = (Real)v.im;
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(&c);
+    buf.insert(buf.end(), p, p + sizeof(c));
+}
+
+int build_plan(qr_op *op, int dtype, int adjoint) {
+    Plan &pl = op->plans[dtype][adjoint];
+    if (pl.built) return QR_OK;
+    if (op->mx.empty()) merge_terms(op);
+    const int n = op->n;
+    const bool f32 = dtype == QR_C64C;
+    pl.b = std::min(n, f32 ? 13 : 12);
+    const int tmax = f32 ? 512 : 256;
+    pl.threads = std::min(1 << pl.b, tmax);
+    pl.amps = (1 << pl.b) / pl.threads;
+    pl.tb = 0;
+    while ((1 << pl.tb) < pl.threads) ++pl.tb;
+    const uint64_t tmask = (1ull << pl.b) - 1;
+
+    // coefficients of this plan (adjoint: conj(c) * (-1)^popc(x & z))
+    const size_t M = op->mx.size();
+    std::vector<cd> c(M);
+    for (size_t k = 0; k < M; ++k) {
+        c[k] = op->mc[k];
+        if (adjoint) {
+            c[k].im = -c[k].im;
+            if (__builtin_popcountll(op->mx[k] & op->mz[k]) & 1) {
+                c[k].re = -c[k].re;
+                c[k].im = -c[k].im;
+            }
+        }
+    }
+    // groups by x in first-occurrence order
+    std::vector<uint64_t> gxs;
+    std::unordered_map<uint64_t, size_t> gid;
+    std::vector<std::vector<size_t>> members;
+    for (size_t k = 0; k < M; ++k) {
+        auto it = gid.find(op->mx[k]);
+        if (it == gid.end()) {
+            gid.emplace(op->mx[k], gxs.size());
+            gxs.push_back(op->mx[k]);
+            members.emplace_back();
+            members.back().push_back(k);
+        } else {
+            members[it->second].push_back(k);
+        }
+    }
+    // diagonal group
+    std::vector<size_t> diag_terms;
+    std::vector<GroupDesc> descs;
+    std::vector<uint64_t> desc_hi;
+    std::vector<unsigned char> tab;
+    std::vector<uint64_t> fz;
+    std::vector<unsigned char> fc;
+    uint32_t ntab = 0, nfat_terms = 0;
+    for (size_t g = 0; g < gxs.size(); ++g) {
+        std::vector<uint64_t> zs;
+        for (size_t k : members[g]) zs.push_back(op->mz[k]);
+        Span sp = gf2_span(zs, kDMax);
+        if (gxs[g] == 0 && sp.overflow) {
+            diag_terms = members[g];
+            continue;
+        }
+        GroupDesc d;
+        memset(&d, 0, sizeof(d));
+        d.z0 = zs[0];
+        d.lo = (uint32_t)(gxs[g] & tmask);
+        if (!sp.overflow) {
+            d.d = (uint32_t)sp.basis.size();
+            for (size_t i = 0; i < sp.basis.size(); ++i) d.beta[i] = sp.basis[i];
+            d.off = ntab;
+            const uint32_t ent = 1u << d.d;
+            for (uint32_t u = 0; u < ent; ++u) {
+                cd s{0.0, 0.0};
+                for (size_t kk = 0; kk < members[g].size(); ++kk) {
+                    const cd v = c[members[g][kk]];
+                    if (__builtin_popcount(u & sp.coord[kk]) & 1) {
+                        s.re -= v.re;
+                        s.im -= v.im;
+                    } else {
+                        s.re += v.re;
+                        s.im += v.im;
+                    }
+                }
+                if (f32) push_cplx<float>(tab, s);
+                else push_cplx<double>(tab, s);
+            }
+            ntab += ent;
+        } else {
+            d.d = kFat;
+            d.off = nfat_terms;
+            d.cnt = (uint32_t)members[g].size();
+            for (size_t k : members[g]) {
+                fz.push_back(op->mz[k]);
+                if (f32) push_cplx<float>(fc, c[k]);
+                else push_cplx<double>(fc, c[k]);
+            }
+            nfat_terms += d.cnt;
+            pl.nfat++;
+        }
+        descs.push_back(d);
+        desc_hi.push_back(gxs[g] >> pl.b);
+    }
+    pl.has_diag = !diag_terms.empty();
+    // blocks: distinct partner-tile XOR values, ascending; a hi == 0 block
+    // always exists when the diagonal vector is used
+    std::vector<size_t> ord(descs.size());
+    for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](size_t a, size_t b) { return desc_hi[a] < desc_hi[b]; });
+    std::vector<GroupDesc> sdesc;
+    std::vector<uint64_t> bhi;
+    std::vector<uint32_t> bg0;
+    if (pl.has_diag && (ord.empty() || desc_hi[ord[0]] != 0)) {
+        bhi.push_back(0);
+        bg0.push_back(0);
+    }
+    for (size_t i : ord) {
+        const uint64_t h = desc_hi[i];
+        if (bhi.empty() || bhi.back() != h) {
+            bhi.push_back(h);
+            bg0.push_back((uint32_t)sdesc.size());
+        }
+        sdesc.push_back(descs[i]);
+    }
+    bg0.push_back((uint32_t)sdesc.size());
+    pl.nblocks = (uint32_t)bhi.size();
+    pl.ngroups = sdesc.size();
+    pl.diag_block = -1;
+    for (size_t j = 0; j < bhi.size(); ++j)
+        if (bhi[j] == 0) pl.diag_block = (int)j;
+    if (sdesc.empty()) sdesc.push_back(GroupDesc{});  // keep a valid pointer
+
+    QR_CUDA(pl.groups.upload(sdesc), "upload groups");
+    QR_CUDA(pl.tables.upload(tab), "upload tables");
+    QR_CUDA(pl.fat_z.upload(fz), "upload fat z");
+    QR_CUDA(pl.fat_c.upload(fc), "upload fat c");
+    QR_CUDA(pl.blk_hi.upload(bhi), "upload blocks");
+    QR_CUDA(pl.blk_g0.upload(bg0), "upload block groups");
+
+    if (pl.has_diag) {
+        const int db = std::min(n, 12);
+        const uint64_t dmask = (1ull << db) - 1;
+        std::vector<size_t> dt = diag_terms;
+        std::stable_sort(dt.begin(), dt.end(), [&](size_t a, size_t b) {
+            return (op->mz[a] & dmask) < (op->mz[b] & dmask);
+        });
+        std::vector<uint64_t> tz, bz;
+        std::vector<double> tcv;
+        std::vector<uint32_t> boff;
+        for (size_t i = 0; i < dt.size(); ++i) {
+            const uint64_t zl = op->mz[dt[i]] & dmask;
+            if (i == 0 || zl != bz.back()) {
+                bz.push_back(zl);
+                boff.push_back((uint32_t)i);
+            }
+            tz.push_back(op->mz[dt[i]]);
+            tcv.push_back(c[dt[i]].re);
+            tcv.push_back(c[dt[i]].im);
+        }
+        boff.push_back((uint32_t)dt.size());
+        DevBuf d_tz, d_tc, d_bz, d_boff;
+        QR_CUDA(d_tz.upload(tz), "upload diag z");
+        QR_CUDA(d_tc.upload(tcv), "upload diag c");
+        QR_CUDA(d_bz.upload(bz), "upload diag bins");
+        QR_CUDA(d_boff.upload(boff), "upload diag bin offsets");
+        const size_t esz = f32 ? sizeof(Cplx<float>) : sizeof(Cplx<double>);
+        QR_CUDA(pl.diag.alloc(op->N * esz), "alloc diagonal");
+        QR_CUDA(launch_diag(dtype, n, db, op->N >> db, d_bz.as<uint64_t>(), d_boff.as<uint32_t>(),
+                            (uint32_t)bz.size(), d_tz.as<uint64_t>(), d_tc.as<double>(), pl.diag.p,
+                            nullptr),
+                "diagonal kernel");
+        QR_CUDA(cudaDeviceSynchronize(), "diagonal kernel sync");
+    }
+    pl.built = true;
+    return QR_OK;
+}
+
+int check_device(const qr_op *op) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev != op->device)
+        return fail(QR_ESTATE, "operator lives on device %d but device %d is current", op->device,
+                    dev);
+    return QR_OK;
+}
+
+int check_kernel_error(qr_op *op) {
+    int h = 0;
+    QR_CUDA(cudaMemcpy(&h, op->d_err.p, sizeof(int), cudaMemcpyDeviceToHost), "read error word");
+    if (h != kErrNone) {
+        int z = 0;
+        cudaMemcpy(op->d_err.p, &z, sizeof(int), cudaMemcpyHostToDevice);
+        return fail(QR_EKERNEL, "kernel reported error %d (bounded mbarrier wait expired)", h);
+    }
+    return QR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qr_op_create(int32_t n, uint64_t nterms, const uint64_t *x, const uint64_t *z,
+                 const uint8_t *phase, const double *coeff, qr_op **out) {
+    if (!out) return fail(QR_EINVAL, "qr_op_create: out is null");
+    *out = nullptr;
+    if (n < 1 || n > 63) return fail(QR_EINVAL, "qr_op_create: n=%d outside [1, 63]", n);
+    if (nterms == 0)
+        return fail(QR_EINVAL, "SparsePauliOp::new: at least one pauli must be supplied");
+    if (nterms > 0xffffffffull) return fail(QR_EINVAL, "qr_op_create: too many terms");
+    if (!x || !z || !phase || !coeff) return fail(QR_EINVAL, "qr_op_create: null term array");
+    const uint64_t lim = (n == 64) ? ~0ull : ((1ull << n) - 1);
+    for (uint64_t k = 0; k < nterms; ++k) {
+        if ((x[k] & ~lim) || (z[k] & ~lim))
+            return fail(QR_EINVAL, "qr_op_create: term %llu has mask bits beyond n=%d",
+                        (unsigned long long)k, n);
+        if (phase[k] > 3)
+            return fail(QR_EINVAL, "qr_op_create: term %llu phase %u > 3", (unsigned long long)k,
+                        (unsigned)phase[k]);
+    }
+    qr_op *op = new (std::nothrow) qr_op();
+    if (!op) return fail(QR_ENOMEM, "qr_op_create: out of host memory");
+    op->n = n;
+    op->N = 1ull << n;
+    op->T = nterms;
+    op->x.assign(x, x + nterms);
+    op->z.assign(z, z + nterms);
+    op->cp.resize(nterms);
+    // make_params (qrusty/src/accel.rs:141-157): c' = m(phase) * c, with
+    // num-complex's product (ar*br - ai*bi, ar*bi + ai*br), no FMA.
+    static const cd m[4] = {{1.0, 0.0}, {0.0, -1.0}, {-1.0, 0.0}, {0.0, 1.0}};
+    for (uint64_t k = 0; k < nterms; ++k) {
+        const cd a = m[phase[k] & 3];
+        const cd b{coeff[2 * k], coeff[2 * k + 1]};
+        op->cp[k].re = a.re * b.re - a.im * b.im;
+        op->cp[k].im = a.re * b.im + a.im * b.re;
+    }
+    cudaError_t e = cudaGetDevice(&op->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&op->nsm, cudaDevAttrMultiProcessorCount, op->device);
+    if (e != cudaSuccess) {
+        delete op;
+        return cuda_fail(e, "qr_op_create: no usable CUDA device");
+    }
+    prepare_csr_tables(op);
+    e = op->d_err.alloc(sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(op->d_err.p, 0, sizeof(int));
+    if (e != cudaSuccess) {
+        delete op;
+        return cuda_fail(e, "qr_op_create: device allocation");
+    }
+    *out = op;
+    return QR_OK;
+}
+
+int qr_op_destroy(qr_op *op) {
+    if (!op) return QR_OK;
+    int dev = -1;
+    cudaGetDevice(&dev);
+    const int home = op->device;
+    if (dev != home) cudaSetDevice(home);
+    if (op->hstream) cudaStreamDestroy(op->hstream);
+    delete op;
+    if (dev >= 0 && dev != home) cudaSetDevice(dev);
+    return QR_OK;
+}
+
+int qr_check(qr_op *op, void *stream) {
+    if (!op) return fail(QR_EINVAL, "qr_check: null operator");
+    int rc = check_device(op);
+    if (rc) return rc;
+    QR_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "qr_check sync");
+    return check_kernel_error(op);
+}
+
+int qr_op_get_info(const qr_op *op_c, qr_op_info *info) {
+    if (!op_c || !info) return fail(QR_EINVAL, "qr_op_get_info: null argument");
+    qr_op *op = const_cast<qr_op *>(op_c);
+    int rc = check_device(op);
+    if (rc) return rc;
+    rc = build_plan(op, QR_C64C, 0);
+    if (rc) return rc;
+    const Plan &pl = op->plans[QR_C64C][0];
+    info->n = op->n;
+    info->tile_bits = pl.b;
+    info->nterms = op->T;
+    info->ngroups = op->G;
+    info->nmerged = op->mx.size();
+    info->nblocks = pl.nblocks;
+    info->nfat = pl.nfat;
+    info->has_diag = pl.has_diag ? 1 : 0;
+    info->device = op->device;
+    return QR_OK;
+}
+
+int qr_csr_size(const qr_op *op, uint64_t *nrows, uint64_t *nnz) {
+    if (!op || !nrows || !nnz) return fail(QR_EINVAL, "qr_csr_size: null argument");
+    *nrows = op->N;
+    if (op->G != 0 && op->N > ~0ull / op->G) return fail(QR_EINVAL, "qr_csr_size: nnz overflows");
+    *nnz = op->N * op->G;
+    return QR_OK;
+}
+
+int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, int32_t mem,
+                 void *stream) {
+    if (!op || !indptr || !indices || !data) return fail(QR_EINVAL, "qr_csr_build: null argument");
+    if (mem != QR_MEM_DEVICE && mem != QR_MEM_HOST)
+        return fail(QR_EINVAL, "qr_csr_build: mem must be QR_MEM_DEVICE or QR_MEM_HOST");
+    int rc = check_device(op);
+    if (rc) return rc;
+    rc = upload_csr_tables(op);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CsrArgs a;
+    a.N = op->N;
+    a.G = op->G;
+    a.gx = op->d_gx.as<uint64_t>();
+    a.goff = op->d_goff.as<uint32_t>();
+    a.tz = op->d_tz.as<uint64_t>();
+    a.tc = op->d_tc.as<double>();
+    a.eoff = op->d_eoff.as<uint32_t>();
+    a.ebit = op->d_ebit.as<uint8_t>();
+    a.esig = op->d_esig.as<int64_t>();
+    if (mem == QR_MEM_DEVICE) {
+        a.indptr = indptr;
+        a.indices = indices;
+        a.data = data;
+        a.row0 = 0;
+        a.nrows = op->N;
+        QR_CUDA(launch_csr_fill(a, op->nsm, st), "csr fill launch");
+        return QR_OK;
+    }
+    // host destination: build in row chunks of <= ~1 GiB on the device
+    const uint64_t per_row = op->G * 24;
+    uint64_t rows = (1ull << 30) / (per_row ? per_row : 1);
+    if (rows == 0) rows = 1;
+    if (rows > op->N) rows = op->N;
+    DevBuf d_ptr, d_idx, d_dat;
+    QR_CUDA(d_ptr.alloc((op->N + 1) * sizeof(uint64_t)), "alloc indptr staging");
+    QR_CUDA(d_idx.alloc(rows * op->G * sizeof(uint64_t)), "alloc indices staging");
+    QR_CUDA(d_dat.alloc(rows * op->G * 2 * sizeof(double)), "alloc data staging");
+    for (uint64_t r0 = 0; r0 < op->N; r0 += rows) {
+        const uint64_t nr = std::min(rows, op->N - r0);
+        a.indptr = (r0 == 0) ? d_ptr.as<uint64_t>() : nullptr;
+        a.indices = d_idx.as<uint64_t>();
+        a.data = d_dat.as<double>();
+        a.row0 = r0;
+        a.nrows = nr;
+        QR_CUDA(launch_csr_fill(a, op->nsm, st), "csr fill launch");
+        QR_CUDA(cudaMemcpyAsync(indices + r0 * op->G, d_idx.p, nr * op->G * sizeof(uint64_t),
+                                cudaMemcpyDeviceToHost, st),
+                "copy indices");
+        QR_CUDA(cudaMemcpyAsync(data + 2 * r0 * op->G, d_dat.p, nr * op->G * 2 * sizeof(double),
+                                cudaMemcpyDeviceToHost, st),
+                "copy data");
+    }
+    QR_CUDA(cudaMemcpyAsync(indptr, d_ptr.p, (op->N + 1) * sizeof(uint64_t),
+                            cudaMemcpyDeviceToHost, st),
+            "copy indptr");
+    QR_CUDA(cudaStreamSynchronize(st), "csr build sync");
+    return QR_OK;
+}
+
+int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates, int32_t adjoint,
+             void *stream) {
+    if (!op || !psi || !y) return fail(QR_EINVAL, "qr_apply: null argument");
+    if (dtype != QR_C128 && dtype != QR_C64C)
+        return fail(QR_EINVAL, "qr_apply: dtype must be QR_C128 or QR_C64C");
+    if (nstates < 1) return fail(QR_EINVAL, "qr_apply: nstates=%d < 1", nstates);
+    if (adjoint != 0 && adjoint != 1) return fail(QR_EINVAL, "qr_apply: adjoint must be 0 or 1");
+    if (op->n > 40) return fail(QR_EINVAL, "qr_apply: n=%d too large for a state vector", op->n);
+    const size_t esz = dtype == QR_C128 ? 16 : 8;
+    const uint64_t bytes = (uint64_t)nstates * op->N * esz;
+    const char *pb = static_cast<const char *>(psi), *yb = static_cast<const char *>(y);
+    if (pb < yb + bytes && yb < pb + bytes) return fail(QR_EINVAL, "qr_apply: psi and y overlap");
+    if ((reinterpret_cast<uintptr_t>(psi) | reinterpret_cast<uintptr_t>(y)) & 15)
+        return fail(QR_EINVAL, "qr_apply: psi and y must be 16-byte aligned");
+    int rc = check_device(op);
+    if (rc) return rc;
+    rc = build_plan(op, dtype, adjoint);
+    if (rc) return rc;
+    const Plan &pl = op->plans[dtype][adjoint];
+    ApplyArgs a;
+    a.psi = psi;
+    a.y = y;
+    a.N = op->N;
+    a.n = op->n;
+    a.b = pl.b;
+    a.tb = pl.tb;
+    a.nstates = nstates;
+    a.ntiles = op->N >> pl.b;
+    a.nitems = (uint64_t)nstates * a.ntiles;
+    a.groups = pl.groups.as<GroupDesc>();
+    a.tables = pl.tables.p;
+    a.fat_z = pl.fat_z.as<uint64_t>();
+    a.fat_c = pl.fat_c.p;
+    a.blk_hi = pl.blk_hi.as<uint64_t>();
+    a.blk_g0 = pl.blk_g0.as<uint32_t>();
+    a.nblocks = pl.nblocks;
+    a.diag = pl.has_diag ? pl.diag.p : nullptr;
+    a.diag_block = pl.diag_block;
+    a.err = op->d_err.as<int>();
+    if (pl.nblocks == 0) {
+        // operator without terms reachable here cannot happen (T >= 1); keep y defined
+        QR_CUDA(cudaMemsetAsync(y, 0, bytes, static_cast<cudaStream_t>(stream)), "zero y");
+        return QR_OK;
+    }
+    QR_CUDA(launch_apply(dtype, a, pl.amps, pl.threads, op->nsm,
+                         static_cast<cudaStream_t>(stream)),
+            "apply launch");
+    return QR_OK;
+}
+
+int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host, int32_t nstates,
+                  int32_t adjoint) {
+    if (!op || !psi_host || !y_host) return fail(QR_EINVAL, "qr_apply_host: null argument");
+    if (dtype != QR_C128 && dtype != QR_C64C)
+        return fail(QR_EINVAL, "qr_apply_host: dtype must be QR_C128 or QR_C64C");
+    if (nstates < 1) return fail(QR_EINVAL, "qr_apply_host: nstates=%d < 1", nstates);
+    int rc = check_device(op);
+    if (rc) return rc;
+    const size_t esz = dtype == QR_C128 ? 16 : 8;
+    const uint64_t bytes = (uint64_t)nstates * op->N * esz;
+    if (!op->hstream) QR_CUDA(cudaStreamCreateWithFlags(&op->hstream, cudaStreamNonBlocking),
+                              "create stream");
+    if (op->stage_in.bytes < bytes) QR_CUDA(op->stage_in.alloc(bytes), "alloc psi staging");
+    if (op->stage_out.bytes < bytes) QR_CUDA(op->stage_out.alloc(bytes), "alloc y staging");
+    QR_CUDA(cudaMemcpyAsync(op->stage_in.p, psi_host, bytes, cudaMemcpyHostToDevice, op->hstream),
+            "copy psi to device");
+    rc = qr_apply(op, dtype, op->stage_in.p, op->stage_out.p, nstates, adjoint, op->hstream);
+    if (rc) return rc;
+    QR_CUDA(cudaMemcpyAsync(y_host, op->stage_out.p, bytes, cudaMemcpyDeviceToHost, op->hstream),
+            "copy y to host");
+    QR_CUDA(cudaStreamSynchronize(op->hstream), "apply_host sync");
+    return check_kernel_error(op);
+}
+
+int qr_csr_spmv(uint64_t nrows, const uint64_t *indptr, const uint64_t *indices,
+                const double *data, const double *v, double *y, void *stream) {
+    if (!indptr || !indices || !data || !v || !y) return fail(QR_EINVAL, "qr_csr_spmv: null argument");
+    int dev = 0, nsm = 0;
+    QR_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    QR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    QR_CUDA(launch_csr_spmv(nrows, indptr, indices, data, v, y, nsm,
+                            static_cast<cudaStream_t>(stream)),
+            "csr spmv launch");
+    return QR_OK;
+}
+
+int qr_last_error(char *buf, size_t len) {
+    const int L = (int)g_err.size();
+    if (buf && len > 0) {
+        size_t c = std::min(len - 1, g_err.size());
+        memcpy(buf, g_err.data(), c);
+        buf[c] = '\0';
+    }
+    return L;
+}
+
+uint64_t qr_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+}  // extern "C"

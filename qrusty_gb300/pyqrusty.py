@@ -1,0 +1,450 @@
+"""pyqrusty-compatible Python edge over libqrusty_gpu.
+
+Mirrors the classes and functions of qrusty's pyo3 binding
+(pyqrusty/src/lib.rs, pyqrusty/python/pyqrusty/__init__.py) for the
+Pauli-operator hot path -- same names, argument meaning and error messages --
+with every numeric result computed by the sm_103a kernels behind the C ABI
+(include/qrusty_gpu.h):
+
+* ``Pauli`` (pyqrusty/src/lib.rs:262-303; parsing qrusty/src/lib.rs:125-181)
+* ``SparsePauliOp`` (pyqrusty/src/lib.rs:305-433; qrusty/src/lib.rs:345-586)
+  with ``to_matrix`` / ``to_matrix_mode`` routed to the GPU CSR builder and
+  a matrix-free ``apply`` (H psi on the GPU)
+* ``SpMat`` (pyqrusty/src/lib.rs:33-214): CSR holder with ``export``
+* ``spmat_dot_densevec`` (pyqrusty/src/lib.rs:476-491): GPU CSR * vector
+* ``csr_matrix`` (pyqrusty/python/pyqrusty/__init__.py:14-17)
+
+Out of scope here (matrix algebra around the path, not the path):
+MatrixMarket I/O, ``+``/``-``/``scale`` on SpMat, ``a_spmat_p_b_spmat``,
+``axpby``/``axpy``/``ax``, ``precond``/``precond2``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import re
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import QR_C128, QR_C64C, QR_MEM_HOST, QrError, check
+
+__all__ = ["Pauli", "SparsePauliOp", "SpMat", "PauliOperator", "spmat_dot_densevec",
+           "csr_matrix", "QrError", "parse_mode"]
+
+_LABEL_RE = re.compile(r"^([+-]?)1?([ij]?)([IXYZ]+)$")
+
+
+def _rust_f64(x: float) -> str:
+    """f64 Display as Rust formats it: shortest round-trip digits, never
+    exponent notation, "-0" for negative zero, "NaN", "inf"."""
+    if math.isnan(x):
+        return "NaN"
+    if math.isinf(x):
+        return "inf" if x > 0 else "-inf"
+    return np.format_float_positional(float(x), unique=True, trim="-")
+
+
+def _complex_to_string(c: complex) -> str:
+    """qrusty/src/util.rs complex64_to_string: format!("{}+{}j", re, im)."""
+    return "%s+%sj" % (_rust_f64(c.real), _rust_f64(c.imag))
+
+
+class Pauli:
+    """One Pauli string, parsed as qrusty's Pauli::parse_label
+    (qrusty/src/lib.rs:125-149): ``^([+-]?)1?([ij]?)([IXYZ]+)$``, base phase
+    1 for i/j plus 2 for a leading '-', letters reversed so that qubit 0 is
+    the rightmost character."""
+
+    __slots__ = ("_base_phase", "_letters")
+
+    def __init__(self, label: str):
+        m = _LABEL_RE.match(label)
+        if m is None:
+            raise Exception("error: malformed label")
+        sign, imag, paulistr = m.group(1), m.group(2), m.group(3)
+        phase = 1 if imag in ("i", "j") else 0
+        if sign == "-":
+            phase += 2
+        self._base_phase = phase
+        self._letters = paulistr[::-1]  # qubit order
+
+    # -- pyqrusty surface
+    def num_qubits(self) -> int:
+        return len(self._letters)
+
+    def label(self) -> str:
+        return self._letters[::-1]
+
+    def __repr__(self) -> str:
+        return "Pauli('%s')" % self.label()
+
+    def __str__(self) -> str:
+        return self.label()
+
+    def to_matrix(self) -> "SpMat":
+        """Single-Pauli matrix in the kron convention (qrusty/src/lib.rs:203-213)."""
+        return SparsePauliOp([self], [1.0 + 0.0j]).to_matrix()
+
+    # -- masks (qrusty/src/lib.rs:161-190)
+    def base_phase(self) -> int:
+        return self._base_phase
+
+    def x_indices(self) -> int:
+        return sum(1 << i for i, c in enumerate(self._letters) if c in "XY")
+
+    def z_indices(self) -> int:
+        return sum(1 << i for i, c in enumerate(self._letters) if c in "YZ")
+
+    def phase(self) -> int:
+        return (self._base_phase + self._letters.count("Y")) % 4
+
+    def xs(self):
+        return [c in "XY" for c in self._letters]
+
+    def zs(self):
+        return [c in "YZ" for c in self._letters]
+
+
+# AccelMode (qrusty/src/lib.rs:270-331).  Kron-family modes build each Pauli
+# as i^base * (x) 2x2 factors (Pauli::to_matrix, lib.rs:203-213); the others
+# multiply by (-i)^phase as make_params does (accel.rs:141-157).  The two
+# agree unless a label carries an i / -i prefix.
+_KRON_MODES = {None, "Binary", "Reduce", "Rayon"}
+_RUC_RE = re.compile(r"RowwiseUnsafeChunked/(\d+)")
+_RC_RE = re.compile(r"RayonChunked/(\d+)")
+
+
+def parse_mode(value: str):
+    """AccelMode::try_from (qrusty/src/lib.rs:293-331); returns
+    (name, step) or raises ValueError."""
+    if value in ("Binary", "Accel", "Rowwise", "RowwiseUnsafe"):
+        return value, None
+    m = _RUC_RE.search(value)
+    if m:
+        return "RowwiseUnsafeChunked", int(m.group(1))
+    if value in ("Reduce", "Rayon"):
+        return value, None
+    m = _RC_RE.search(value)
+    if m:
+        return "RayonChunked", int(m.group(1))
+    raise ValueError("AccelMode:try_from: unrecognized argument string")
+
+
+class PauliOperator:
+    """Owner of one ``qr_op`` handle: the operator's term tables on the GPU.
+
+    Terms are (x, z, phase, coeff) as qrusty's make_params consumes them.
+    """
+
+    def __init__(self, n: int, x, z, phase, coeffs):
+        L = _lib.load()
+        self.n = int(n)
+        self._x = np.ascontiguousarray(x, dtype=np.uint64)
+        self._z = np.ascontiguousarray(z, dtype=np.uint64)
+        self._ph = np.ascontiguousarray(phase, dtype=np.uint8)
+        self._c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+        T = len(self._x)
+        if not (len(self._z) == len(self._ph) == len(self._c) == T):
+            raise ValueError("term arrays differ in length")
+        h = C.c_void_p()
+        check(L.qr_op_create(self.n, T, self._x.ctypes.data, self._z.ctypes.data,
+                             self._ph.ctypes.data, self._c.ctypes.data, C.byref(h)))
+        self._h = h
+        self.nterms = T
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().qr_op_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> dict:
+        inf = _lib.OpInfo()
+        check(_lib.load().qr_op_get_info(self._h, C.byref(inf)))
+        return {f: getattr(inf, f) for f, _ in inf._fields_}
+
+    def csr_size(self):
+        nr, nz = C.c_uint64(), C.c_uint64()
+        check(_lib.load().qr_csr_size(self._h, C.byref(nr), C.byref(nz)))
+        return nr.value, nz.value
+
+    def csr_host(self):
+        """(indptr u64, indices u64, data c128) numpy arrays built on the GPU."""
+        nr, nz = self.csr_size()
+        indptr = np.empty(nr + 1, dtype=np.uint64)
+        indices = np.empty(nz, dtype=np.uint64)
+        data = np.empty(nz, dtype=np.complex128)
+        check(_lib.load().qr_csr_build(self._h, indptr.ctypes.data, indices.ctypes.data,
+                                       data.ctypes.data, QR_MEM_HOST, None))
+        return indptr, indices, data
+
+    def csr_device(self, stream=None):
+        """(indptr, indices, data) as torch CUDA tensors (data complex128)."""
+        import torch
+        nr, nz = self.csr_size()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        indptr = torch.empty(nr + 1, dtype=torch.int64, device=dev)
+        indices = torch.empty(nz, dtype=torch.int64, device=dev)
+        data = torch.empty(nz, dtype=torch.complex128, device=dev)
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(_lib.load().qr_csr_build(self._h, indptr.data_ptr(), indices.data_ptr(),
+                                       data.data_ptr(), _lib.QR_MEM_DEVICE, st))
+        return indptr, indices, data
+
+    def apply(self, psi, out=None, adjoint: bool = False, stream=None):
+        """y = H psi (or H^dagger psi) on the GPU.
+
+        torch CUDA tensor in (complex64 -> compensated c64 kernel, complex128
+        -> plain c128 kernel), shape (2^n,) or (S, 2^n): asynchronous on the
+        current stream, returns a tensor.  numpy array in: copies to the
+        device, applies, copies back (synchronous), returns numpy."""
+        N = 1 << self.n
+        if isinstance(psi, np.ndarray):
+            if psi.dtype == np.complex64:
+                dt = QR_C64C
+            elif psi.dtype == np.complex128:
+                dt = QR_C128
+            else:
+                raise TypeError("psi must be complex64 or complex128")
+            p = np.ascontiguousarray(psi)
+            if p.size % N:
+                raise ValueError("psi length %d is not a multiple of 2^n=%d" % (p.size, N))
+            y = np.empty_like(p) if out is None else out
+            check(_lib.load().qr_apply_host(self._h, dt, p.ctypes.data, y.ctypes.data,
+                                            p.size // N, int(bool(adjoint))))
+            return y
+        import torch
+        if not (isinstance(psi, torch.Tensor) and psi.is_cuda):
+            raise TypeError("psi must be a numpy array or a CUDA torch tensor")
+        if psi.dtype == torch.complex64:
+            dt = QR_C64C
+        elif psi.dtype == torch.complex128:
+            dt = QR_C128
+        else:
+            raise TypeError("psi must be complex64 or complex128")
+        p = psi.contiguous()
+        if p.numel() % N:
+            raise ValueError("psi length %d is not a multiple of 2^n=%d" % (p.numel(), N))
+        y = torch.empty_like(p) if out is None else out
+        st = stream if stream is not None else torch.cuda.current_stream(p.device).cuda_stream
+        check(_lib.load().qr_apply(self._h, dt, p.data_ptr(), y.data_ptr(), p.numel() // N,
+                                   int(bool(adjoint)), st))
+        return y
+
+    def sync_check(self, stream=None):
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(_lib.load().qr_check(self._h, st))
+
+
+def _letters_masks(paulis):
+    x = np.fromiter((p.x_indices() for p in paulis), dtype=np.uint64, count=len(paulis))
+    z = np.fromiter((p.z_indices() for p in paulis), dtype=np.uint64, count=len(paulis))
+    return x, z
+
+
+class SparsePauliOp:
+    """Sum of (Pauli, coeff) pairs in insertion order
+    (qrusty/src/lib.rs:345-376, pyqrusty/src/lib.rs:305-433).
+    Duplicate strings are not merged."""
+
+    def __init__(self, paulis, coeffs):
+        paulis = list(paulis)
+        coeffs = [complex(c) for c in coeffs]
+        if len(paulis) != len(coeffs):
+            raise Exception("SparsePauliOp::new: paulis and coeffs must have same length")
+        if len(paulis) == 0:
+            raise Exception("SparsePauliOp::new: at least one pauli must be supplied")
+        nq = paulis[0].num_qubits()
+        if any(p.num_qubits() != nq for p in paulis):
+            raise Exception("SparsePauliOp::new: all supplied paulis must have the same #qubits")
+        self._paulis = paulis
+        self._coeffs = coeffs
+        self._ops = {}
+
+    @classmethod
+    def from_labels(cls, labels, coeffs):
+        return cls([Pauli(l) for l in labels], coeffs)
+
+    def __len__(self) -> int:
+        return len(self._paulis)
+
+    def __getitem__(self, idx):
+        if isinstance(idx, slice):
+            start, stop, step = idx.indices(len(self._paulis))
+            return [(self._paulis[i], self._coeffs[i]) for i in range(start, stop, step)]
+        idx = int(idx)
+        if not (0 <= idx < len(self._paulis)):
+            raise Exception("__getitem__ called on invalid index %d" % idx)
+        return (self._paulis[idx], self._coeffs[idx])
+
+    def num_qubits(self) -> int:
+        return self._paulis[0].num_qubits()
+
+    def __repr__(self) -> str:
+        labels = "','".join(p.label() for p in self._paulis)
+        coeffs = ", ".join(_complex_to_string(c) for c in self._coeffs)
+        return "SparsePauliOp('%s', [%s])" % (labels, coeffs)
+
+    __str__ = __repr__
+
+    def __add__(self, other: "SparsePauliOp") -> "SparsePauliOp":
+        return SparsePauliOp(self._paulis + other._paulis, self._coeffs + other._coeffs)
+
+    # -- GPU operator for one phase convention
+    def operator(self, convention: str = "rowwise") -> PauliOperator:
+        op = self._ops.get(convention)
+        if op is None:
+            x, z = _letters_masks(self._paulis)
+            ph = np.fromiter((p.phase() for p in self._paulis), dtype=np.uint8,
+                             count=len(self._paulis))
+            if convention == "kron":
+                bp = np.fromiter((p.base_phase() for p in self._paulis), dtype=np.uint8,
+                                 count=len(self._paulis))
+                ph = ((ph.astype(np.int64) + 2 * bp) % 4).astype(np.uint8)
+            elif convention != "rowwise":
+                raise ValueError("convention must be 'rowwise' or 'kron'")
+            op = PauliOperator(self.num_qubits(), x, z, ph, np.array(self._coeffs))
+            self._ops[convention] = op
+        return op
+
+    def to_matrix(self) -> "SpMat":
+        """Kron-convention matrix (qrusty/src/lib.rs:401-412), built on the GPU."""
+        return SpMat._from_op(self.operator("kron"))
+
+    def to_matrix_mode(self, mode: str = "") -> "SpMat":
+        """pyqrusty/src/lib.rs:406-415.  "" -> to_matrix(); every AccelMode
+        builds the CSR on the GPU (no CPU path)."""
+        if mode == "":
+            return self.to_matrix()
+        try:
+            name, _step = parse_mode(mode)
+        except ValueError:
+            raise Exception("to_matrix_mode: unrecognized mode %s" % mode) from None
+        conv = "kron" if name in _KRON_MODES else "rowwise"
+        return SpMat._from_op(self.operator(conv))
+
+    def apply(self, psi, out=None, adjoint: bool = False):
+        """Matrix-free y = H psi on the GPU (rowwise convention); see
+        PauliOperator.apply."""
+        return self.operator("rowwise").apply(psi, out=out, adjoint=adjoint)
+
+
+class SpMat:
+    """CSR matrix holder (pyqrusty/src/lib.rs:33-214): complex128 data,
+    u64 indices/indptr.  ``export`` moves the arrays out and leaves the
+    matrix empty, after which other methods raise as the reference does."""
+
+    def __init__(self, shape, data, indices, indptr):
+        self._it = (tuple(int(s) for s in shape), np.ascontiguousarray(data, dtype=np.complex128),
+                    np.ascontiguousarray(indices, dtype=np.uint64),
+                    np.ascontiguousarray(indptr, dtype=np.uint64))
+        self._dev = None
+
+    @classmethod
+    def _from_op(cls, op: PauliOperator) -> "SpMat":
+        indptr, indices, data = op.csr_host()
+        N = 1 << op.n
+        return cls((N, N), data, indices, indptr)
+
+    @staticmethod
+    def new_unchecked(shape, data, indices, indptr) -> "SpMat":
+        return SpMat(shape, data, indices, indptr)
+
+    def _get(self, msg):
+        if self._it is None:
+            raise Exception(msg)
+        return self._it
+
+    def shape(self):
+        return self._get("SpMat.shape(): matrix is already dropped")[0]
+
+    def nnz(self) -> int:
+        return len(self._get("cannot get NNZ of an exported sparse matrix")[1])
+
+    def diagonal(self):
+        shape, data, indices, indptr = self._get(
+            "SpMat.diagonal(): already-exported sparse matrix")
+        n = min(shape)
+        out = np.zeros(n, dtype=np.complex128)
+        for r in range(n):
+            lo, hi = int(indptr[r]), int(indptr[r + 1])
+            hit = np.nonzero(indices[lo:hi] == r)[0]
+            if len(hit):
+                out[r] = data[lo + hit[0]]
+        return out
+
+    def __repr__(self) -> str:
+        if self._it is None:
+            return "<already-dropped sparse matrix of type Complex64>"
+        (rows, cols), data = self._it[0], self._it[1]
+        return ("<%dx%d sparse matrix of type Complex64\n\twith %d stored elements in "
+                "Compressed Sparse Row format>" % (rows, cols, len(data)))
+
+    __str__ = __repr__
+
+    def __copy__(self) -> "SpMat":
+        m = SpMat.__new__(SpMat)
+        m._it = None if self._it is None else (self._it[0], self._it[1].copy(),
+                                               self._it[2].copy(), self._it[3].copy())
+        m._dev = None
+        return m
+
+    def export(self):
+        if self._it is None:
+            raise Exception("cannot export from an already-exported sparse matrix")
+        shape, data, indices, indptr = self._it
+        self._it = None
+        self._dev = None
+        return (shape, data, indices, indptr)
+
+    def _device(self):
+        import torch
+        shape, data, indices, indptr = self._get(
+            "cannot multiply with an exported sparse matrix")
+        if self._dev is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+            self._dev = (torch.from_numpy(indptr.view(np.int64)).to(dev),
+                         torch.from_numpy(indices.view(np.int64)).to(dev),
+                         torch.from_numpy(data).to(dev))
+        return self._dev
+
+
+def spmat_dot_densevec(spmat: SpMat, x):
+    """y = spmat * x on the GPU (pyqrusty/src/lib.rs:476-491,
+    qrusty/src/accel.rs:338-370).  numpy complex128 in and out."""
+    import torch
+    if spmat._it is None:
+        raise Exception("cannot multiply with an exported sparse matrix")
+    shape = spmat._it[0]
+    xv = np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
+    if xv.ndim != 1 or xv.shape[0] != shape[1]:
+        raise Exception("spmat_dot_densevec: vector length %d != %d columns"
+                        % (xv.shape[0] if xv.ndim else 0, shape[1]))
+    indptr, indices, data = spmat._device()
+    dev = data.device
+    xd = torch.from_numpy(xv).to(dev)
+    yd = torch.empty(shape[0], dtype=torch.complex128, device=dev)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    check(_lib.load().qr_csr_spmv(shape[0], indptr.data_ptr(), indices.data_ptr(),
+                                  data.data_ptr(), xd.data_ptr(), yd.data_ptr(), st))
+    return yd.cpu().numpy()
+
+
+def csr_matrix(m: SpMat):
+    """pyqrusty/python/pyqrusty/__init__.py:14-17."""
+    (shape, data, indices, indptr) = m.export()
+    from scipy.sparse import csr_matrix as _csr
+    return _csr((data, indices, indptr), shape=shape, dtype=complex)

@@ -1,0 +1,156 @@
+"""GPU CSR construction vs the oracle (qrusty's rowwise builder restated):
+indptr / indices bit-exact, values bit-exact (same term-order FP64 fold)."""
+import numpy as np
+import pytest
+
+from qrusty_gb300 import PauliOperator, Pauli, SparsePauliOp, csr_matrix
+from qrusty_gb300 import workloads as W
+from tests.helpers import kron_dense, terms_of_labels
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+def check_csr(oracle, n, x, z, ph, c, sample_rows=None):
+    op = PauliOperator(n, x, z, ph, c)
+    indptr, indices, data = op.csr_host()
+    cp = oracle.make_params(ph, c)
+    G = len(np.unique(x))
+    N = 1 << n
+    assert len(indices) == N * G
+    if sample_rows is None:
+        oi, oj, od = oracle.csr_build(n, x, z, cp, step=1024)
+        assert np.array_equal(indptr, oi)
+        assert np.array_equal(indices, oj)
+        assert np.array_equal(_bits(data), _bits(od))
+    else:
+        assert np.array_equal(indptr, np.arange(N + 1, dtype=np.uint64) * np.uint64(G))
+        for r in sample_rows:
+            cols, vals = oracle.make_row(x, z, cp, r)
+            lo = r * G
+            assert np.array_equal(indices[lo:lo + G], cols)
+            assert np.array_equal(_bits(data[lo:lo + G]), _bits(vals))
+    return op, (indptr, indices, data)
+
+
+@pytest.mark.parametrize("name", ["H2", "H4", "H6"])
+def test_fixtures(cuda, oracle, golden, name):
+    labels, coeffs = golden[name]
+    check_csr(oracle, *terms_of_labels(labels, coeffs))
+
+
+def test_fixture_H8_rows(cuda, oracle, golden):
+    labels, coeffs = golden["H8"]
+    n, x, z, ph, c = terms_of_labels(labels, coeffs)
+    rng = np.random.default_rng(3)
+    rows = [0, 1, (1 << n) - 1] + [int(v) for v in rng.integers(0, 1 << n, 40)]
+    check_csr(oracle, n, x, z, ph, c, sample_rows=rows)
+
+
+def test_cfg0(cuda, oracle):
+    t, _ = W.cfg0(with_state=False)
+    check_csr(oracle, t.n, t.x, t.z, t.phase, t.coeff)
+
+
+def test_cfg1_small(cuda, oracle):
+    t, _ = W.cfg1(with_state=False, n=12)
+    check_csr(oracle, t.n, t.x, t.z, t.phase, t.coeff)
+
+
+def test_jw_small(cuda, oracle):
+    t = W.cfg2(n=12, npair=600, nz=150)
+    check_csr(oracle, t.n, t.x, t.z, t.phase, t.coeff)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_edge_cases(cuda, oracle, seed):
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(1, 11))
+    T = int(rng.integers(1, 60))
+    # few distinct strings so that duplicates and cancellations occur
+    pool = rng.integers(0, 1 << n, size=(max(1, T // 3), 2)).astype(np.uint64)
+    pick = rng.integers(0, len(pool), T)
+    x, z = pool[pick, 0], pool[pick, 1]
+    ph = rng.integers(0, 4, T).astype(np.uint8)
+    c = (rng.integers(-2, 3, T) + 1j * rng.integers(-2, 3, T)).astype(np.complex128)
+    check_csr(oracle, n, x, z, ph, c)
+
+
+def test_single_term_and_n1(cuda, oracle):
+    check_csr(oracle, 1, np.array([1], np.uint64), np.array([1], np.uint64),
+              np.array([1], np.uint8), np.array([0.5 - 2j]))
+    check_csr(oracle, 5, np.array([0], np.uint64), np.array([0], np.uint64),
+              np.array([0], np.uint8), np.array([3.0]))
+
+
+def test_cancellation_zero_kept(cuda, oracle):
+    x = np.array([1, 1, 2], np.uint64)
+    z = np.array([0, 0, 2], np.uint64)
+    op, (ip, ij, d) = check_csr(oracle, 2, x, z, np.zeros(3, np.uint8),
+                                np.array([1.0, -1.0, 0.5]))
+    assert np.count_nonzero(d == 0) == 4
+
+
+@pytest.mark.parametrize("name", ["H2", "H4"])
+def test_reference_test_H(cuda, golden, name):
+    """pyqrusty/tests/test_H.py:32-48 on the GPU build: kron path
+    (to_matrix) == RowwiseUnsafeChunked/100, dense, exactly."""
+    labels, coeffs = golden[name]
+    H = SparsePauliOp([Pauli(l) for l in labels], list(coeffs))
+    m1 = csr_matrix(H.to_matrix()).todense()
+    assert np.array_equal(m1, csr_matrix(H.to_matrix_mode(mode="")).todense())
+    m2 = csr_matrix(H.to_matrix_mode(mode="RowwiseUnsafeChunked/100")).todense()
+    assert np.array_equal(m1, m2)
+    assert np.array_equal(m1, kron_dense(labels, coeffs))
+
+
+def test_reference_test_H6_and_shape(cuda, golden):
+    labels, coeffs = golden["H6"]
+    H = SparsePauliOp([Pauli(l) for l in labels], list(coeffs))
+    m = H.to_matrix()
+    assert m.shape() == (1 << 12, 1 << 12)
+    m1 = csr_matrix(m).todense()
+    m2 = csr_matrix(H.to_matrix_mode(mode="RowwiseUnsafeChunked/100")).todense()
+    assert np.array_equal(m1, m2)
+
+
+@pytest.mark.parametrize("label,mat", [
+    ("I", [[1, 0], [0, 1]]), ("X", [[0, 1], [1, 0]]), ("Z", [[1, 0], [0, -1]]),
+    ("Y", [[0, -1j], [1j, 0]])])
+def test_reference_pauli_matrices(cuda, label, mat):  # test_it.py:60-83
+    spmat = csr_matrix(Pauli(label).to_matrix())
+    assert np.array_equal(np.array(mat, dtype=complex), spmat.todense())
+
+
+def test_i_plus_2x_all_modes(cuda):  # qrusty/src/lib.rs:775-813
+    spop = SparsePauliOp([Pauli("I"), Pauli("X")], [1.0, 2.0])
+    want = np.array([[1, 2], [2, 1]], dtype=complex)
+    for mode in ["", "Binary", "Accel", "Rowwise", "RowwiseUnsafe", "RowwiseUnsafeChunked/500",
+                 "Reduce", "Rayon", "RayonChunked/1"]:
+        assert np.array_equal(csr_matrix(spop.to_matrix_mode(mode)).todense(), want)
+
+
+def test_export_moves(cuda):  # pyqrusty/src/lib.rs:190-214
+    m = Pauli("XY").to_matrix()
+    assert m.nnz() == 4
+    assert repr(m).startswith("<4x4 sparse matrix of type Complex64")
+    shape, data, indices, indptr = m.export()
+    assert shape == (4, 4) and data.dtype == np.complex128 and indices.dtype == np.uint64
+    with pytest.raises(Exception, match="already-exported"):
+        m.export()
+    assert repr(m) == "<already-dropped sparse matrix of type Complex64>"
+
+
+def test_device_build_matches_host(cuda):
+    import torch
+    t, _ = W.cfg0(with_state=False)
+    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
+    hi, hj, hd = op.csr_host()
+    di, dj, dd = op.csr_device()
+    torch.cuda.synchronize()
+    assert np.array_equal(di.cpu().numpy().view(np.uint64), hi)
+    assert np.array_equal(dj.cpu().numpy().view(np.uint64), hj)
+    assert np.array_equal(_bits(dd.cpu().numpy()), _bits(hd))
