@@ -114,9 +114,12 @@ int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host,
  * spmat_dot_densevec, qrusty/src/accel.rs:338-370, and its binding
  * pyqrusty/src/lib.rs:476-491).  complex128; each row's products are summed
  * by one warp (lane-strided partial sums, then a butterfly), so the result
- * matches a storage-order sum to rounding, not bit for bit. */
-int qr_csr_spmv(uint64_t nrows, const uint64_t *indptr, const uint64_t *indices,
-                const double *data, const double *v, double *y, void *stream);
+ * matches a storage-order sum to rounding, not bit for bit.  v has ncols
+ * entries; a column index >= ncols is skipped.  indptr must be a valid
+ * non-decreasing row-pointer array over data / indices. */
+int qr_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
+                const uint64_t *indices, const double *data, const double *v, double *y,
+                void *stream);
 
 /* Message of the calling thread's last failure ("" if none).  Copies at
  * most len-1 bytes plus a terminating NUL; returns the full length. */

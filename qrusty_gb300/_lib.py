@@ -72,7 +72,7 @@ def load(build_if_missing: bool = True):
     L.qr_apply.argtypes = [vp, i32, vp, vp, i32, i32, vp]
     L.qr_check.argtypes = [vp, vp]
     L.qr_apply_host.argtypes = [vp, i32, vp, vp, i32, i32]
-    L.qr_csr_spmv.argtypes = [u64, vp, vp, vp, vp, vp, vp]
+    L.qr_csr_spmv.argtypes = [u64, u64, vp, vp, vp, vp, vp, vp]
     L.qr_last_error.argtypes = [C.c_char_p, C.c_size_t]
     for name in EXPORTS:
         getattr(L, name).restype = C.c_int

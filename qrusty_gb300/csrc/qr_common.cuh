@@ -53,7 +53,7 @@ struct ApplyArgs {
 };
 
 // Device error codes written to the error word.
-enum : int { kErrNone = 0, kErrMbarTimeout = 1 };
+enum : int { kErrNone = 0, kErrMbarTimeout = 1, kErrCsrPos = 2 };
 
 // Per-process launch counter (all launches issued through this library).
 void count_launch(uint64_t k = 1);
@@ -77,10 +77,11 @@ struct CsrArgs {
     uint64_t *indptr, *indices;
     double *data;
     uint64_t row0, nrows;     // rows to fill
+    int *err;                 // device error word (bad position => kErrCsrPos)
 };
 cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st);
-cudaError_t launch_csr_spmv(uint64_t nrows, const uint64_t *indptr, const uint64_t *indices,
-                            const double *data, const double *v, double *y, int nsm,
-                            cudaStream_t st);
+cudaError_t launch_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
+                            const uint64_t *indices, const double *data, const double *v,
+                            double *y, int nsm, cudaStream_t st);
 
 }  // namespace qr

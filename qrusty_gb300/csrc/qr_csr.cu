@@ -49,6 +49,10 @@ __global__ void __launch_bounds__(256) csr_fill_kernel(const CsrArgs a) {
             vr = __dadd_rn(vr, cr);
             vi = __dadd_rn(vi, ci);
         }
+        if (pos < 0 || (uint64_t)pos >= a.G) {  // cannot happen for a valid trie table
+            atomicExch(a.err, kErrCsrPos);
+            continue;
+        }
         const uint64_t o = rr * a.G + (uint64_t)pos;
         a.indices[o] = r ^ a.gx[g];
         reinterpret_cast<double2 *>(a.data)[o] = make_double2(vr, vi);
@@ -76,7 +80,8 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
 // y = A v, complex128.  One warp per row; lanes stride the row's entries and
 // the partial sums are combined with a butterfly.  Replaces
 // spmat_dot_densevec (qrusty/src/accel.rs:338-370).
-__global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, const uint64_t *indptr,
+__global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, uint64_t ncols,
+                                                       const uint64_t *indptr,
                                                        const uint64_t *indices,
                                                        const double2 *data, const double2 *v,
                                                        double2 *y) {
@@ -87,8 +92,10 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, const uin
         const uint64_t j0 = indptr[r], j1 = indptr[r + 1];
         double sr = 0.0, si = 0.0;
         for (uint64_t j = j0 + lane; j < j1; j += 32) {
+            const uint64_t c = indices[j];
+            if (c >= ncols) continue;  // out-of-range column: skipped
             const double2 d = data[j];
-            const double2 x = v[indices[j]];
+            const double2 x = v[c];
             sr = fma(d.x, x.x, fma(-d.y, x.y, sr));
             si = fma(d.x, x.y, fma(d.y, x.x, si));
         }
@@ -101,13 +108,13 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, const uin
     }
 }
 
-cudaError_t launch_csr_spmv(uint64_t nrows, const uint64_t *indptr, const uint64_t *indices,
-                            const double *data, const double *v, double *y, int nsm,
-                            cudaStream_t st) {
+cudaError_t launch_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
+                            const uint64_t *indices, const double *data, const double *v,
+                            double *y, int nsm, cudaStream_t st) {
     if (nrows == 0) return cudaSuccess;
     uint64_t g = (nrows + 7) / 8;
     if (g > (uint64_t)nsm * 32) g = (uint64_t)nsm * 32;
-    csr_spmv_kernel<<<(unsigned)g, 256, 0, st>>>(nrows, indptr, indices,
+    csr_spmv_kernel<<<(unsigned)g, 256, 0, st>>>(nrows, ncols, indptr, indices,
                                                  reinterpret_cast<const double2 *>(data),
                                                  reinterpret_cast<const double2 *>(v),
                                                  reinterpret_cast<double2 *>(y));

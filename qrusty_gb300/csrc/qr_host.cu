@@ -466,7 +466,9 @@ int check_kernel_error(qr_op *op) {
     if (h != kErrNone) {
         int z = 0;
         cudaMemcpy(op->d_err.p, &z, sizeof(int), cudaMemcpyHostToDevice);
-        return fail(QR_EKERNEL, "kernel reported error %d (bounded mbarrier wait expired)", h);
+        return fail(QR_EKERNEL, "kernel reported error %d (%s)", h,
+                    h == kErrMbarTimeout ? "bounded mbarrier wait expired"
+                                         : "CSR position out of range");
     }
     return QR_OK;
 }
@@ -596,6 +598,7 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, i
     a.eoff = op->d_eoff.as<uint32_t>();
     a.ebit = op->d_ebit.as<uint8_t>();
     a.esig = op->d_esig.as<int64_t>();
+    a.err = op->d_err.as<int>();
     if (mem == QR_MEM_DEVICE) {
         a.indptr = indptr;
         a.indices = indices;
@@ -633,7 +636,7 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, i
                             cudaMemcpyDeviceToHost, st),
             "copy indptr");
     QR_CUDA(cudaStreamSynchronize(st), "csr build sync");
-    return QR_OK;
+    return check_kernel_error(op);
 }
 
 int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates, int32_t adjoint,
@@ -710,13 +713,13 @@ int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host, 
     return check_kernel_error(op);
 }
 
-int qr_csr_spmv(uint64_t nrows, const uint64_t *indptr, const uint64_t *indices,
+int qr_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr, const uint64_t *indices,
                 const double *data, const double *v, double *y, void *stream) {
     if (!indptr || !indices || !data || !v || !y) return fail(QR_EINVAL, "qr_csr_spmv: null argument");
     int dev = 0, nsm = 0;
     QR_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     QR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "device attribute");
-    QR_CUDA(launch_csr_spmv(nrows, indptr, indices, data, v, y, nsm,
+    QR_CUDA(launch_csr_spmv(nrows, ncols, indptr, indices, data, v, y, nsm,
                             static_cast<cudaStream_t>(stream)),
             "csr spmv launch");
     return QR_OK;

@@ -433,12 +433,16 @@ def spmat_dot_densevec(spmat: SpMat, x):
     if xv.ndim != 1 or xv.shape[0] != shape[1]:
         raise Exception("spmat_dot_densevec: vector length %d != %d columns"
                         % (xv.shape[0] if xv.ndim else 0, shape[1]))
+    ip_h, data_h = spmat._it[3], spmat._it[1]
+    if len(ip_h) != shape[0] + 1 or int(ip_h[-1]) != len(data_h) or \
+            np.any(np.diff(ip_h.astype(np.int64)) < 0):
+        raise Exception("spmat_dot_densevec: malformed CSR row pointers")
     indptr, indices, data = spmat._device()
     dev = data.device
     xd = torch.from_numpy(xv).to(dev)
     yd = torch.empty(shape[0], dtype=torch.complex128, device=dev)
     st = torch.cuda.current_stream(dev).cuda_stream
-    check(_lib.load().qr_csr_spmv(shape[0], indptr.data_ptr(), indices.data_ptr(),
+    check(_lib.load().qr_csr_spmv(shape[0], shape[1], indptr.data_ptr(), indices.data_ptr(),
                                   data.data_ptr(), xd.data_ptr(), yd.data_ptr(), st))
     return yd.cpu().numpy()
 

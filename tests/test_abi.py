@@ -69,7 +69,7 @@ def test_null_handles_rejected():
     assert L.qr_apply(None, 0, None, None, 1, 0, None) == _lib.QR_EINVAL
     assert L.qr_csr_build(None, None, None, None, 0, None) == _lib.QR_EINVAL
     assert L.qr_op_destroy(None) == _lib.QR_OK
-    assert L.qr_csr_spmv(4, None, None, None, None, None, None) == _lib.QR_EINVAL
+    assert L.qr_csr_spmv(4, 4, None, None, None, None, None, None) == _lib.QR_EINVAL
     buf = C.create_string_buffer(8)
     n = L.qr_last_error(buf, 8)
     assert n >= len(buf.value) and len(buf.value) <= 7
