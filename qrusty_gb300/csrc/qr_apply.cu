@@ -318,6 +318,220 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
     }
 }
 
+// ---------------------------------------------------------------- c64c kernel
+// Compensated complex64 path.  The host splits every x-group into sub-groups
+// whose z masks agree on the thread's register bits (tile bits
+// [kTb, kTb + log2 AMPS)), so a sub-group's factor is, per thread,
+//     D_m = (-1)^popc(m & zm) * Dt,
+// with Dt a thread constant (table entry with the thread's sign folded in)
+// and zm the sub-group's z bits on the register bits.  The sign pattern over
+// m is dispatched to a compile-time instantiation, so the inner step per
+// amplitude is one shared-memory load and two packed FMAs:
+//     A_m += (+-Dt.re) * p,  B_m += (+-Dt.im) * p      (fma.rn.f32x2)
+// and y = A + iB is folded into the running (hi, lo) two-sum pair every
+// kFlush blocks.
+constexpr int kTb = 9;          // log2(threads) whenever AMPS >= 2
+constexpr int kMsh = kTb + 3;   // byte shift of the register index m
+constexpr int kFlush = 4;       // blocks per compensated fold
+
+template <int AMPS, int ZM>
+__device__ __forceinline__ void group_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                          const unsigned char *sb, uint32_t off, float2 D) {
+    const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
+    const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        const float2 p = *reinterpret_cast<const float2 *>(sb + (off ^ ((uint32_t)m << kMsh)));
+        const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
+        A[m] = __ffma2_rn(neg ? an : ap, p, A[m]);
+        B[m] = __ffma2_rn(neg ? bn : bp, p, B[m]);
+    }
+}
+
+template <int AMPS>
+__device__ __forceinline__ void group_c64_dispatch(uint32_t zm, float2 (&A)[AMPS],
+                                                   float2 (&B)[AMPS], const unsigned char *sb,
+                                                   uint32_t off, float2 D) {
+#define QR_ZM_CASE(k)                                                 \
+    case k:                                                           \
+        if constexpr (k < AMPS) group_c64<AMPS, k>(A, B, sb, off, D); \
+        break;
+    switch (zm) {
+        QR_ZM_CASE(0) QR_ZM_CASE(1) QR_ZM_CASE(2) QR_ZM_CASE(3)
+        QR_ZM_CASE(4) QR_ZM_CASE(5) QR_ZM_CASE(6) QR_ZM_CASE(7)
+        QR_ZM_CASE(8) QR_ZM_CASE(9) QR_ZM_CASE(10) QR_ZM_CASE(11)
+        QR_ZM_CASE(12) QR_ZM_CASE(13) QR_ZM_CASE(14) QR_ZM_CASE(15)
+        default: break;
+    }
+#undef QR_ZM_CASE
+}
+
+template <int AMPS>
+__global__ void __launch_bounds__(512, 1) apply_c64c(const ApplyArgs a, int stages) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const uint32_t threads = blockDim.x;
+    const uint32_t t = threadIdx.x;
+    const uint32_t tile = 1u << a.b;
+    const uint32_t tile_bytes = tile * 8u;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)stages * tile_bytes);
+
+    const float2 *psi = static_cast<const float2 *>(a.psi);
+    float2 *y = static_cast<float2 *>(a.y);
+    const float2 *tables = static_cast<const float2 *>(a.tables);
+    const float2 *fat_c = static_cast<const float2 *>(a.fat_c);
+    const float2 *diag = static_cast<const float2 *>(a.diag);
+    const uint32_t nb = a.nblocks;
+    const uint32_t tmask = threads - 1;
+
+    const uint64_t first = blockIdx.x;
+    const uint64_t my_items =
+        a.nitems > first ? (a.nitems - first + gridDim.x - 1) / gridDim.x : 0;
+    const uint64_t total = my_items * nb;
+    if (total == 0) return;
+
+    if (t == 0) {
+        for (int s = 0; s < stages; ++s) mbar_init(&full[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](uint64_t L) {
+        const uint64_t k = L / nb;
+        const uint32_t j = (uint32_t)(L - k * nb);
+        const uint64_t item = first + k * gridDim.x;
+        const uint64_t st = item / a.ntiles;
+        const uint64_t q = item - st * a.ntiles;
+        const float2 *src = psi + st * a.N + ((q ^ a.blk_hi[j]) << a.b);
+        const int s = (int)(L % (uint64_t)stages);
+        mbar_expect_tx(&full[s], tile_bytes);
+        bulk_g2s(smem_raw + (size_t)s * tile_bytes, src, tile_bytes, &full[s]);
+    };
+    if (t == 0) {
+        const uint64_t pro = total < (uint64_t)stages ? total : (uint64_t)stages;
+        for (uint64_t L = 0; L < pro; ++L) issue(L);
+    }
+
+    float2 A[AMPS], B[AMPS], hi[AMPS], lo[AMPS];
+
+    for (uint64_t L = 0; L < total; ++L) {
+        const uint64_t k = L / nb;
+        const uint32_t j = (uint32_t)(L - k * nb);
+        const uint64_t item = first + k * gridDim.x;
+        const uint64_t st = item / a.ntiles;
+        const uint64_t q = item - st * a.ntiles;
+        if (j == 0) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                A[m] = B[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
+            }
+        }
+        const int s = (int)(L % (uint64_t)stages);
+        const uint32_t par = (uint32_t)((L / (uint64_t)stages) & 1ull);
+        const bool ok = mbar_wait_bounded(&full[s], par, kWaitLimitNs);
+        const uint32_t soff = (uint32_t)s * tile_bytes;
+
+        if ((int)j == a.diag_block && diag != nullptr) {
+            const float2 *dg = diag + (q << a.b);
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const uint32_t rl = t + threads * (uint32_t)m;
+                const float2 d = dg[rl];
+                const float2 p = *reinterpret_cast<const float2 *>(smem_raw + soff + rl * 8u);
+                A[m] = __ffma2_rn(make_float2(d.x, d.x), p, A[m]);
+                B[m] = __ffma2_rn(make_float2(d.y, d.y), p, B[m]);
+            }
+        }
+
+        const uint32_t g1 = a.blk_g0[j + 1];
+        for (uint32_t g = a.blk_g0[j]; g < g1; ++g) {
+            const GroupDesc gd = a.groups[g];
+            const uint32_t lo_t = gd.lo & tmask;
+            const uint32_t lo_m = gd.lo >> a.tb;
+            const uint32_t off = soff | ((t ^ lo_t) << 3) | (lo_m << kMsh);
+            const uint64_t rbase = (q << a.b) | t;
+            if (gd.d != kFat) {
+                uint32_t u = 0;
+#pragma unroll
+                for (int i = 0; i < kDMax; ++i)
+                    if (i < (int)gd.d) u |= ((uint32_t)__popcll(rbase & gd.beta[i]) & 1u) << i;
+                float2 D = tables[gd.off + u];
+                if (__popcll(rbase & gd.z0) & 1) {
+                    D.x = -D.x;
+                    D.y = -D.y;
+                }
+                const uint32_t zm = (uint32_t)(gd.z0 >> a.tb) & (AMPS - 1);
+                group_c64_dispatch<AMPS>(zm, A, B, smem_raw, off, D);
+            } else {
+#pragma unroll
+                for (int m = 0; m < AMPS; ++m) {
+                    const uint64_t r = rbase | ((uint64_t)m << a.tb);
+                    float dr = 0.f, di = 0.f;
+                    for (uint32_t kk = 0; kk < gd.cnt; ++kk) {
+                        const uint64_t zk = a.fat_z[gd.off + kk];
+                        const float2 ck = fat_c[gd.off + kk];
+                        const bool ng = (__popcll(r & zk) & 1) != 0;
+                        dr += ng ? -ck.x : ck.x;
+                        di += ng ? -ck.y : ck.y;
+                    }
+                    const float2 p = *reinterpret_cast<const float2 *>(
+                        smem_raw + (off ^ ((uint32_t)m << kMsh)));
+                    A[m] = __ffma2_rn(make_float2(dr, dr), p, A[m]);
+                    B[m] = __ffma2_rn(make_float2(di, di), p, B[m]);
+                }
+            }
+        }
+
+        const bool last = (j == nb - 1);
+        if (last || (j % kFlush) == kFlush - 1) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const float yr = __fsub_rn(A[m].x, B[m].y);
+                const float yi = __fadd_rn(A[m].y, B[m].x);
+                two_sum_into(hi[m].x, lo[m].x, yr);
+                two_sum_into(hi[m].y, lo[m].y, yi);
+                A[m] = B[m] = make_float2(0.f, 0.f);
+            }
+        }
+        if (last) {
+            float2 *yo = y + st * a.N + (q << a.b);
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m)
+                yo[t + threads * (uint32_t)m] =
+                    make_float2(__fadd_rn(hi[m].x, lo[m].x), __fadd_rn(hi[m].y, lo[m].y));
+        }
+
+        if (__syncthreads_or(ok ? 0 : 1)) {
+            if (t == 0) {
+                atomicExch(a.err, kErrMbarTimeout);
+                for (uint64_t L2 = L; L2 < total && L2 < L + (uint64_t)stages; ++L2) {
+                    const int s2 = (int)(L2 % (uint64_t)stages);
+                    mbar_wait_bounded(&full[s2], (uint32_t)((L2 / stages) & 1ull), kWaitLimitNs);
+                }
+            }
+            return;
+        }
+        if (t == 0 && L + (uint64_t)stages < total) issue(L + (uint64_t)stages);
+    }
+}
+
+template <int AMPS>
+static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
+    const uint32_t tile_bytes = (1u << a.b) * 8u;
+    int stages = (int)((200u * 1024u) / tile_bytes);
+    if (stages > kMaxStages) stages = kMaxStages;
+    if (stages < 2) stages = 2;
+    const size_t smem = (size_t)stages * tile_bytes + kMaxStages * sizeof(uint64_t);
+    auto kern = apply_c64c<AMPS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    uint64_t grid = a.nitems < (uint64_t)nsm ? a.nitems : (uint64_t)nsm;
+    if (grid == 0) return cudaSuccess;
+    kern<<<(unsigned)grid, threads, smem, st>>>(a, stages);
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <typename Real, int AMPS, bool COMP>
 static cudaError_t launch_one(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
     const uint32_t tile_bytes = (1u << a.b) * (uint32_t)sizeof(Cplx<Real>);
@@ -352,7 +566,14 @@ static cudaError_t dispatch_amps(const ApplyArgs &a, int amps, int threads, int 
 cudaError_t launch_apply(int dtype, const ApplyArgs &a, int amps, int threads, int nsm,
                          cudaStream_t st) {
     if (dtype == 0) return dispatch_amps<double, false>(a, amps, threads, nsm, st);
-    return dispatch_amps<float, true>(a, amps, threads, nsm, st);
+    if (amps >= 2 && a.tb != kTb) return cudaErrorInvalidValue;
+    switch (amps) {
+        case 1: return launch_c64c<1>(a, threads, nsm, st);
+        case 2: return launch_c64c<2>(a, threads, nsm, st);
+        case 4: return launch_c64c<4>(a, threads, nsm, st);
+        case 8: return launch_c64c<8>(a, threads, nsm, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 // ---------------------------------------------------------------- diagonal

@@ -283,7 +283,7 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
     if (op->mx.empty()) merge_terms(op);
     const int n = op->n;
     const bool f32 = dtype == QR_C64C;
-    pl.b = std::min(n, f32 ? 13 : 12);
+    pl.b = std::min(n, 12);
     const int tmax = f32 ? 512 : 256;
     pl.threads = std::min(1 << pl.b, tmax);
     pl.amps = (1 << pl.b) / pl.threads;
@@ -327,53 +327,78 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
     std::vector<uint64_t> fz;
     std::vector<unsigned char> fc;
     uint32_t ntab = 0, nfat_terms = 0;
+    // The compensated-c64 kernel keeps a sub-group's factor thread-constant
+    // up to a Walsh sign over the register bits [tb, tb + log2 amps): split
+    // each x-group by its terms' z bits there.  The c128 kernel does not split.
+    int abits = 0;
+    while ((1 << abits) < pl.amps) ++abits;
+    const uint64_t mmask = f32 ? (((1ull << abits) - 1) << pl.tb) : 0;
     for (size_t g = 0; g < gxs.size(); ++g) {
-        std::vector<uint64_t> zs;
-        for (size_t k : members[g]) zs.push_back(op->mz[k]);
-        Span sp = gf2_span(zs, kDMax);
-        if (gxs[g] == 0 && sp.overflow) {
-            diag_terms = members[g];
-            continue;
+        if (gxs[g] == 0) {
+            std::vector<uint64_t> zs;
+            for (size_t k : members[g]) zs.push_back(op->mz[k]);
+            if (gf2_span(zs, kDMax).overflow) {
+                diag_terms = members[g];
+                continue;
+            }
         }
-        GroupDesc d;
-        memset(&d, 0, sizeof(d));
-        d.z0 = zs[0];
-        d.lo = (uint32_t)(gxs[g] & tmask);
-        if (!sp.overflow) {
-            d.d = (uint32_t)sp.basis.size();
-            for (size_t i = 0; i < sp.basis.size(); ++i) d.beta[i] = sp.basis[i];
-            d.off = ntab;
-            const uint32_t ent = 1u << d.d;
-            for (uint32_t u = 0; u < ent; ++u) {
-                cd s{0.0, 0.0};
-                for (size_t kk = 0; kk < members[g].size(); ++kk) {
-                    const cd v = c[members[g][kk]];
-                    if (__builtin_popcount(u & sp.coord[kk]) & 1) {
-                        s.re -= v.re;
-                        s.im -= v.im;
-                    } else {
-                        s.re += v.re;
-                        s.im += v.im;
+        // partitions by z & mmask, in first-occurrence order
+        std::vector<uint64_t> pkeys;
+        std::vector<std::vector<size_t>> parts;
+        for (size_t k : members[g]) {
+            const uint64_t key = op->mz[k] & mmask;
+            size_t pi = 0;
+            while (pi < pkeys.size() && pkeys[pi] != key) ++pi;
+            if (pi == pkeys.size()) {
+                pkeys.push_back(key);
+                parts.emplace_back();
+            }
+            parts[pi].push_back(k);
+        }
+        for (const auto &part : parts) {
+            std::vector<uint64_t> zs;
+            for (size_t k : part) zs.push_back(op->mz[k]);
+            Span sp = gf2_span(zs, kDMax);
+            GroupDesc d;
+            memset(&d, 0, sizeof(d));
+            d.z0 = zs[0];
+            d.lo = (uint32_t)(gxs[g] & tmask);
+            if (!sp.overflow) {
+                d.d = (uint32_t)sp.basis.size();
+                for (size_t i = 0; i < sp.basis.size(); ++i) d.beta[i] = sp.basis[i];
+                d.off = ntab;
+                const uint32_t ent = 1u << d.d;
+                for (uint32_t u = 0; u < ent; ++u) {
+                    cd acc{0.0, 0.0};
+                    for (size_t kk = 0; kk < part.size(); ++kk) {
+                        const cd v = c[part[kk]];
+                        if (__builtin_popcount(u & sp.coord[kk]) & 1) {
+                            acc.re -= v.re;
+                            acc.im -= v.im;
+                        } else {
+                            acc.re += v.re;
+                            acc.im += v.im;
+                        }
                     }
+                    if (f32) push_cplx<float>(tab, acc);
+                    else push_cplx<double>(tab, acc);
                 }
-                if (f32) push_cplx<float>(tab, s);
-                else push_cplx<double>(tab, s);
+                ntab += ent;
+            } else {
+                d.d = kFat;
+                d.off = nfat_terms;
+                d.cnt = (uint32_t)part.size();
+                for (size_t k : part) {
+                    fz.push_back(op->mz[k]);
+                    if (f32) push_cplx<float>(fc, c[k]);
+                    else push_cplx<double>(fc, c[k]);
+                }
+                nfat_terms += d.cnt;
+                pl.nfat++;
             }
-            ntab += ent;
-        } else {
-            d.d = kFat;
-            d.off = nfat_terms;
-            d.cnt = (uint32_t)members[g].size();
-            for (size_t k : members[g]) {
-                fz.push_back(op->mz[k]);
-                if (f32) push_cplx<float>(fc, c[k]);
-                else push_cplx<double>(fc, c[k]);
-            }
-            nfat_terms += d.cnt;
-            pl.nfat++;
+            descs.push_back(d);
+            desc_hi.push_back(gxs[g] >> pl.b);
         }
-        descs.push_back(d);
-        desc_hi.push_back(gxs[g] >> pl.b);
     }
     pl.has_diag = !diag_terms.empty();
     // blocks: distinct partner-tile XOR values, ascending; a hi == 0 block
