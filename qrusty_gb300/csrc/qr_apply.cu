@@ -319,42 +319,62 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 }
 
 // ---------------------------------------------------------------- c64c kernel
-// Compensated complex64 path.  The host splits every x-group into sub-groups
-// whose z masks agree on the thread's register bits (tile bits
-// [kTb, kTb + log2 AMPS)), so a sub-group's factor is, per thread,
+// Compensated complex64 path.  256 threads x AMPS = 16 amplitudes per 4096-
+// amplitude tile; thread t owns r_lo = t + 256 m.  The host splits every
+// x-group into sub-groups whose z masks agree on the register bits
+// [kTb, kTb + log2 AMPS), so for a thread the sub-group's factor is
 //     D_m = (-1)^popc(m & zm) * Dt,
-// with Dt a thread constant (table entry with the thread's sign folded in)
-// and zm the sub-group's z bits on the register bits.  The sign pattern over
-// m is dispatched to a compile-time instantiation, so the inner step per
-// amplitude is one shared-memory load and two packed FMAs:
+// Dt = +-table[u] with (sign, u) = the thread's precomputed parity code XOR
+// the tile's parity code (computed once per tile into shared memory).
+// Sub-groups of a block are sorted into runs of equal zm, so one dispatch
+// per run selects a compile-time sign pattern; the inner step per amplitude
+// is one shared-memory load and two packed FMAs:
 //     A_m += (+-Dt.re) * p,  B_m += (+-Dt.im) * p      (fma.rn.f32x2)
 // and y = A + iB is folded into the running (hi, lo) two-sum pair every
 // kFlush blocks.
-constexpr int kTb = 9;          // log2(threads) whenever AMPS >= 2
+constexpr int kTb = 8;          // log2(threads) whenever AMPS >= 2
 constexpr int kMsh = kTb + 3;   // byte shift of the register index m
 constexpr int kFlush = 4;       // blocks per compensated fold
+constexpr int kC64Threads = 256;
 
 template <int AMPS, int ZM>
-__device__ __forceinline__ void group_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                          const unsigned char *sb, uint32_t off, float2 D) {
-    const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
-    const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
+__device__ __forceinline__ void run_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                        const unsigned char *sm, uint32_t soff, uint32_t t,
+                                        uint32_t tmask, int tb, const ApplyArgs &a,
+                                        const float2 *tables, const uint8_t *s_tq, uint32_t g0,
+                                        uint32_t g1, uint32_t threads) {
+    for (uint32_t g = g0; g < g1; ++g) {
+        const uint4 sd = a.sub[g];
+        const uint32_t cu = (uint32_t)a.codes[(size_t)g * threads + t] ^ (uint32_t)s_tq[g];
+        float2 D = tables[sd.y + (cu >> 1)];
+        if (cu & 1u) {
+            D.x = -D.x;
+            D.y = -D.y;
+        }
+        const uint32_t off = soff | ((t ^ (sd.x & tmask)) << 3) | ((sd.x >> tb) << kMsh);
+        const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
+        const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
 #pragma unroll
-    for (int m = 0; m < AMPS; ++m) {
-        const float2 p = *reinterpret_cast<const float2 *>(sb + (off ^ ((uint32_t)m << kMsh)));
-        const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
-        A[m] = __ffma2_rn(neg ? an : ap, p, A[m]);
-        B[m] = __ffma2_rn(neg ? bn : bp, p, B[m]);
+        for (int m = 0; m < AMPS; ++m) {
+            const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << kMsh)));
+            const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
+            A[m] = __ffma2_rn(neg ? an : ap, p, A[m]);
+            B[m] = __ffma2_rn(neg ? bn : bp, p, B[m]);
+        }
     }
 }
 
 template <int AMPS>
-__device__ __forceinline__ void group_c64_dispatch(uint32_t zm, float2 (&A)[AMPS],
-                                                   float2 (&B)[AMPS], const unsigned char *sb,
-                                                   uint32_t off, float2 D) {
-#define QR_ZM_CASE(k)                                                 \
-    case k:                                                           \
-        if constexpr (k < AMPS) group_c64<AMPS, k>(A, B, sb, off, D); \
+__device__ __forceinline__ void run_c64_dispatch(uint32_t zm, float2 (&A)[AMPS],
+                                                 float2 (&B)[AMPS], const unsigned char *sm,
+                                                 uint32_t soff, uint32_t t, uint32_t tmask,
+                                                 int tb, const ApplyArgs &a, const float2 *tables,
+                                                 const uint8_t *s_tq, uint32_t g0, uint32_t g1,
+                                                 uint32_t threads) {
+#define QR_ZM_CASE(k)                                                                        \
+    case k:                                                                                  \
+        if constexpr (k < AMPS)                                                              \
+            run_c64<AMPS, k>(A, B, sm, soff, t, tmask, tb, a, tables, s_tq, g0, g1, threads); \
         break;
     switch (zm) {
         QR_ZM_CASE(0) QR_ZM_CASE(1) QR_ZM_CASE(2) QR_ZM_CASE(3)
@@ -367,13 +387,14 @@ __device__ __forceinline__ void group_c64_dispatch(uint32_t zm, float2 (&A)[AMPS
 }
 
 template <int AMPS>
-__global__ void __launch_bounds__(512, 1) apply_c64c(const ApplyArgs a, int stages) {
+__global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a, int stages) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t threads = blockDim.x;
     const uint32_t t = threadIdx.x;
     const uint32_t tile = 1u << a.b;
     const uint32_t tile_bytes = tile * 8u;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)stages * tile_bytes);
+    uint8_t *s_tq = reinterpret_cast<uint8_t *>(full + kMaxStages);
 
     const float2 *psi = static_cast<const float2 *>(a.psi);
     float2 *y = static_cast<float2 *>(a.y);
@@ -421,9 +442,18 @@ __global__ void __launch_bounds__(512, 1) apply_c64c(const ApplyArgs a, int stag
         const uint64_t q = item - st * a.ntiles;
         if (j == 0) {
 #pragma unroll
-            for (int m = 0; m < AMPS; ++m) {
-                A[m] = B[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
+            for (int m = 0; m < AMPS; ++m) A[m] = B[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
+            // tile parity codes of every sub-group: bit 0 = popc(q & z0 >> b),
+            // bit i+1 = popc(q & beta_i >> b)
+            for (uint32_t g = t; g < a.nsub; g += threads) {
+                const uint64_t *h = a.sub_hi + 5 * (size_t)g;
+                uint32_t c = (uint32_t)__popcll(q & h[0]) & 1u;
+#pragma unroll
+                for (int i = 0; i < kDMax; ++i)
+                    c |= ((uint32_t)__popcll(q & h[1 + i]) & 1u) << (i + 1);
+                s_tq[g] = (uint8_t)c;
             }
+            __syncthreads();
         }
         const int s = (int)(L % (uint64_t)stages);
         const uint32_t par = (uint32_t)((L / (uint64_t)stages) & 1ull);
@@ -442,41 +472,35 @@ __global__ void __launch_bounds__(512, 1) apply_c64c(const ApplyArgs a, int stag
             }
         }
 
-        const uint32_t g1 = a.blk_g0[j + 1];
-        for (uint32_t g = a.blk_g0[j]; g < g1; ++g) {
-            const GroupDesc gd = a.groups[g];
-            const uint32_t lo_t = gd.lo & tmask;
-            const uint32_t lo_m = gd.lo >> a.tb;
-            const uint32_t off = soff | ((t ^ lo_t) << 3) | (lo_m << kMsh);
-            const uint64_t rbase = (q << a.b) | t;
-            if (gd.d != kFat) {
-                uint32_t u = 0;
-#pragma unroll
-                for (int i = 0; i < kDMax; ++i)
-                    if (i < (int)gd.d) u |= ((uint32_t)__popcll(rbase & gd.beta[i]) & 1u) << i;
-                float2 D = tables[gd.off + u];
-                if (__popcll(rbase & gd.z0) & 1) {
-                    D.x = -D.x;
-                    D.y = -D.y;
-                }
-                const uint32_t zm = (uint32_t)(gd.z0 >> a.tb) & (AMPS - 1);
-                group_c64_dispatch<AMPS>(zm, A, B, smem_raw, off, D);
+        const uint32_t r1 = a.blk_r0[j + 1];
+        for (uint32_t r = a.blk_r0[j]; r < r1; ++r) {
+            const uint32_t zm = a.run_zm[r];
+            const uint32_t g0 = a.run_g0[r], g1 = a.run_g0[r + 1];
+            if (zm != kFat) {
+                run_c64_dispatch<AMPS>(zm, A, B, smem_raw, soff, t, tmask, a.tb, a, tables, s_tq,
+                                       g0, g1, threads);
             } else {
+                const uint64_t rbase = (q << a.b) | t;
+                for (uint32_t g = g0; g < g1; ++g) {
+                    const uint4 sd = a.sub[g];
+                    const uint32_t off =
+                        soff | ((t ^ (sd.x & tmask)) << 3) | ((sd.x >> a.tb) << kMsh);
 #pragma unroll
-                for (int m = 0; m < AMPS; ++m) {
-                    const uint64_t r = rbase | ((uint64_t)m << a.tb);
-                    float dr = 0.f, di = 0.f;
-                    for (uint32_t kk = 0; kk < gd.cnt; ++kk) {
-                        const uint64_t zk = a.fat_z[gd.off + kk];
-                        const float2 ck = fat_c[gd.off + kk];
-                        const bool ng = (__popcll(r & zk) & 1) != 0;
-                        dr += ng ? -ck.x : ck.x;
-                        di += ng ? -ck.y : ck.y;
+                    for (int m = 0; m < AMPS; ++m) {
+                        const uint64_t rr = rbase | ((uint64_t)m << a.tb);
+                        float dr = 0.f, di = 0.f;
+                        for (uint32_t kk = 0; kk < sd.w; ++kk) {
+                            const uint64_t zk = a.fat_z[sd.y + kk];
+                            const float2 ck = fat_c[sd.y + kk];
+                            const bool ng = (__popcll(rr & zk) & 1) != 0;
+                            dr += ng ? -ck.x : ck.x;
+                            di += ng ? -ck.y : ck.y;
+                        }
+                        const float2 p = *reinterpret_cast<const float2 *>(
+                            smem_raw + (off ^ ((uint32_t)m << kMsh)));
+                        A[m] = __ffma2_rn(make_float2(dr, dr), p, A[m]);
+                        B[m] = __ffma2_rn(make_float2(di, di), p, B[m]);
                     }
-                    const float2 p = *reinterpret_cast<const float2 *>(
-                        smem_raw + (off ^ ((uint32_t)m << kMsh)));
-                    A[m] = __ffma2_rn(make_float2(dr, dr), p, A[m]);
-                    B[m] = __ffma2_rn(make_float2(di, di), p, B[m]);
                 }
             }
         }
@@ -517,10 +541,12 @@ __global__ void __launch_bounds__(512, 1) apply_c64c(const ApplyArgs a, int stag
 template <int AMPS>
 static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
     const uint32_t tile_bytes = (1u << a.b) * 8u;
-    int stages = (int)((200u * 1024u) / tile_bytes);
+    int stages = (int)((160u * 1024u) / tile_bytes);
     if (stages > kMaxStages) stages = kMaxStages;
     if (stages < 2) stages = 2;
-    const size_t smem = (size_t)stages * tile_bytes + kMaxStages * sizeof(uint64_t);
+    const size_t smem = (size_t)stages * tile_bytes + kMaxStages * sizeof(uint64_t) +
+                        (((size_t)a.nsub + 15) & ~(size_t)15);
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
     auto kern = apply_c64c<AMPS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -572,6 +598,7 @@ cudaError_t launch_apply(int dtype, const ApplyArgs &a, int amps, int threads, i
         case 2: return launch_c64c<2>(a, threads, nsm, st);
         case 4: return launch_c64c<4>(a, threads, nsm, st);
         case 8: return launch_c64c<8>(a, threads, nsm, st);
+        case 16: return launch_c64c<16>(a, threads, nsm, st);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -50,6 +50,14 @@ struct ApplyArgs {
     const void *diag;       // Cplx<Real>[N] or null (only read in block hi == 0)
     int diag_block;         // index of the hi == 0 block, or -1
     int *err;               // device error word
+    // compensated-c64 plan (sub-groups in same-sign runs; see qr_apply.cu)
+    const uint4 *sub;       // per sub-group: {lo, table or fat offset, kind, fat count}
+    const uint64_t *sub_hi; // per sub-group: 5 masks >> b (z0, beta[0..3]) for tile parities
+    const uint8_t *codes;   // per sub-group x thread: thread parity code (sign | u << 1)
+    const uint32_t *blk_r0; // runs of block j: [blk_r0[j], blk_r0[j+1])
+    const uint32_t *run_g0; // sub-groups of run r: [run_g0[r], run_g0[r+1])
+    const uint32_t *run_zm; // register-bit z pattern of run r, or kFat
+    uint32_t nsub;
 };
 
 // Device error codes written to the error word.

@@ -93,6 +93,9 @@ struct Plan {
     int diag_block = -1;
     bool has_diag = false;
     DevBuf groups, tables, fat_z, fat_c, blk_hi, blk_g0, diag;
+    // compensated-c64 kernel tables
+    uint32_t nsub = 0;
+    DevBuf sub, sub_hi, codes, blk_r0, run_g0, run_zm;
 };
 
 }  // namespace qr
@@ -277,6 +280,20 @@ void push_cplx(std::vector<unsigned char> &buf, cd v) {
     buf.insert(buf.end(), p, p + sizeof(c));
 }
 
+// One sub-group of the apply plan: terms sharing x (and, for the c64c
+// kernel, z on the register bits), with their FP64 table or term list.
+struct SubGroup {
+    uint64_t hi = 0;       // partner-tile XOR (x >> b)
+    uint32_t lo = 0;       // x & (tile - 1)
+    uint32_t zm = 0;       // z bits on the register bits (c64c), or kFat
+    uint64_t z0 = 0;
+    uint64_t beta[kDMax] = {0, 0, 0, 0};
+    uint32_t d = 0;        // rank, or kFat
+    std::vector<cd> table; // 2^d entries
+    std::vector<uint64_t> fz;
+    std::vector<cd> fc;
+};
+
 int build_plan(qr_op *op, int dtype, int adjoint) {
     Plan &pl = op->plans[dtype][adjoint];
     if (pl.built) return QR_OK;
@@ -284,7 +301,7 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
     const int n = op->n;
     const bool f32 = dtype == QR_C64C;
     pl.b = std::min(n, 12);
-    const int tmax = f32 ? 512 : 256;
+    const int tmax = f32 ? 256 : 256;
     pl.threads = std::min(1 << pl.b, tmax);
     pl.amps = (1 << pl.b) / pl.threads;
     pl.tb = 0;
@@ -319,20 +336,14 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
             members[it->second].push_back(k);
         }
     }
-    // diagonal group
-    std::vector<size_t> diag_terms;
-    std::vector<GroupDesc> descs;
-    std::vector<uint64_t> desc_hi;
-    std::vector<unsigned char> tab;
-    std::vector<uint64_t> fz;
-    std::vector<unsigned char> fc;
-    uint32_t ntab = 0, nfat_terms = 0;
     // The compensated-c64 kernel keeps a sub-group's factor thread-constant
     // up to a Walsh sign over the register bits [tb, tb + log2 amps): split
     // each x-group by its terms' z bits there.  The c128 kernel does not split.
     int abits = 0;
     while ((1 << abits) < pl.amps) ++abits;
     const uint64_t mmask = f32 ? (((1ull << abits) - 1) << pl.tb) : 0;
+    std::vector<size_t> diag_terms;
+    std::vector<SubGroup> subs;
     for (size_t g = 0; g < gxs.size(); ++g) {
         if (gxs[g] == 0) {
             std::vector<uint64_t> zs;
@@ -342,7 +353,6 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
                 continue;
             }
         }
-        // partitions by z & mmask, in first-occurrence order
         std::vector<uint64_t> pkeys;
         std::vector<std::vector<size_t>> parts;
         for (size_t k : members[g]) {
@@ -359,15 +369,15 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
             std::vector<uint64_t> zs;
             for (size_t k : part) zs.push_back(op->mz[k]);
             Span sp = gf2_span(zs, kDMax);
-            GroupDesc d;
-            memset(&d, 0, sizeof(d));
-            d.z0 = zs[0];
-            d.lo = (uint32_t)(gxs[g] & tmask);
+            SubGroup sg;
+            sg.hi = gxs[g] >> pl.b;
+            sg.lo = (uint32_t)(gxs[g] & tmask);
+            sg.z0 = zs[0];
             if (!sp.overflow) {
-                d.d = (uint32_t)sp.basis.size();
-                for (size_t i = 0; i < sp.basis.size(); ++i) d.beta[i] = sp.basis[i];
-                d.off = ntab;
-                const uint32_t ent = 1u << d.d;
+                sg.d = (uint32_t)sp.basis.size();
+                sg.zm = (uint32_t)((sg.z0 & mmask) >> pl.tb);
+                for (size_t i = 0; i < sp.basis.size(); ++i) sg.beta[i] = sp.basis[i];
+                const uint32_t ent = 1u << sg.d;
                 for (uint32_t u = 0; u < ent; ++u) {
                     cd acc{0.0, 0.0};
                     for (size_t kk = 0; kk < part.size(); ++kk) {
@@ -380,57 +390,128 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
                             acc.im += v.im;
                         }
                     }
-                    if (f32) push_cplx<float>(tab, acc);
-                    else push_cplx<double>(tab, acc);
+                    sg.table.push_back(acc);
                 }
-                ntab += ent;
             } else {
-                d.d = kFat;
-                d.off = nfat_terms;
-                d.cnt = (uint32_t)part.size();
+                sg.d = kFat;
+                sg.zm = kFat;
                 for (size_t k : part) {
-                    fz.push_back(op->mz[k]);
-                    if (f32) push_cplx<float>(fc, c[k]);
-                    else push_cplx<double>(fc, c[k]);
+                    sg.fz.push_back(op->mz[k]);
+                    sg.fc.push_back(c[k]);
                 }
-                nfat_terms += d.cnt;
-                pl.nfat++;
             }
-            descs.push_back(d);
-            desc_hi.push_back(gxs[g] >> pl.b);
+            subs.push_back(std::move(sg));
         }
     }
     pl.has_diag = !diag_terms.empty();
-    // blocks: distinct partner-tile XOR values, ascending; a hi == 0 block
-    // always exists when the diagonal vector is used
-    std::vector<size_t> ord(descs.size());
+    // order: partner tile ascending, then (c64c) run key zm with fat last
+    std::vector<size_t> ord(subs.size());
     for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
-    std::stable_sort(ord.begin(), ord.end(),
-                     [&](size_t a, size_t b) { return desc_hi[a] < desc_hi[b]; });
-    std::vector<GroupDesc> sdesc;
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+        if (subs[a].hi != subs[b].hi) return subs[a].hi < subs[b].hi;
+        return f32 && subs[a].zm < subs[b].zm;
+    });
     std::vector<uint64_t> bhi;
     std::vector<uint32_t> bg0;
-    if (pl.has_diag && (ord.empty() || desc_hi[ord[0]] != 0)) {
+    if (pl.has_diag && (ord.empty() || subs[ord[0]].hi != 0)) {
         bhi.push_back(0);
         bg0.push_back(0);
     }
-    for (size_t i : ord) {
-        const uint64_t h = desc_hi[i];
+    for (size_t i = 0; i < ord.size(); ++i) {
+        const uint64_t h = subs[ord[i]].hi;
         if (bhi.empty() || bhi.back() != h) {
             bhi.push_back(h);
-            bg0.push_back((uint32_t)sdesc.size());
+            bg0.push_back((uint32_t)i);
         }
-        sdesc.push_back(descs[i]);
     }
-    bg0.push_back((uint32_t)sdesc.size());
+    bg0.push_back((uint32_t)ord.size());
     pl.nblocks = (uint32_t)bhi.size();
-    pl.ngroups = sdesc.size();
+    pl.ngroups = ord.size();
     pl.diag_block = -1;
     for (size_t j = 0; j < bhi.size(); ++j)
         if (bhi[j] == 0) pl.diag_block = (int)j;
-    if (sdesc.empty()) sdesc.push_back(GroupDesc{});  // keep a valid pointer
 
-    QR_CUDA(pl.groups.upload(sdesc), "upload groups");
+    std::vector<unsigned char> tab, fc;
+    std::vector<uint64_t> fz;
+    uint32_t ntab = 0, nfat_terms = 0;
+    std::vector<GroupDesc> descs;           // c128 kernel
+    std::vector<uint4> sd;                  // c64c kernel
+    std::vector<uint64_t> shi;
+    std::vector<uint8_t> codes;
+    std::vector<uint32_t> r0, rg0, rzm;
+    pl.nfat = 0;
+    for (size_t i = 0; i < ord.size(); ++i) {
+        const SubGroup &sg = subs[ord[i]];
+        GroupDesc d;
+        memset(&d, 0, sizeof(d));
+        d.z0 = sg.z0;
+        d.lo = sg.lo;
+        d.d = sg.d;
+        for (int q = 0; q < kDMax; ++q) d.beta[q] = sg.beta[q];
+        uint4 u4;
+        u4.x = sg.lo;
+        u4.z = sg.d;
+        u4.w = 0;
+        if (sg.d != kFat) {
+            d.off = ntab;
+            u4.y = ntab;
+            for (const cd &v : sg.table) {
+                if (f32) push_cplx<float>(tab, v);
+                else push_cplx<double>(tab, v);
+            }
+            ntab += (uint32_t)sg.table.size();
+        } else {
+            d.off = nfat_terms;
+            d.cnt = (uint32_t)sg.fz.size();
+            u4.y = nfat_terms;
+            u4.w = d.cnt;
+            for (size_t k = 0; k < sg.fz.size(); ++k) {
+                fz.push_back(sg.fz[k]);
+                if (f32) push_cplx<float>(fc, sg.fc[k]);
+                else push_cplx<double>(fc, sg.fc[k]);
+            }
+            nfat_terms += d.cnt;
+            pl.nfat++;
+        }
+        descs.push_back(d);
+        if (f32) {
+            sd.push_back(u4);
+            shi.push_back(sg.z0 >> pl.b);
+            for (int q = 0; q < kDMax; ++q) shi.push_back(sg.beta[q] >> pl.b);
+            for (uint32_t t = 0; t < (uint32_t)pl.threads; ++t) {
+                uint32_t code = (uint32_t)__builtin_popcountll(t & sg.z0) & 1u;
+                if (sg.d != kFat)
+                    for (uint32_t q = 0; q < sg.d; ++q)
+                        code |= ((uint32_t)__builtin_popcountll(t & sg.beta[q]) & 1u) << (q + 1);
+                codes.push_back((uint8_t)code);
+            }
+        }
+    }
+    if (f32) {
+        // runs of equal zm inside each block
+        for (uint32_t j = 0; j < pl.nblocks; ++j) {
+            r0.push_back((uint32_t)rzm.size());
+            for (uint32_t g = bg0[j]; g < bg0[j + 1]; ++g) {
+                const uint32_t zm = subs[ord[g]].zm;
+                if (g == bg0[j] || zm != rzm.back()) {
+                    rzm.push_back(zm);
+                    rg0.push_back(g);
+                }
+            }
+        }
+        r0.push_back((uint32_t)rzm.size());
+        rg0.push_back((uint32_t)ord.size());
+        pl.nsub = (uint32_t)ord.size();
+        if (sd.empty()) sd.push_back(make_uint4(0, 0, 0, 0));
+        QR_CUDA(pl.sub.upload(sd), "upload sub-groups");
+        QR_CUDA(pl.sub_hi.upload(shi), "upload sub-group masks");
+        QR_CUDA(pl.codes.upload(codes), "upload thread codes");
+        QR_CUDA(pl.blk_r0.upload(r0), "upload block runs");
+        QR_CUDA(pl.run_g0.upload(rg0), "upload runs");
+        QR_CUDA(pl.run_zm.upload(rzm), "upload run patterns");
+    }
+    if (descs.empty()) descs.push_back(GroupDesc{});  // keep a valid pointer
+    QR_CUDA(pl.groups.upload(descs), "upload groups");
     QR_CUDA(pl.tables.upload(tab), "upload tables");
     QR_CUDA(pl.fat_z.upload(fz), "upload fat z");
     QR_CUDA(pl.fat_c.upload(fc), "upload fat c");
@@ -703,6 +784,13 @@ int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates
     a.diag = pl.has_diag ? pl.diag.p : nullptr;
     a.diag_block = pl.diag_block;
     a.err = op->d_err.as<int>();
+    a.sub = pl.sub.as<uint4>();
+    a.sub_hi = pl.sub_hi.as<uint64_t>();
+    a.codes = pl.codes.as<uint8_t>();
+    a.blk_r0 = pl.blk_r0.as<uint32_t>();
+    a.run_g0 = pl.run_g0.as<uint32_t>();
+    a.run_zm = pl.run_zm.as<uint32_t>();
+    a.nsub = pl.nsub;
     if (pl.nblocks == 0) {
         // operator without terms reachable here cannot happen (T >= 1); keep y defined
         QR_CUDA(cudaMemsetAsync(y, 0, bytes, static_cast<cudaStream_t>(stream)), "zero y");
