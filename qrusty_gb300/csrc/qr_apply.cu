@@ -323,58 +323,52 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 // amplitude tile; thread t owns r_lo = t + 256 m.  The host splits every
 // x-group into sub-groups whose z masks agree on the register bits
 // [kTb, kTb + log2 AMPS), so for a thread the sub-group's factor is
-//     D_m = (-1)^popc(m & zm) * Dt,
-// Dt = +-table[u] with (sign, u) = the thread's precomputed parity code XOR
-// the tile's parity code (computed once per tile into shared memory).
-// Sub-groups of a block are sorted into runs of equal zm, so one dispatch
-// per run selects a compile-time sign pattern; the inner step per amplitude
-// is one shared-memory load and two packed FMAs:
+//     D_m = (-1)^popc(m & zm) * Dt,   Dt = (-1)^popc(r0 & z0) * tab[u],
+// r0 = (tile << b) | t, u_i = popc(r0 & beta_i) & 1 (rank <= 2, table
+// inline in the 64-byte descriptor, read one sub-group ahead).  The sign
+// pattern over m selects a compile-time instantiation, so the inner step per
+// amplitude is one shared-memory load and two packed FMAs:
 //     A_m += (+-Dt.re) * p,  B_m += (+-Dt.im) * p      (fma.rn.f32x2)
 // and y = A + iB is folded into the running (hi, lo) two-sum pair every
-// kFlush blocks.
+// kFlush partner tiles.
+//
+// Pipeline: a kC64Stages-deep ring of partner tiles filled by 1-D TMA bulk
+// copies.  Warps run decoupled: each waits on the stage's full mbarrier,
+// consumes it, and counts itself out on a shared counter; the last warp out
+// refills the stage with the tile kC64Stages steps ahead.  No CTA-wide
+// barrier sits on the steady-state path.
 constexpr int kTb = 8;          // log2(threads) whenever AMPS >= 2
 constexpr int kMsh = kTb + 3;   // byte shift of the register index m
-constexpr int kFlush = 4;       // blocks per compensated fold
+constexpr int kFlush = 4;       // partner tiles per compensated fold
 constexpr int kC64Threads = 256;
+constexpr int kC64Stages = 6;
+
+template <bool WIDE>
+__device__ __forceinline__ uint32_t parity(uint64_t r, uint64_t m) {
+    if constexpr (WIDE) return (uint32_t)__popcll(r & m) & 1u;
+    else return (uint32_t)__popc((uint32_t)r & (uint32_t)m) & 1u;
+}
 
 template <int AMPS, int ZM>
-__device__ __forceinline__ void run_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                        const unsigned char *sm, uint32_t soff, uint32_t t,
-                                        uint32_t tmask, int tb, const ApplyArgs &a,
-                                        const float2 *tables, const uint8_t *s_tq, uint32_t g0,
-                                        uint32_t g1, uint32_t threads) {
-    for (uint32_t g = g0; g < g1; ++g) {
-        const uint4 sd = a.sub[g];
-        const uint32_t cu = (uint32_t)a.codes[(size_t)g * threads + t] ^ (uint32_t)s_tq[g];
-        float2 D = tables[sd.y + (cu >> 1)];
-        if (cu & 1u) {
-            D.x = -D.x;
-            D.y = -D.y;
-        }
-        const uint32_t off = soff | ((t ^ (sd.x & tmask)) << 3) | ((sd.x >> tb) << kMsh);
-        const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
-        const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
+__device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                          const unsigned char *sm, uint32_t off, float2 D) {
+    const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
+    const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
 #pragma unroll
-        for (int m = 0; m < AMPS; ++m) {
-            const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << kMsh)));
-            const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
-            A[m] = __ffma2_rn(neg ? an : ap, p, A[m]);
-            B[m] = __ffma2_rn(neg ? bn : bp, p, B[m]);
-        }
+    for (int m = 0; m < AMPS; ++m) {
+        const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << kMsh)));
+        const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
+        A[m] = __ffma2_rn(neg ? an : ap, p, A[m]);
+        B[m] = __ffma2_rn(neg ? bn : bp, p, B[m]);
     }
 }
 
 template <int AMPS>
-__device__ __forceinline__ void run_c64_dispatch(uint32_t zm, float2 (&A)[AMPS],
-                                                 float2 (&B)[AMPS], const unsigned char *sm,
-                                                 uint32_t soff, uint32_t t, uint32_t tmask,
-                                                 int tb, const ApplyArgs &a, const float2 *tables,
-                                                 const uint8_t *s_tq, uint32_t g0, uint32_t g1,
-                                                 uint32_t threads) {
-#define QR_ZM_CASE(k)                                                                        \
-    case k:                                                                                  \
-        if constexpr (k < AMPS)                                                              \
-            run_c64<AMPS, k>(A, B, sm, soff, t, tmask, tb, a, tables, s_tq, g0, g1, threads); \
+__device__ __forceinline__ void mloop_dispatch(uint32_t zm, float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                               const unsigned char *sm, uint32_t off, float2 D) {
+#define QR_ZM_CASE(k)                                                  \
+    case k:                                                            \
+        if constexpr (k < AMPS) mloop_c64<AMPS, k>(A, B, sm, off, D);  \
         break;
     switch (zm) {
         QR_ZM_CASE(0) QR_ZM_CASE(1) QR_ZM_CASE(2) QR_ZM_CASE(3)
@@ -386,15 +380,48 @@ __device__ __forceinline__ void run_c64_dispatch(uint32_t zm, float2 (&A)[AMPS],
 #undef QR_ZM_CASE
 }
 
+// Rank 3-4 (table) or term-by-term ("fat") sub-group through GroupDesc.
 template <int AMPS>
-__global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a, int stages) {
+__device__ __forceinline__ void big_group_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                           const unsigned char *sm, uint32_t off,
+                                           const GroupDesc &gd, uint64_t r0, int tb,
+                                           const float2 *tables, const uint64_t *fat_z,
+                                           const float2 *fat_c) {
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        const uint64_t r = r0 | ((uint64_t)m << tb);
+        float dr = 0.f, di = 0.f;
+        if (gd.d != kFat) {
+            uint32_t u = 0;
+            for (uint32_t i = 0; i < gd.d; ++i) u |= ((uint32_t)__popcll(r & gd.beta[i]) & 1u) << i;
+            const float2 T = tables[gd.off + u];
+            const bool ng = (__popcll(r & gd.z0) & 1) != 0;
+            dr = ng ? -T.x : T.x;
+            di = ng ? -T.y : T.y;
+        } else {
+            for (uint32_t kk = 0; kk < gd.cnt; ++kk) {
+                const float2 ck = fat_c[gd.off + kk];
+                const bool ng = (__popcll(r & fat_z[gd.off + kk]) & 1) != 0;
+                dr += ng ? -ck.x : ck.x;
+                di += ng ? -ck.y : ck.y;
+            }
+        }
+        const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << kMsh)));
+        A[m] = __ffma2_rn(make_float2(dr, dr), p, A[m]);
+        B[m] = __ffma2_rn(make_float2(di, di), p, B[m]);
+    }
+}
+
+template <int AMPS, bool WIDE>
+__global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t threads = blockDim.x;
+    const uint32_t nwarps = threads >> 5;
     const uint32_t t = threadIdx.x;
-    const uint32_t tile = 1u << a.b;
-    const uint32_t tile_bytes = tile * 8u;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)stages * tile_bytes);
-    uint8_t *s_tq = reinterpret_cast<uint8_t *>(full + kMaxStages);
+    const uint32_t lane = t & 31;
+    const uint32_t tile_bytes = (1u << a.b) * 8u;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)kC64Stages * tile_bytes);
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kC64Stages);
 
     const float2 *psi = static_cast<const float2 *>(a.psi);
     float2 *y = static_cast<float2 *>(a.y);
@@ -410,12 +437,6 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a, 
     const uint64_t total = my_items * nb;
     if (total == 0) return;
 
-    if (t == 0) {
-        for (int s = 0; s < stages; ++s) mbar_init(&full[s], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-
     auto issue = [&](uint64_t L) {
         const uint64_t k = L / nb;
         const uint32_t j = (uint32_t)(L - k * nb);
@@ -423,16 +444,25 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a, 
         const uint64_t st = item / a.ntiles;
         const uint64_t q = item - st * a.ntiles;
         const float2 *src = psi + st * a.N + ((q ^ a.blk_hi[j]) << a.b);
-        const int s = (int)(L % (uint64_t)stages);
+        const int s = (int)(L % (uint64_t)kC64Stages);
         mbar_expect_tx(&full[s], tile_bytes);
         bulk_g2s(smem_raw + (size_t)s * tile_bytes, src, tile_bytes, &full[s]);
     };
     if (t == 0) {
-        const uint64_t pro = total < (uint64_t)stages ? total : (uint64_t)stages;
+        for (int s = 0; s < kC64Stages; ++s) {
+            mbar_init(&full[s], 1);
+            cnt[s] = 0;
+        }
+        mbar_fence_init();
+        const uint64_t pro = total < (uint64_t)kC64Stages ? total : (uint64_t)kC64Stages;
         for (uint64_t L = 0; L < pro; ++L) issue(L);
     }
+    __syncthreads();
 
     float2 A[AMPS], B[AMPS], hi[AMPS], lo[AMPS];
+    const SubDescC64 *subs = a.sub;
+    uint32_t gnext = 0;  // next sub-group in the tile's linear order
+    SubDescC64 pf = subs[0];
 
     for (uint64_t L = 0; L < total; ++L) {
         const uint64_t k = L / nb;
@@ -440,24 +470,17 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a, 
         const uint64_t item = first + k * gridDim.x;
         const uint64_t st = item / a.ntiles;
         const uint64_t q = item - st * a.ntiles;
+        const uint64_t r0 = (q << a.b) | t;
         if (j == 0) {
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) A[m] = B[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
-            // tile parity codes of every sub-group: bit 0 = popc(q & z0 >> b),
-            // bit i+1 = popc(q & beta_i >> b)
-            for (uint32_t g = t; g < a.nsub; g += threads) {
-                const uint64_t *h = a.sub_hi + 5 * (size_t)g;
-                uint32_t c = (uint32_t)__popcll(q & h[0]) & 1u;
-#pragma unroll
-                for (int i = 0; i < kDMax; ++i)
-                    c |= ((uint32_t)__popcll(q & h[1 + i]) & 1u) << (i + 1);
-                s_tq[g] = (uint8_t)c;
-            }
-            __syncthreads();
         }
-        const int s = (int)(L % (uint64_t)stages);
-        const uint32_t par = (uint32_t)((L / (uint64_t)stages) & 1ull);
-        const bool ok = mbar_wait_bounded(&full[s], par, kWaitLimitNs);
+        const int s = (int)(L % (uint64_t)kC64Stages);
+        const uint32_t par = (uint32_t)((L / (uint64_t)kC64Stages) & 1ull);
+        if (!mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
+            if (lane == 0) atomicExch(a.err, kErrMbarTimeout);
+            return;
+        }
         const uint32_t soff = (uint32_t)s * tile_bytes;
 
         if ((int)j == a.diag_block && diag != nullptr) {
@@ -472,36 +495,25 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a, 
             }
         }
 
-        const uint32_t r1 = a.blk_r0[j + 1];
-        for (uint32_t r = a.blk_r0[j]; r < r1; ++r) {
-            const uint32_t zm = a.run_zm[r];
-            const uint32_t g0 = a.run_g0[r], g1 = a.run_g0[r + 1];
-            if (zm != kFat) {
-                run_c64_dispatch<AMPS>(zm, A, B, smem_raw, soff, t, tmask, a.tb, a, tables, s_tq,
-                                       g0, g1, threads);
-            } else {
-                const uint64_t rbase = (q << a.b) | t;
-                for (uint32_t g = g0; g < g1; ++g) {
-                    const uint4 sd = a.sub[g];
-                    const uint32_t off =
-                        soff | ((t ^ (sd.x & tmask)) << 3) | ((sd.x >> a.tb) << kMsh);
-#pragma unroll
-                    for (int m = 0; m < AMPS; ++m) {
-                        const uint64_t rr = rbase | ((uint64_t)m << a.tb);
-                        float dr = 0.f, di = 0.f;
-                        for (uint32_t kk = 0; kk < sd.w; ++kk) {
-                            const uint64_t zk = a.fat_z[sd.y + kk];
-                            const float2 ck = fat_c[sd.y + kk];
-                            const bool ng = (__popcll(rr & zk) & 1) != 0;
-                            dr += ng ? -ck.x : ck.x;
-                            di += ng ? -ck.y : ck.y;
-                        }
-                        const float2 p = *reinterpret_cast<const float2 *>(
-                            smem_raw + (off ^ ((uint32_t)m << kMsh)));
-                        A[m] = __ffma2_rn(make_float2(dr, dr), p, A[m]);
-                        B[m] = __ffma2_rn(make_float2(di, di), p, B[m]);
-                    }
+        const uint32_t g1 = a.blk_g0[j + 1];
+        for (uint32_t g = a.blk_g0[j]; g < g1; ++g) {
+            const SubDescC64 sd = pf;  // == subs[g]
+            gnext = (g + 1 < a.nsub) ? g + 1 : 0;
+            pf = subs[gnext];
+            const uint32_t off = soff | ((t ^ (sd.lo & tmask)) << 3) | ((sd.lo >> a.tb) << kMsh);
+            if ((sd.kind >> 8) == 0) {
+                const uint32_t u = parity<WIDE>(r0, sd.beta0) | (parity<WIDE>(r0, sd.beta1) << 1);
+                float2 D;
+                D.x = (u & 2u) ? ((u & 1u) ? sd.tab[6] : sd.tab[4]) : ((u & 1u) ? sd.tab[2] : sd.tab[0]);
+                D.y = (u & 2u) ? ((u & 1u) ? sd.tab[7] : sd.tab[5]) : ((u & 1u) ? sd.tab[3] : sd.tab[1]);
+                if (parity<WIDE>(r0, sd.z0)) {
+                    D.x = -D.x;
+                    D.y = -D.y;
                 }
+                mloop_dispatch<AMPS>(sd.kind & 15u, A, B, smem_raw, off, D);
+            } else {
+                big_group_c64<AMPS>(A, B, smem_raw, off, a.groups[g], r0, a.tb, tables, a.fat_z,
+                                    fat_c);
             }
         }
 
@@ -524,38 +536,41 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a, 
                     make_float2(__fadd_rn(hi[m].x, lo[m].x), __fadd_rn(hi[m].y, lo[m].y));
         }
 
-        if (__syncthreads_or(ok ? 0 : 1)) {
-            if (t == 0) {
-                atomicExch(a.err, kErrMbarTimeout);
-                for (uint64_t L2 = L; L2 < total && L2 < L + (uint64_t)stages; ++L2) {
-                    const int s2 = (int)(L2 % (uint64_t)stages);
-                    mbar_wait_bounded(&full[s2], (uint32_t)((L2 / stages) & 1ull), kWaitLimitNs);
+        // this warp is done with stage s; the last warp out refills it
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            const uint32_t old = atomicAdd(&cnt[s], 1u);
+            if (old == nwarps - 1) {
+                cnt[s] = 0;
+                if (L + (uint64_t)kC64Stages < total) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue(L + (uint64_t)kC64Stages);
                 }
             }
-            return;
         }
-        if (t == 0 && L + (uint64_t)stages < total) issue(L + (uint64_t)stages);
     }
 }
 
-template <int AMPS>
-static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
+template <int AMPS, bool WIDE>
+static cudaError_t launch_c64c_w(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
     const uint32_t tile_bytes = (1u << a.b) * 8u;
-    int stages = (int)((160u * 1024u) / tile_bytes);
-    if (stages > kMaxStages) stages = kMaxStages;
-    if (stages < 2) stages = 2;
-    const size_t smem = (size_t)stages * tile_bytes + kMaxStages * sizeof(uint64_t) +
-                        (((size_t)a.nsub + 15) & ~(size_t)15);
-    if (smem > 227 * 1024) return cudaErrorInvalidValue;
-    auto kern = apply_c64c<AMPS>;
+    const size_t smem = (size_t)kC64Stages * tile_bytes + kC64Stages * (sizeof(uint64_t) + 4);
+    auto kern = apply_c64c<AMPS, WIDE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     uint64_t grid = a.nitems < (uint64_t)nsm ? a.nitems : (uint64_t)nsm;
     if (grid == 0) return cudaSuccess;
-    kern<<<(unsigned)grid, threads, smem, st>>>(a, stages);
+    kern<<<(unsigned)grid, threads, smem, st>>>(a);
     count_launch();
     return cudaGetLastError();
+}
+
+template <int AMPS>
+static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
+    if (a.n > 32) return launch_c64c_w<AMPS, true>(a, threads, nsm, st);
+    return launch_c64c_w<AMPS, false>(a, threads, nsm, st);
 }
 
 template <typename Real, int AMPS, bool COMP>

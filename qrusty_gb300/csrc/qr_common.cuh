@@ -30,6 +30,17 @@ template <typename Real> struct Cplx;
 template <> struct alignas(8) Cplx<float> { float re, im; };
 template <> struct alignas(16) Cplx<double> { double re, im; };
 
+// Sub-group descriptor of the compensated-c64 kernel (64 bytes).  kind =
+// zm | d << 4 | big << 8: zm is the z pattern on the register bits, d <= 2
+// the rank of the inline table, big marks a sub-group evaluated through the
+// side GroupDesc table instead (rank 3-4, or term by term).
+struct alignas(16) SubDescC64 {
+    uint64_t z0, beta0, beta1;
+    uint32_t lo;
+    uint32_t kind;
+    float tab[8];  // inline table: (re, im) x 4
+};
+
 struct ApplyArgs {
     const void *psi;
     void *y;
@@ -50,15 +61,12 @@ struct ApplyArgs {
     const void *diag;       // Cplx<Real>[N] or null (only read in block hi == 0)
     int diag_block;         // index of the hi == 0 block, or -1
     int *err;               // device error word
-    // compensated-c64 plan (sub-groups in same-sign runs; see qr_apply.cu)
-    const uint4 *sub;       // per sub-group: {lo, table or fat offset, kind, fat count}
-    const uint64_t *sub_hi; // per sub-group: 5 masks >> b (z0, beta[0..3]) for tile parities
-    const uint8_t *codes;   // per sub-group x thread: thread parity code (sign | u << 1)
-    const uint32_t *blk_r0; // runs of block j: [blk_r0[j], blk_r0[j+1])
-    const uint32_t *run_g0; // sub-groups of run r: [run_g0[r], run_g0[r+1])
-    const uint32_t *run_zm; // register-bit z pattern of run r, or kFat
+    // compensated-c64 plan: one SubDescC64 per sub-group (see qr_apply.cu)
+    const SubDescC64 *sub;
     uint32_t nsub;
 };
+
+
 
 // Device error codes written to the error word.
 enum : int { kErrNone = 0, kErrMbarTimeout = 1, kErrCsrPos = 2 };

@@ -95,7 +95,7 @@ struct Plan {
     DevBuf groups, tables, fat_z, fat_c, blk_hi, blk_g0, diag;
     // compensated-c64 kernel tables
     uint32_t nsub = 0;
-    DevBuf sub, sub_hi, codes, blk_r0, run_g0, run_zm;
+    DevBuf sub;
 };
 
 }  // namespace qr
@@ -435,10 +435,7 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
     std::vector<uint64_t> fz;
     uint32_t ntab = 0, nfat_terms = 0;
     std::vector<GroupDesc> descs;           // c128 kernel
-    std::vector<uint4> sd;                  // c64c kernel
-    std::vector<uint64_t> shi;
-    std::vector<uint8_t> codes;
-    std::vector<uint32_t> r0, rg0, rzm;
+    std::vector<SubDescC64> sd;             // c64c kernel
     pl.nfat = 0;
     for (size_t i = 0; i < ord.size(); ++i) {
         const SubGroup &sg = subs[ord[i]];
@@ -448,13 +445,8 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
         d.lo = sg.lo;
         d.d = sg.d;
         for (int q = 0; q < kDMax; ++q) d.beta[q] = sg.beta[q];
-        uint4 u4;
-        u4.x = sg.lo;
-        u4.z = sg.d;
-        u4.w = 0;
         if (sg.d != kFat) {
             d.off = ntab;
-            u4.y = ntab;
             for (const cd &v : sg.table) {
                 if (f32) push_cplx<float>(tab, v);
                 else push_cplx<double>(tab, v);
@@ -463,8 +455,6 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
         } else {
             d.off = nfat_terms;
             d.cnt = (uint32_t)sg.fz.size();
-            u4.y = nfat_terms;
-            u4.w = d.cnt;
             for (size_t k = 0; k < sg.fz.size(); ++k) {
                 fz.push_back(sg.fz[k]);
                 if (f32) push_cplx<float>(fc, sg.fc[k]);
@@ -475,40 +465,33 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
         }
         descs.push_back(d);
         if (f32) {
-            sd.push_back(u4);
-            shi.push_back(sg.z0 >> pl.b);
-            for (int q = 0; q < kDMax; ++q) shi.push_back(sg.beta[q] >> pl.b);
-            for (uint32_t t = 0; t < (uint32_t)pl.threads; ++t) {
-                uint32_t code = (uint32_t)__builtin_popcountll(t & sg.z0) & 1u;
-                if (sg.d != kFat)
-                    for (uint32_t q = 0; q < sg.d; ++q)
-                        code |= ((uint32_t)__builtin_popcountll(t & sg.beta[q]) & 1u) << (q + 1);
-                codes.push_back((uint8_t)code);
+            SubDescC64 c64;
+            memset(&c64, 0, sizeof(c64));
+            c64.z0 = sg.z0;
+            c64.lo = sg.lo;
+            const bool big = (sg.d == kFat) || sg.d > 2;
+            if (!big) {
+                c64.beta0 = sg.d > 0 ? sg.beta[0] : 0;
+                c64.beta1 = sg.d > 1 ? sg.beta[1] : 0;
+                for (size_t u = 0; u < sg.table.size(); ++u) {
+                    c64.tab[2 * u] = (float)sg.table[u].re;
+                    c64.tab[2 * u + 1] = (float)sg.table[u].im;
+                }
+                c64.kind = (sg.zm & 15u) | (sg.d << 4);
+            } else {
+                c64.kind = 1u << 8;
             }
+            sd.push_back(c64);
         }
     }
     if (f32) {
-        // runs of equal zm inside each block
-        for (uint32_t j = 0; j < pl.nblocks; ++j) {
-            r0.push_back((uint32_t)rzm.size());
-            for (uint32_t g = bg0[j]; g < bg0[j + 1]; ++g) {
-                const uint32_t zm = subs[ord[g]].zm;
-                if (g == bg0[j] || zm != rzm.back()) {
-                    rzm.push_back(zm);
-                    rg0.push_back(g);
-                }
-            }
-        }
-        r0.push_back((uint32_t)rzm.size());
-        rg0.push_back((uint32_t)ord.size());
         pl.nsub = (uint32_t)ord.size();
-        if (sd.empty()) sd.push_back(make_uint4(0, 0, 0, 0));
+        if (sd.empty()) {
+            SubDescC64 z;
+            memset(&z, 0, sizeof(z));
+            sd.push_back(z);
+        }
         QR_CUDA(pl.sub.upload(sd), "upload sub-groups");
-        QR_CUDA(pl.sub_hi.upload(shi), "upload sub-group masks");
-        QR_CUDA(pl.codes.upload(codes), "upload thread codes");
-        QR_CUDA(pl.blk_r0.upload(r0), "upload block runs");
-        QR_CUDA(pl.run_g0.upload(rg0), "upload runs");
-        QR_CUDA(pl.run_zm.upload(rzm), "upload run patterns");
     }
     if (descs.empty()) descs.push_back(GroupDesc{});  // keep a valid pointer
     QR_CUDA(pl.groups.upload(descs), "upload groups");
@@ -784,12 +767,7 @@ int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates
     a.diag = pl.has_diag ? pl.diag.p : nullptr;
     a.diag_block = pl.diag_block;
     a.err = op->d_err.as<int>();
-    a.sub = pl.sub.as<uint4>();
-    a.sub_hi = pl.sub_hi.as<uint64_t>();
-    a.codes = pl.codes.as<uint8_t>();
-    a.blk_r0 = pl.blk_r0.as<uint32_t>();
-    a.run_g0 = pl.run_g0.as<uint32_t>();
-    a.run_zm = pl.run_zm.as<uint32_t>();
+    a.sub = pl.sub.as<SubDescC64>();
     a.nsub = pl.nsub;
     if (pl.nblocks == 0) {
         // operator without terms reachable here cannot happen (T >= 1); keep y defined
