@@ -349,9 +349,38 @@ __device__ __forceinline__ uint32_t parity(uint64_t r, uint64_t m) {
     else return (uint32_t)__popc((uint32_t)r & (uint32_t)m) & 1u;
 }
 
-template <int AMPS, int ZM>
+// Thread-dependent state of one sub-group, computed one group ahead.
+struct GroupState {
+    float2 D;       // Dt: table entry with the thread's sign folded in
+    uint32_t off;   // byte offset of the thread's partner for m = 0 (without stage)
+    uint32_t kind;  // descriptor kind (zm | d << 4 | big << 8)
+};
+
+template <bool WIDE>
+__device__ __forceinline__ GroupState group_setup(const SubDescC64 &sd, uint64_t r0, uint32_t t,
+                                                  uint32_t tmask, int tb) {
+    GroupState gs;
+    gs.kind = sd.kind;
+    gs.off = ((t ^ (sd.lo & tmask)) << 3) | ((sd.lo >> tb) << kMsh);
+    const uint32_t u = parity<WIDE>(r0, sd.beta0) | (parity<WIDE>(r0, sd.beta1) << 1);
+    float dx = (u & 2u) ? ((u & 1u) ? sd.tab[6] : sd.tab[4]) : ((u & 1u) ? sd.tab[2] : sd.tab[0]);
+    float dy = (u & 2u) ? ((u & 1u) ? sd.tab[7] : sd.tab[5]) : ((u & 1u) ? sd.tab[3] : sd.tab[1]);
+    if (parity<WIDE>(r0, sd.z0)) {
+        dx = -dx;
+        dy = -dy;
+    }
+    gs.D = make_float2(dx, dy);
+    return gs;
+}
+
+// One sub-group's m-loop (compile-time sign pattern ZM), with the next
+// sub-group's setup in the same basic block so its dependency chain overlaps
+// the 2*AMPS independent FMAs.
+template <int AMPS, int ZM, bool WIDE>
 __device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                          const unsigned char *sm, uint32_t off, float2 D) {
+                                          const unsigned char *sm, uint32_t off, float2 D,
+                                          const SubDescC64 &nd, uint64_t r0n, uint32_t t,
+                                          uint32_t tmask, int tb, GroupState &next) {
     const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
     const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
 #pragma unroll
@@ -361,14 +390,18 @@ __device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
         A[m] = __ffma2_rn(neg ? an : ap, p, A[m]);
         B[m] = __ffma2_rn(neg ? bn : bp, p, B[m]);
     }
+    next = group_setup<WIDE>(nd, r0n, t, tmask, tb);
 }
 
-template <int AMPS>
+template <int AMPS, bool WIDE>
 __device__ __forceinline__ void mloop_dispatch(uint32_t zm, float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                               const unsigned char *sm, uint32_t off, float2 D) {
-#define QR_ZM_CASE(k)                                                  \
-    case k:                                                            \
-        if constexpr (k < AMPS) mloop_c64<AMPS, k>(A, B, sm, off, D);  \
+                                               const unsigned char *sm, uint32_t off, float2 D,
+                                               const SubDescC64 &nd, uint64_t r0n, uint32_t t,
+                                               uint32_t tmask, int tb, GroupState &next) {
+#define QR_ZM_CASE(k)                                                                     \
+    case k:                                                                               \
+        if constexpr (k < AMPS)                                                           \
+            mloop_c64<AMPS, k, WIDE>(A, B, sm, off, D, nd, r0n, t, tmask, tb, next);      \
         break;
     switch (zm) {
         QR_ZM_CASE(0) QR_ZM_CASE(1) QR_ZM_CASE(2) QR_ZM_CASE(3)
@@ -461,8 +494,16 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
 
     float2 A[AMPS], B[AMPS], hi[AMPS], lo[AMPS];
     const SubDescC64 *subs = a.sub;
-    uint32_t gnext = 0;  // next sub-group in the tile's linear order
-    SubDescC64 pf = subs[0];
+    const uint32_t nsub = a.nsub;
+    // current sub-group's state (computed one group ahead) and the prefetched
+    // descriptor of the sub-group after it, in the tile-by-tile linear order
+    GroupState cur;
+    SubDescC64 pf;
+    if (nsub > 0) {
+        const uint64_t q0 = first % a.ntiles;
+        cur = group_setup<WIDE>(subs[0], (q0 << a.b) | t, t, tmask, a.tb);
+        pf = subs[nsub > 1 ? 1 : 0];
+    }
 
     for (uint64_t L = 0; L < total; ++L) {
         const uint64_t k = L / nb;
@@ -497,24 +538,27 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
 
         const uint32_t g1 = a.blk_g0[j + 1];
         for (uint32_t g = a.blk_g0[j]; g < g1; ++g) {
-            const SubDescC64 sd = pf;  // == subs[g]
-            gnext = (g + 1 < a.nsub) ? g + 1 : 0;
-            pf = subs[gnext];
-            const uint32_t off = soff | ((t ^ (sd.lo & tmask)) << 3) | ((sd.lo >> a.tb) << kMsh);
-            if ((sd.kind >> 8) == 0) {
-                const uint32_t u = parity<WIDE>(r0, sd.beta0) | (parity<WIDE>(r0, sd.beta1) << 1);
-                float2 D;
-                D.x = (u & 2u) ? ((u & 1u) ? sd.tab[6] : sd.tab[4]) : ((u & 1u) ? sd.tab[2] : sd.tab[0]);
-                D.y = (u & 2u) ? ((u & 1u) ? sd.tab[7] : sd.tab[5]) : ((u & 1u) ? sd.tab[3] : sd.tab[1]);
-                if (parity<WIDE>(r0, sd.z0)) {
-                    D.x = -D.x;
-                    D.y = -D.y;
-                }
-                mloop_dispatch<AMPS>(sd.kind & 15u, A, B, smem_raw, off, D);
+            // next sub-group in linear order: g + 1 of this tile, or 0 of the next
+            uint64_t r0n = r0;
+            uint32_t gn = g + 1;
+            if (gn == nsub) {
+                gn = 0;
+                const uint64_t itn = item + gridDim.x;
+                r0n = ((itn % a.ntiles) << a.b) | t;
+            }
+            const SubDescC64 nd = pf;  // == subs[gn]
+            pf = subs[gn + 1 < nsub ? gn + 1 : 0];
+            const uint32_t off = soff | cur.off;
+            GroupState nxt;
+            if ((cur.kind >> 8) == 0) {
+                mloop_dispatch<AMPS, WIDE>(cur.kind & 15u, A, B, smem_raw, off, cur.D, nd, r0n, t,
+                                           tmask, a.tb, nxt);
             } else {
                 big_group_c64<AMPS>(A, B, smem_raw, off, a.groups[g], r0, a.tb, tables, a.fat_z,
                                     fat_c);
+                nxt = group_setup<WIDE>(nd, r0n, t, tmask, a.tb);
             }
+            cur = nxt;
         }
 
         const bool last = (j == nb - 1);
