@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 // barrier sits on the steady-state path.
 constexpr int kTb = 8;          // log2(threads) whenever AMPS >= 2
 constexpr int kMsh = kTb + 3;   // byte shift of the register index m
-constexpr int kFlush = 4;       // partner tiles per compensated fold
+constexpr int kFlush = 8;       // partner tiles per compensated fold
 constexpr int kC64Threads = 256;
 constexpr int kC64Stages = 6;
 
@@ -379,8 +379,9 @@ __device__ __forceinline__ GroupState group_setup(const SubDescC64 &sd, uint64_t
 template <int AMPS, int ZM, bool WIDE>
 __device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                           const unsigned char *sm, uint32_t off, float2 D,
-                                          const SubDescC64 &nd, uint64_t r0n, uint32_t t,
+                                          const SubDescC64 *ndp, uint64_t r0n, uint32_t t,
                                           uint32_t tmask, int tb, GroupState &next) {
+    const SubDescC64 nd = *ndp;
     const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
     const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
 #pragma unroll
@@ -396,7 +397,7 @@ __device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
 template <int AMPS, bool WIDE>
 __device__ __forceinline__ void mloop_dispatch(uint32_t zm, float2 (&A)[AMPS], float2 (&B)[AMPS],
                                                const unsigned char *sm, uint32_t off, float2 D,
-                                               const SubDescC64 &nd, uint64_t r0n, uint32_t t,
+                                               const SubDescC64 *nd, uint64_t r0n, uint32_t t,
                                                uint32_t tmask, int tb, GroupState &next) {
 #define QR_ZM_CASE(k)                                                                     \
     case k:                                                                               \
@@ -495,34 +496,27 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
     float2 A[AMPS], B[AMPS], hi[AMPS], lo[AMPS];
     const SubDescC64 *subs = a.sub;
     const uint32_t nsub = a.nsub;
-    // current sub-group's state (computed one group ahead) and the prefetched
-    // descriptor of the sub-group after it, in the tile-by-tile linear order
+    // loop state advanced incrementally (no division on the steady path)
+    uint32_t j = 0, s = 0, par = 0;
+    uint64_t item = first;
+    uint64_t st = item / a.ntiles;
+    uint64_t q = item - st * a.ntiles;
+    // current sub-group's thread state, computed one group ahead in the
+    // tile-by-tile linear order of sub-groups
     GroupState cur;
-    SubDescC64 pf;
-    if (nsub > 0) {
-        const uint64_t q0 = first % a.ntiles;
-        cur = group_setup<WIDE>(subs[0], (q0 << a.b) | t, t, tmask, a.tb);
-        pf = subs[nsub > 1 ? 1 : 0];
-    }
+    if (nsub > 0) cur = group_setup<WIDE>(subs[0], (q << a.b) | t, t, tmask, a.tb);
 
     for (uint64_t L = 0; L < total; ++L) {
-        const uint64_t k = L / nb;
-        const uint32_t j = (uint32_t)(L - k * nb);
-        const uint64_t item = first + k * gridDim.x;
-        const uint64_t st = item / a.ntiles;
-        const uint64_t q = item - st * a.ntiles;
         const uint64_t r0 = (q << a.b) | t;
         if (j == 0) {
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) A[m] = B[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
         }
-        const int s = (int)(L % (uint64_t)kC64Stages);
-        const uint32_t par = (uint32_t)((L / (uint64_t)kC64Stages) & 1ull);
         if (!mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
             if (lane == 0) atomicExch(a.err, kErrMbarTimeout);
             return;
         }
-        const uint32_t soff = (uint32_t)s * tile_bytes;
+        const uint32_t soff = s * tile_bytes;
 
         if ((int)j == a.diag_block && diag != nullptr) {
             const float2 *dg = diag + (q << a.b);
@@ -543,20 +537,19 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
             uint32_t gn = g + 1;
             if (gn == nsub) {
                 gn = 0;
-                const uint64_t itn = item + gridDim.x;
-                r0n = ((itn % a.ntiles) << a.b) | t;
+                uint64_t qn = q + gridDim.x;
+                while (qn >= a.ntiles) qn -= a.ntiles;
+                r0n = (qn << a.b) | t;
             }
-            const SubDescC64 nd = pf;  // == subs[gn]
-            pf = subs[gn + 1 < nsub ? gn + 1 : 0];
             const uint32_t off = soff | cur.off;
             GroupState nxt;
             if ((cur.kind >> 8) == 0) {
-                mloop_dispatch<AMPS, WIDE>(cur.kind & 15u, A, B, smem_raw, off, cur.D, nd, r0n, t,
-                                           tmask, a.tb, nxt);
+                mloop_dispatch<AMPS, WIDE>(cur.kind & 15u, A, B, smem_raw, off, cur.D, subs + gn,
+                                           r0n, t, tmask, a.tb, nxt);
             } else {
                 big_group_c64<AMPS>(A, B, smem_raw, off, a.groups[g], r0, a.tb, tables, a.fat_z,
                                     fat_c);
-                nxt = group_setup<WIDE>(nd, r0n, t, tmask, a.tb);
+                nxt = group_setup<WIDE>(subs[gn], r0n, t, tmask, a.tb);
             }
             cur = nxt;
         }
@@ -591,6 +584,20 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     issue(L + (uint64_t)kC64Stages);
                 }
+            }
+        }
+        // advance (stage ring, partner tile, item)
+        if (++s == kC64Stages) {
+            s = 0;
+            par ^= 1u;
+        }
+        if (++j == nb) {
+            j = 0;
+            item += gridDim.x;
+            q += gridDim.x;
+            while (q >= a.ntiles) {
+                q -= a.ntiles;
+                ++st;
             }
         }
     }
