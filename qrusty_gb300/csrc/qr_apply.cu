@@ -376,7 +376,7 @@ __device__ __forceinline__ GroupState group_setup(const SubDescC64 &sd, uint64_t
 // One sub-group's m-loop (compile-time sign pattern ZM), with the next
 // sub-group's setup in the same basic block so its dependency chain overlaps
 // the 2*AMPS independent FMAs.
-template <int AMPS, int ZM, bool WIDE>
+template <int AMPS, int ZM, bool XM, bool WIDE>
 __device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                           const unsigned char *sm, uint32_t off, float2 D,
                                           const SubDescC64 *ndp, uint64_t r0n, uint32_t t,
@@ -386,7 +386,10 @@ __device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
     const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
 #pragma unroll
     for (int m = 0; m < AMPS; ++m) {
-        const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << kMsh)));
+        // XM: the sub-group's x has register bits, so partners are permuted by
+        // XOR; otherwise the offsets are compile-time immediates.
+        const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
+        const float2 p = *reinterpret_cast<const float2 *>(sm + o);
         const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
         A[m] = __ffma2_rn(neg ? an : ap, p, A[m]);
         B[m] = __ffma2_rn(neg ? bn : bp, p, B[m]);
@@ -399,16 +402,21 @@ __device__ __forceinline__ void mloop_dispatch(uint32_t zm, float2 (&A)[AMPS], f
                                                const unsigned char *sm, uint32_t off, float2 D,
                                                const SubDescC64 *nd, uint64_t r0n, uint32_t t,
                                                uint32_t tmask, int tb, GroupState &next) {
-#define QR_ZM_CASE(k)                                                                     \
-    case k:                                                                               \
-        if constexpr (k < AMPS)                                                           \
-            mloop_c64<AMPS, k, WIDE>(A, B, sm, off, D, nd, r0n, t, tmask, tb, next);      \
+#define QR_ZM_CASE(k)                                                                        \
+    case k:                                                                                  \
+        if constexpr ((k & 15) < AMPS)                                                       \
+            mloop_c64<AMPS, (k & 15), (k >> 4) != 0, WIDE>(A, B, sm, off, D, nd, r0n, t, tmask, \
+                                                           tb, next);                        \
         break;
     switch (zm) {
         QR_ZM_CASE(0) QR_ZM_CASE(1) QR_ZM_CASE(2) QR_ZM_CASE(3)
         QR_ZM_CASE(4) QR_ZM_CASE(5) QR_ZM_CASE(6) QR_ZM_CASE(7)
         QR_ZM_CASE(8) QR_ZM_CASE(9) QR_ZM_CASE(10) QR_ZM_CASE(11)
         QR_ZM_CASE(12) QR_ZM_CASE(13) QR_ZM_CASE(14) QR_ZM_CASE(15)
+        QR_ZM_CASE(16) QR_ZM_CASE(17) QR_ZM_CASE(18) QR_ZM_CASE(19)
+        QR_ZM_CASE(20) QR_ZM_CASE(21) QR_ZM_CASE(22) QR_ZM_CASE(23)
+        QR_ZM_CASE(24) QR_ZM_CASE(25) QR_ZM_CASE(26) QR_ZM_CASE(27)
+        QR_ZM_CASE(28) QR_ZM_CASE(29) QR_ZM_CASE(30) QR_ZM_CASE(31)
         default: break;
     }
 #undef QR_ZM_CASE
@@ -544,7 +552,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
             const uint32_t off = soff | cur.off;
             GroupState nxt;
             if ((cur.kind >> 8) == 0) {
-                mloop_dispatch<AMPS, WIDE>(cur.kind & 15u, A, B, smem_raw, off, cur.D, subs + gn,
+                mloop_dispatch<AMPS, WIDE>(cur.kind & 31u, A, B, smem_raw, off, cur.D, subs + gn,
                                            r0n, t, tmask, a.tb, nxt);
             } else {
                 big_group_c64<AMPS>(A, B, smem_raw, off, a.groups[g], r0, a.tb, tables, a.fat_z,

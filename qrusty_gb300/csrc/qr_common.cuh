@@ -31,9 +31,10 @@ template <> struct alignas(8) Cplx<float> { float re, im; };
 template <> struct alignas(16) Cplx<double> { double re, im; };
 
 // Sub-group descriptor of the compensated-c64 kernel (64 bytes).  kind =
-// zm | d << 4 | big << 8: zm is the z pattern on the register bits, d <= 2
-// the rank of the inline table, big marks a sub-group evaluated through the
-// side GroupDesc table instead (rank 3-4, or term by term).
+// zm | xm << 4 | d << 5 | big << 8: zm is the z pattern on the register
+// bits, xm = 1 when x has register bits (partners permuted by XOR there),
+// d <= 2 the rank of the inline table, big marks a sub-group evaluated
+// through the side GroupDesc table instead (rank 3-4, or term by term).
 struct alignas(16) SubDescC64 {
     uint64_t z0, beta0, beta1;
     uint32_t lo;

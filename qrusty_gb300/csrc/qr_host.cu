@@ -477,7 +477,8 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
                     c64.tab[2 * u] = (float)sg.table[u].re;
                     c64.tab[2 * u + 1] = (float)sg.table[u].im;
                 }
-                c64.kind = (sg.zm & 15u) | (sg.d << 4);
+                const uint32_t xm = ((sg.lo >> pl.tb) != 0) ? 1u : 0u;
+                c64.kind = (sg.zm & 15u) | (xm << 4) | (sg.d << 5);
             } else {
                 c64.kind = 1u << 8;
             }
