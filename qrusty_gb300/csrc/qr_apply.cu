@@ -319,8 +319,8 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 }
 
 // ---------------------------------------------------------------- c64c kernel
-// Compensated complex64 path.  256 threads x AMPS = 16 amplitudes per 4096-
-// amplitude tile; thread t owns r_lo = t + 256 m.  The host splits every
+// Compensated complex64 path.  512 threads x AMPS = 8 amplitudes per 4096-
+// amplitude tile; thread t owns r_lo = t + 512 m.  The host splits every
 // x-group into sub-groups whose z masks agree on the register bits
 // [kTb, kTb + log2 AMPS), so for a thread the sub-group's factor is
 //     D_m = (-1)^popc(m & zm) * Dt,   Dt = (-1)^popc(r0 & z0) * tab[u],
@@ -337,10 +337,10 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 // consumes it, and counts itself out on a shared counter; the last warp out
 // refills the stage with the tile kC64Stages steps ahead.  No CTA-wide
 // barrier sits on the steady-state path.
-constexpr int kTb = 8;          // log2(threads) whenever AMPS >= 2
+constexpr int kTb = 9;          // log2(threads) whenever AMPS >= 2
 constexpr int kMsh = kTb + 3;   // byte shift of the register index m
 constexpr int kFlush = 8;       // partner tiles per compensated fold
-constexpr int kC64Threads = 256;
+constexpr int kC64Threads = 512;
 constexpr int kC64Stages = 6;
 
 template <bool WIDE>
