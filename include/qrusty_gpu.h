@@ -58,7 +58,8 @@ typedef struct {
     uint64_t ngroups;     /* distinct x masks (= nnz per CSR row)          */
     uint64_t nmerged;     /* distinct (x, z) strings after FP64 merging    */
     uint64_t nblocks;     /* distinct partner tiles x >> tile_bits         */
-    uint64_t nfat;        /* groups evaluated term by term in qr_apply     */
+    uint64_t nfat;        /* complex128 plan: groups evaluated term by term */
+    uint64_t nsub;        /* complex64 plan: rank <= 2 sub-groups          */
     int32_t has_diag;     /* x = 0 group held as a precomputed diagonal    */
     int32_t device;       /* CUDA device the operator lives on             */
 } qr_op_info;

@@ -42,7 +42,8 @@ class QrError(RuntimeError):
 class OpInfo(C.Structure):
     _fields_ = [("n", C.c_int32), ("tile_bits", C.c_int32), ("nterms", C.c_uint64),
                 ("ngroups", C.c_uint64), ("nmerged", C.c_uint64), ("nblocks", C.c_uint64),
-                ("nfat", C.c_uint64), ("has_diag", C.c_int32), ("device", C.c_int32)]
+                ("nfat", C.c_uint64), ("nsub", C.c_uint64), ("has_diag", C.c_int32),
+                ("device", C.c_int32)]
 
 
 _lib = None

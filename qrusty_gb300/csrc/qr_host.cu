@@ -670,6 +670,8 @@ int qr_op_get_info(const qr_op *op_c, qr_op_info *info) {
     if (rc) return rc;
     rc = build_plan(op, QR_C64C, 0);
     if (rc) return rc;
+    rc = build_plan(op, QR_C128, 0);
+    if (rc) return rc;
     const Plan &pl = op->plans[QR_C64C][0];
     info->n = op->n;
     info->tile_bits = pl.b;
@@ -677,7 +679,8 @@ int qr_op_get_info(const qr_op *op_c, qr_op_info *info) {
     info->ngroups = op->G;
     info->nmerged = op->mx.size();
     info->nblocks = pl.nblocks;
-    info->nfat = pl.nfat;
+    info->nfat = op->plans[QR_C128][0].nfat;
+    info->nsub = pl.nsub;
     info->has_diag = pl.has_diag ? 1 : 0;
     info->device = op->device;
     return QR_OK;
