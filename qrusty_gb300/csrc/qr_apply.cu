@@ -321,16 +321,16 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 // ---------------------------------------------------------------- c64c kernel
 // Compensated complex64 path.  512 threads x AMPS = 8 amplitudes per 4096-
 // amplitude tile; thread t owns r_lo = t + 512 m.  The host splits every
-// x-group into sub-groups of rank <= 2 whose z masks agree on the register
-// bits [kTb, kTb + log2 AMPS), so for a thread the sub-group's factor is
-//     D_m = (-1)^(popc(m & zm) + s) * T[u],
-// with (s, u) the parities of r0 = (tile << b) | t against z0 / beta0,1.
-// (zm, s) selects a compile-time sign pattern, so the inner step per
+// x-group into sub-groups whose z masks agree on the register bits
+// [kTb, kTb + log2 AMPS), so for a thread the sub-group's factor is
+//     D_m = (-1)^popc(m & zm) * Dt,   Dt = (-1)^popc(r0 & z0) * tab[u],
+// r0 = (tile << b) | t, u_i = popc(r0 & beta_i) & 1 (rank <= 2, table
+// inline in the 64-byte descriptor, read one sub-group ahead).  The sign
+// pattern over m selects a compile-time instantiation, so the inner step per
 // amplitude is one shared-memory load and two packed FMAs:
-//     A_m += (+-T.re) * p,  B_m += (+-T.im) * p      (fma.rn.f32x2)
+//     A_m += (+-Dt.re) * p,  B_m += (+-Dt.im) * p      (fma.rn.f32x2)
 // and y = A + iB is folded into the running (hi, lo) two-sum pair every
-// kFlush partner tiles.  The next sub-group's (s, u, T[u]) is computed inside
-// the current case, so its loads and parities overlap the current FMAs.
+// kFlush partner tiles.
 //
 // Pipeline: a kC64Stages-deep ring of partner tiles filled by 1-D TMA bulk
 // copies.  Warps run decoupled: each waits on the stage's full mbarrier,
@@ -351,37 +351,46 @@ __device__ __forceinline__ uint32_t parity(uint64_t r, uint64_t m) {
 
 // Thread-dependent state of one sub-group, computed one group ahead.
 struct GroupState {
-    float4 T;       // (re, re, im, im) of the thread's table entry
+    float2 D;       // Dt: table entry with the thread's sign folded in
     uint32_t off;   // byte offset of the thread's partner for m = 0 (without stage)
-    uint32_t key;   // zm | s << 4
+    uint32_t kind;  // descriptor kind (zm | d << 4 | big << 8)
 };
 
 template <bool WIDE>
-__device__ __forceinline__ GroupState group_setup(const SubDescC64 *sd, uint64_t r0, uint32_t t,
+__device__ __forceinline__ GroupState group_setup(const SubDescC64 &sd, uint64_t r0, uint32_t t,
                                                   uint32_t tmask, int tb) {
     GroupState gs;
-    const uint64_t z0 = sd->z0, b0 = sd->beta0, b1 = sd->beta1;
-    const uint32_t lo = sd->lo, zm = sd->zm;
-    const uint32_t u = parity<WIDE>(r0, b0) | (parity<WIDE>(r0, b1) << 1);
-    gs.T = sd->tab[u];
-    gs.key = zm | (parity<WIDE>(r0, z0) << 4);
-    gs.off = ((t ^ (lo & tmask)) << 3) | ((lo >> tb) << kMsh);
+    gs.kind = sd.kind;
+    gs.off = ((t ^ (sd.lo & tmask)) << 3) | ((sd.lo >> tb) << kMsh);
+    const uint32_t u = parity<WIDE>(r0, sd.beta0) | (parity<WIDE>(r0, sd.beta1) << 1);
+    float dx = (u & 2u) ? ((u & 1u) ? sd.tab[6] : sd.tab[4]) : ((u & 1u) ? sd.tab[2] : sd.tab[0]);
+    float dy = (u & 2u) ? ((u & 1u) ? sd.tab[7] : sd.tab[5]) : ((u & 1u) ? sd.tab[3] : sd.tab[1]);
+    if (parity<WIDE>(r0, sd.z0)) {
+        dx = -dx;
+        dy = -dy;
+    }
+    gs.D = make_float2(dx, dy);
     return gs;
 }
 
-// One sub-group's m-loop with compile-time sign pattern (ZM, S), plus the
-// next sub-group's setup in the same basic block.
-template <int AMPS, int ZM, int S, bool WIDE>
+// One sub-group's m-loop (compile-time sign pattern ZM), with the next
+// sub-group's setup in the same basic block so its dependency chain overlaps
+// the 2*AMPS independent FMAs.
+template <int AMPS, int ZM, bool XM, bool WIDE>
 __device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                          const unsigned char *sm, uint32_t off, float4 T,
-                                          const SubDescC64 *nd, uint64_t r0n, uint32_t t,
+                                          const unsigned char *sm, uint32_t off, float2 D,
+                                          const SubDescC64 *ndp, uint64_t r0n, uint32_t t,
                                           uint32_t tmask, int tb, GroupState &next) {
-    const float2 ap = make_float2(T.x, T.y), bp = make_float2(T.z, T.w);
-    const float2 an = make_float2(-T.x, -T.y), bn = make_float2(-T.z, -T.w);
+    const SubDescC64 nd = *ndp;
+    const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
+    const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
 #pragma unroll
     for (int m = 0; m < AMPS; ++m) {
-        const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << kMsh)));
-        const bool neg = ((__builtin_popcount((unsigned)(m & ZM)) + S) & 1) != 0;
+        // XM: the sub-group's x has register bits, so partners are permuted by
+        // XOR; otherwise the offsets are compile-time immediates.
+        const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
+        const float2 p = *reinterpret_cast<const float2 *>(sm + o);
+        const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
         A[m] = __ffma2_rn(neg ? an : ap, p, A[m]);
         B[m] = __ffma2_rn(neg ? bn : bp, p, B[m]);
     }
@@ -389,28 +398,60 @@ __device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
 }
 
 template <int AMPS, bool WIDE>
-__device__ __forceinline__ void mloop_dispatch(uint32_t key, float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                               const unsigned char *sm, uint32_t off, float4 T,
+__device__ __forceinline__ void mloop_dispatch(uint32_t zm, float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                               const unsigned char *sm, uint32_t off, float2 D,
                                                const SubDescC64 *nd, uint64_t r0n, uint32_t t,
                                                uint32_t tmask, int tb, GroupState &next) {
-#define QR_KEY_CASE(k)                                                                      \
-    case k:                                                                                 \
-        if constexpr ((k & 15) < AMPS)                                                      \
-            mloop_c64<AMPS, (k & 15), (k >> 4), WIDE>(A, B, sm, off, T, nd, r0n, t, tmask,  \
-                                                      tb, next);                            \
+#define QR_ZM_CASE(k)                                                                        \
+    case k:                                                                                  \
+        if constexpr ((k & 15) < AMPS)                                                       \
+            mloop_c64<AMPS, (k & 15), (k >> 4) != 0, WIDE>(A, B, sm, off, D, nd, r0n, t, tmask, \
+                                                           tb, next);                        \
         break;
-    switch (key) {
-        QR_KEY_CASE(0) QR_KEY_CASE(1) QR_KEY_CASE(2) QR_KEY_CASE(3)
-        QR_KEY_CASE(4) QR_KEY_CASE(5) QR_KEY_CASE(6) QR_KEY_CASE(7)
-        QR_KEY_CASE(8) QR_KEY_CASE(9) QR_KEY_CASE(10) QR_KEY_CASE(11)
-        QR_KEY_CASE(12) QR_KEY_CASE(13) QR_KEY_CASE(14) QR_KEY_CASE(15)
-        QR_KEY_CASE(16) QR_KEY_CASE(17) QR_KEY_CASE(18) QR_KEY_CASE(19)
-        QR_KEY_CASE(20) QR_KEY_CASE(21) QR_KEY_CASE(22) QR_KEY_CASE(23)
-        QR_KEY_CASE(24) QR_KEY_CASE(25) QR_KEY_CASE(26) QR_KEY_CASE(27)
-        QR_KEY_CASE(28) QR_KEY_CASE(29) QR_KEY_CASE(30) QR_KEY_CASE(31)
+    switch (zm) {
+        QR_ZM_CASE(0) QR_ZM_CASE(1) QR_ZM_CASE(2) QR_ZM_CASE(3)
+        QR_ZM_CASE(4) QR_ZM_CASE(5) QR_ZM_CASE(6) QR_ZM_CASE(7)
+        QR_ZM_CASE(8) QR_ZM_CASE(9) QR_ZM_CASE(10) QR_ZM_CASE(11)
+        QR_ZM_CASE(12) QR_ZM_CASE(13) QR_ZM_CASE(14) QR_ZM_CASE(15)
+        QR_ZM_CASE(16) QR_ZM_CASE(17) QR_ZM_CASE(18) QR_ZM_CASE(19)
+        QR_ZM_CASE(20) QR_ZM_CASE(21) QR_ZM_CASE(22) QR_ZM_CASE(23)
+        QR_ZM_CASE(24) QR_ZM_CASE(25) QR_ZM_CASE(26) QR_ZM_CASE(27)
+        QR_ZM_CASE(28) QR_ZM_CASE(29) QR_ZM_CASE(30) QR_ZM_CASE(31)
         default: break;
     }
-#undef QR_KEY_CASE
+#undef QR_ZM_CASE
+}
+
+// Rank 3-4 (table) or term-by-term ("fat") sub-group through GroupDesc.
+template <int AMPS>
+__device__ __forceinline__ void big_group_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                           const unsigned char *sm, uint32_t off,
+                                           const GroupDesc &gd, uint64_t r0, int tb,
+                                           const float2 *tables, const uint64_t *fat_z,
+                                           const float2 *fat_c) {
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        const uint64_t r = r0 | ((uint64_t)m << tb);
+        float dr = 0.f, di = 0.f;
+        if (gd.d != kFat) {
+            uint32_t u = 0;
+            for (uint32_t i = 0; i < gd.d; ++i) u |= ((uint32_t)__popcll(r & gd.beta[i]) & 1u) << i;
+            const float2 T = tables[gd.off + u];
+            const bool ng = (__popcll(r & gd.z0) & 1) != 0;
+            dr = ng ? -T.x : T.x;
+            di = ng ? -T.y : T.y;
+        } else {
+            for (uint32_t kk = 0; kk < gd.cnt; ++kk) {
+                const float2 ck = fat_c[gd.off + kk];
+                const bool ng = (__popcll(r & fat_z[gd.off + kk]) & 1) != 0;
+                dr += ng ? -ck.x : ck.x;
+                di += ng ? -ck.y : ck.y;
+            }
+        }
+        const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << kMsh)));
+        A[m] = __ffma2_rn(make_float2(dr, dr), p, A[m]);
+        B[m] = __ffma2_rn(make_float2(di, di), p, B[m]);
+    }
 }
 
 template <int AMPS, bool WIDE>
@@ -426,10 +467,11 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
 
     const float2 *psi = static_cast<const float2 *>(a.psi);
     float2 *y = static_cast<float2 *>(a.y);
+    const float2 *tables = static_cast<const float2 *>(a.tables);
+    const float2 *fat_c = static_cast<const float2 *>(a.fat_c);
     const float2 *diag = static_cast<const float2 *>(a.diag);
     const uint32_t nb = a.nblocks;
     const uint32_t tmask = threads - 1;
-    const int tb = a.tb;
 
     const uint64_t first = blockIdx.x;
     const uint64_t my_items =
@@ -464,12 +506,13 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
     const uint32_t nsub = a.nsub;
     // loop state advanced incrementally (no division on the steady path)
     uint32_t j = 0, s = 0, par = 0;
-    uint64_t st = first / a.ntiles;
-    uint64_t q = first - st * a.ntiles;
+    uint64_t item = first;
+    uint64_t st = item / a.ntiles;
+    uint64_t q = item - st * a.ntiles;
     // current sub-group's thread state, computed one group ahead in the
     // tile-by-tile linear order of sub-groups
     GroupState cur;
-    if (nsub > 0) cur = group_setup<WIDE>(subs, (q << a.b) | t, t, tmask, tb);
+    if (nsub > 0) cur = group_setup<WIDE>(subs[0], (q << a.b) | t, t, tmask, a.tb);
 
     for (uint64_t L = 0; L < total; ++L) {
         const uint64_t r0 = (q << a.b) | t;
@@ -506,9 +549,16 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
                 while (qn >= a.ntiles) qn -= a.ntiles;
                 r0n = (qn << a.b) | t;
             }
+            const uint32_t off = soff | cur.off;
             GroupState nxt;
-            mloop_dispatch<AMPS, WIDE>(cur.key, A, B, smem_raw, soff | cur.off, cur.T, subs + gn,
-                                       r0n, t, tmask, tb, nxt);
+            if ((cur.kind >> 8) == 0) {
+                mloop_dispatch<AMPS, WIDE>(cur.kind & 31u, A, B, smem_raw, off, cur.D, subs + gn,
+                                           r0n, t, tmask, a.tb, nxt);
+            } else {
+                big_group_c64<AMPS>(A, B, smem_raw, off, a.groups[g], r0, a.tb, tables, a.fat_z,
+                                    fat_c);
+                nxt = group_setup<WIDE>(subs[gn], r0n, t, tmask, a.tb);
+            }
             cur = nxt;
         }
 
@@ -551,6 +601,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
         }
         if (++j == nb) {
             j = 0;
+            item += gridDim.x;
             q += gridDim.x;
             while (q >= a.ntiles) {
                 q -= a.ntiles;

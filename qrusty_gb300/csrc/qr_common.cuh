@@ -30,16 +30,16 @@ template <typename Real> struct Cplx;
 template <> struct alignas(8) Cplx<float> { float re, im; };
 template <> struct alignas(16) Cplx<double> { double re, im; };
 
-// Sub-group descriptor of the compensated-c64 kernel (96 bytes).  Every
-// sub-group has rank <= 2: its factor at row r is
-//     (-1)^popc(r & z0) * T[u],  u = popc(r & beta0) & 1 | (popc(r & beta1) & 1) << 1,
-// with T[u] stored pre-duplicated as (re, re, im, im) for the packed FMAs.
-// zm = z0's bits on the register bits selects the Walsh sign pattern.
+// Sub-group descriptor of the compensated-c64 kernel (64 bytes).  kind =
+// zm | xm << 4 | d << 5 | big << 8: zm is the z pattern on the register
+// bits, xm = 1 when x has register bits (partners permuted by XOR there),
+// d <= 2 the rank of the inline table, big marks a sub-group evaluated
+// through the side GroupDesc table instead (rank 3-4, or term by term).
 struct alignas(16) SubDescC64 {
     uint64_t z0, beta0, beta1;
-    uint32_t lo;   // x & (tile - 1)
-    uint32_t zm;   // (z0 >> tb) & (amps - 1)
-    float4 tab[4];
+    uint32_t lo;
+    uint32_t kind;
+    float tab[8];  // inline table: (re, im) x 4
 };
 
 struct ApplyArgs {

@@ -235,7 +235,7 @@ void merge_terms(qr_op *op) {
 // and the coordinates of every term's difference in that basis.
 struct Span {
     std::vector<uint64_t> basis;
-    std::vector<uint64_t> coord;  // per term
+    std::vector<uint32_t> coord;  // per term
     bool overflow = false;
 };
 Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
@@ -244,7 +244,7 @@ Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
     sp.coord.resize(zs.size());
     for (size_t k = 0; k < zs.size(); ++k) {
         uint64_t v = zs[k] ^ z0;
-        uint64_t c = 0;
+        uint32_t c = 0;
         // basis kept in order of insertion; reduce by descending pivot
         std::vector<size_t> ord(sp.basis.size());
         for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
@@ -255,7 +255,7 @@ Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
             const int piv = 63 - __builtin_clzll(bv);
             if ((v >> piv) & 1ull) {
                 v ^= bv;
-                c |= 1ull << i;
+                c |= 1u << i;
             }
         }
         if (v != 0) {
@@ -263,7 +263,7 @@ Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
                 sp.overflow = true;
                 return sp;
             }
-            c |= 1ull << sp.basis.size();
+            c |= 1u << sp.basis.size();
             sp.basis.push_back(v);
         }
         sp.coord[k] = c;
@@ -365,36 +365,7 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
             }
             parts[pi].push_back(k);
         }
-        // c64c: split further until every sub-group has rank <= 2 (terms whose
-        // z differences agree beyond the first two basis vectors)
-        std::vector<std::vector<size_t>> pieces;
         for (const auto &part : parts) {
-            if (!f32) {
-                pieces.push_back(part);
-                continue;
-            }
-            std::vector<uint64_t> zs;
-            for (size_t k : part) zs.push_back(op->mz[k]);
-            Span full = gf2_span(zs, 64);
-            if (full.basis.size() <= 2) {
-                pieces.push_back(part);
-                continue;
-            }
-            std::vector<uint64_t> hk;
-            std::vector<std::vector<size_t>> hp;
-            for (size_t kk = 0; kk < part.size(); ++kk) {
-                const uint64_t key = full.coord[kk] >> 2;
-                size_t pi = 0;
-                while (pi < hk.size() && hk[pi] != key) ++pi;
-                if (pi == hk.size()) {
-                    hk.push_back(key);
-                    hp.emplace_back();
-                }
-                hp[pi].push_back(part[kk]);
-            }
-            for (auto &h : hp) pieces.push_back(std::move(h));
-        }
-        for (const auto &part : pieces) {
             std::vector<uint64_t> zs;
             for (size_t k : part) zs.push_back(op->mz[k]);
             Span sp = gf2_span(zs, kDMax);
@@ -411,7 +382,7 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
                     cd acc{0.0, 0.0};
                     for (size_t kk = 0; kk < part.size(); ++kk) {
                         const cd v = c[part[kk]];
-                        if (__builtin_popcountll(u & sp.coord[kk]) & 1) {
+                        if (__builtin_popcount(u & sp.coord[kk]) & 1) {
                             acc.re -= v.re;
                             acc.im -= v.im;
                         } else {
@@ -498,12 +469,18 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
             memset(&c64, 0, sizeof(c64));
             c64.z0 = sg.z0;
             c64.lo = sg.lo;
-            c64.zm = sg.zm & 15u;
-            c64.beta0 = sg.d > 0 ? sg.beta[0] : 0;
-            c64.beta1 = sg.d > 1 ? sg.beta[1] : 0;
-            for (size_t u = 0; u < sg.table.size() && u < 4; ++u) {
-                const float re = (float)sg.table[u].re, im = (float)sg.table[u].im;
-                c64.tab[u] = make_float4(re, re, im, im);
+            const bool big = (sg.d == kFat) || sg.d > 2;
+            if (!big) {
+                c64.beta0 = sg.d > 0 ? sg.beta[0] : 0;
+                c64.beta1 = sg.d > 1 ? sg.beta[1] : 0;
+                for (size_t u = 0; u < sg.table.size(); ++u) {
+                    c64.tab[2 * u] = (float)sg.table[u].re;
+                    c64.tab[2 * u + 1] = (float)sg.table[u].im;
+                }
+                const uint32_t xm = ((sg.lo >> pl.tb) != 0) ? 1u : 0u;
+                c64.kind = (sg.zm & 15u) | (xm << 4) | (sg.d << 5);
+            } else {
+                c64.kind = 1u << 8;
             }
             sd.push_back(c64);
         }
