@@ -122,6 +122,36 @@ int qr_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
                 const uint64_t *indices, const double *data, const double *v, double *y,
                 void *stream);
 
+/* Replace the coefficients of the operator's T terms (same order and
+ * meaning as in qr_op_create); terms, masks and phases are unchanged.
+ * Cached plans are rebuilt on next use (synchronous).  Replaces building a
+ * new SparsePauliOp (qrusty/src/lib.rs:354-376) when only c changes, as in
+ * gradient-based coefficient optimisation. */
+int qr_op_set_coeffs(qr_op *op, const double *coeff);
+
+/* out[s] = <a_s, b_s> = sum_r conj(a_s[r]) * b_s[r] for nstates states of
+ * 2^n amplitudes, accumulated in FP64 (complex128 out: 2 doubles per state,
+ * device pointer).  dtype QR_C128 or QR_C64C (inputs complex64).  New: no
+ * reference counterpart (qrusty leaves inner products to numpy). */
+int qr_vdot(int32_t n, int32_t dtype, const void *a, const void *b, int32_t nstates,
+            double *out, void *stream);
+
+/* out[s] = <psi_s| H |psi_s> in FP64 (2 doubles per state, device pointer);
+ * H psi is formed in an operator-owned device buffer.  New: no reference
+ * counterpart (spmat_dot_densevec + numpy vdot in qrusty's sandbox). */
+int qr_expect(qr_op *op, int32_t dtype, const void *psi, int32_t nstates, double *out,
+              void *stream);
+
+/* Gradient of the coefficients of y = H(c) psi: for every INPUT term k,
+ * out[k] = sum_s <P_k psi_s, g_s> (complex128, 2 doubles per term, device
+ * pointer), where P_k = (1, -i, -1, +i)[phase_k] X^x_k Z^z_k is the term
+ * without its coefficient and g the upstream gradient.  For real
+ * coefficients the gradient is Re(out[k]).  FP32 products for QR_C64C,
+ * FP64 accumulation across threads and tiles.  New: no reference
+ * counterpart (used by the autograd backward). */
+int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32_t nstates,
+                 double *out, void *stream);
+
 /* Message of the calling thread's last failure ("" if none).  Copies at
  * most len-1 bytes plus a terminating NUL; returns the full length. */
 int qr_last_error(char *buf, size_t len);

@@ -73,6 +73,9 @@ def lib():
         L.or_apply_rows.argtypes = [C.c_size_t, _u64p, _u64p, _f64p, C.c_uint64, C.c_uint64,
                                     _f64p, _f64p, C.c_int]
         L.or_apply_rows.restype = None
+        L.or_term_grad.argtypes = [C.c_size_t, C.c_int, _u64p, _u64p, _u8p, _f64p, _f64p, _f64p,
+                                   C.c_int]
+        L.or_term_grad.restype = None
         _lib = L
     return _lib
 
@@ -169,3 +172,16 @@ def apply_rows(x, z, cprime, psi, row_lo, row_hi, nthreads=None):
 
 def apply(n, x, z, cprime, psi, nthreads=None):
     return apply_rows(x, z, cprime, psi, 0, 1 << n, nthreads)
+
+
+def term_grad(n, x, z, phase, psi, g, nthreads=None):
+    """<P_k psi, g> per term in FP64 (definition check for the autograd
+    backward; no reference counterpart)."""
+    x = np.ascontiguousarray(x, dtype=np.uint64)
+    z = np.ascontiguousarray(z, dtype=np.uint64)
+    ph = np.ascontiguousarray(phase, dtype=np.uint8)
+    p = np.ascontiguousarray(psi, dtype=np.complex128).view(np.float64)
+    gg = np.ascontiguousarray(g, dtype=np.complex128).view(np.float64)
+    out = np.empty(2 * len(x), dtype=np.float64)
+    lib().or_term_grad(len(x), n, z, x, ph, p, gg, out, nthreads or default_threads())
+    return out.view(np.complex128)

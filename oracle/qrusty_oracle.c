@@ -363,3 +363,45 @@ void or_apply_rows(size_t T, const uint64_t *z, const uint64_t *x, const double 
     atomic_init(&c.next, 0);
     run_pool(nthreads, mf_worker, &c);
 }
+
+/* ------------------------------------------------------------------ */
+/* Per-term coefficient gradient, FP64 definition check (no reference   */
+/* counterpart: qrusty has no gradients).  out[k] = <P_k psi, g> =      */
+/* sum_r conj(m(phase_k) (-1)^popc(r & z_k) psi[r ^ x_k]) g[r].         */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    size_t T, N; const uint64_t *x, *z; const uint8_t *phase;
+    const cplx *psi, *g; cplx *out;
+    atomic_size_t next;
+} tg_ctx;
+
+static void *tg_worker(void *arg)
+{
+    static const cplx m[4] = {{1.0, 0.0}, {0.0, -1.0}, {-1.0, 0.0}, {0.0, 1.0}};
+    tg_ctx *c = (tg_ctx *)arg;
+    for (;;) {
+        size_t k = atomic_fetch_add(&c->next, 1);
+        if (k >= c->T) break;
+        cplx s = {0.0, 0.0};
+        for (size_t r = 0; r < c->N; ++r) {
+            cplx p = c->psi[r ^ c->x[k]];
+            cplx v = {p.re * c->g[r].re + p.im * c->g[r].im, p.re * c->g[r].im - p.im * c->g[r].re};
+            if (__builtin_popcountll(r & c->z[k]) & 1) v = c_neg(v);
+            s = c_add(s, v);
+        }
+        cplx u = m[c->phase[k] % 4];
+        cplx uc = {u.re, -u.im};
+        c->out[k] = c_mul(uc, s);
+    }
+    return NULL;
+}
+
+void or_term_grad(size_t T, int n, const uint64_t *z, const uint64_t *x, const uint8_t *phase,
+                  const double *psi, const double *g, double *out, int nthreads)
+{
+    tg_ctx c;
+    c.T = T; c.N = (size_t)1 << n; c.x = x; c.z = z; c.phase = phase;
+    c.psi = (const cplx *)psi; c.g = (const cplx *)g; c.out = (cplx *)out;
+    atomic_init(&c.next, 0);
+    run_pool(nthreads, tg_worker, &c);
+}

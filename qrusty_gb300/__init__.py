@@ -5,7 +5,7 @@ package for this path (Pauli, SparsePauliOp, SpMat, spmat_dot_densevec,
 csr_matrix), backed by libqrusty_gpu.so (C ABI: include/qrusty_gpu.h).
 """
 from .pyqrusty import (Pauli, PauliOperator, QrError, SparsePauliOp, SpMat, csr_matrix,
-                       parse_mode, spmat_dot_densevec)
+                       parse_mode, spmat_dot_densevec, vdot)
 
 __all__ = ["Pauli", "SparsePauliOp", "SpMat", "spmat_dot_densevec", "csr_matrix",
-           "PauliOperator", "QrError", "parse_mode"]
+           "PauliOperator", "QrError", "parse_mode", "vdot"]

@@ -26,8 +26,8 @@ QR_C64C = 1
 # Every entry point include/qrusty_gpu.h declares (checked by the tests).
 EXPORTS = (
     "qr_op_create", "qr_op_destroy", "qr_op_get_info", "qr_csr_size", "qr_csr_build",
-    "qr_apply", "qr_check", "qr_apply_host", "qr_csr_spmv", "qr_last_error",
-    "qr_launch_count",
+    "qr_apply", "qr_check", "qr_apply_host", "qr_csr_spmv", "qr_op_set_coeffs", "qr_vdot",
+    "qr_expect", "qr_term_grad", "qr_last_error", "qr_launch_count",
 )
 
 
@@ -74,6 +74,10 @@ def load(build_if_missing: bool = True):
     L.qr_check.argtypes = [vp, vp]
     L.qr_apply_host.argtypes = [vp, i32, vp, vp, i32, i32]
     L.qr_csr_spmv.argtypes = [u64, u64, vp, vp, vp, vp, vp, vp]
+    L.qr_op_set_coeffs.argtypes = [vp, vp]
+    L.qr_vdot.argtypes = [i32, i32, vp, vp, i32, vp, vp]
+    L.qr_expect.argtypes = [vp, i32, vp, i32, vp, vp]
+    L.qr_term_grad.argtypes = [vp, i32, vp, vp, i32, vp, vp]
     L.qr_last_error.argtypes = [C.c_char_p, C.c_size_t]
     for name in EXPORTS:
         getattr(L, name).restype = C.c_int

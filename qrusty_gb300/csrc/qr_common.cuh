@@ -101,4 +101,14 @@ cudaError_t launch_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indp
                             const uint64_t *indices, const double *data, const double *v,
                             double *y, int nsm, cudaStream_t st);
 
+// qr_reduce.cu
+uint32_t vdot_blocks(uint64_t N, int nsm);
+cudaError_t launch_vdot(int dtype, uint64_t N, const void *a, const void *b, int nstates,
+                        double2 *partial, uint32_t nblk, double2 *out, cudaStream_t st);
+cudaError_t launch_term_grad(int dtype, uint64_t N, int nstates, const uint64_t *sx,
+                             const uint64_t *sz, uint32_t nstr, const void *psi, const void *g,
+                             double2 *partial, uint32_t nchunk, uint64_t chunk, double2 *R,
+                             uint64_t T, const uint32_t *map, const uint8_t *phase, double2 *out,
+                             cudaStream_t st);
+
 }  // namespace qr

@@ -121,9 +121,15 @@ struct qr_op {
     std::vector<int64_t> esig;
     bool csr_uploaded = false;
     DevBuf d_gx, d_goff, d_tz, d_tc, d_eoff, d_ebit, d_esig;
-    // merged terms (FP64 simplification) for qr_apply
+    // merged terms (FP64 simplification) for qr_apply; mmap[k] = merged index
     std::vector<uint64_t> mx, mz;
     std::vector<cd> mc;
+    std::vector<uint32_t> mmap;
+    std::vector<uint8_t> ph;            // input phases
+    std::vector<uint64_t> csr_order;    // input index of CSR term i
+    DevBuf d_mx, d_mz, d_mmap, d_ph;    // term-gradient tables (lazy)
+    bool grad_uploaded = false;
+    DevBuf expect_y;                    // H psi buffer of qr_expect
     Plan plans[2][2];  // [dtype][adjoint]
     DevBuf d_err;
     // host-call staging
@@ -175,6 +181,7 @@ int prepare_csr_tables(qr_op *op) {
     }
     op->goff.push_back((uint32_t)T);
     op->G = op->gx.size();
+    op->csr_order = order;
     std::vector<std::vector<std::pair<uint8_t, int64_t>>> ent(op->G);
     build_trie(op->gx, 0, op->G, op->n - 1, ent);
     op->eoff.assign(1, 0);
@@ -215,15 +222,18 @@ void merge_terms(qr_op *op) {
     op->mx.clear();
     op->mz.clear();
     op->mc.clear();
+    op->mmap.assign(op->T, 0);
     for (uint64_t k = 0; k < op->T; ++k) {
         auto key = std::make_pair(op->x[k], op->z[k]);
         auto it = idx.find(key);
         if (it == idx.end()) {
+            op->mmap[k] = (uint32_t)op->mx.size();
             idx.emplace(key, op->mx.size());
             op->mx.push_back(op->x[k]);
             op->mz.push_back(op->z[k]);
             op->mc.push_back(op->cp[k]);
         } else {
+            op->mmap[k] = (uint32_t)it->second;
             cd &c = op->mc[it->second];
             c.re += op->cp[k].re;
             c.im += op->cp[k].im;
@@ -592,6 +602,7 @@ int qr_op_create(int32_t n, uint64_t nterms, const uint64_t *x, const uint64_t *
     op->T = nterms;
     op->x.assign(x, x + nterms);
     op->z.assign(z, z + nterms);
+    op->ph.assign(phase, phase + nterms);
     op->cp.resize(nterms);
     // make_params (qrusty/src/accel.rs:141-157): c' = m(phase) * c, with
     // num-complex's product (ar*br - ai*bi, ar*bi + ai*br), no FMA.
@@ -817,6 +828,125 @@ int qr_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr, const ui
     QR_CUDA(launch_csr_spmv(nrows, ncols, indptr, indices, data, v, y, nsm,
                             static_cast<cudaStream_t>(stream)),
             "csr spmv launch");
+    return QR_OK;
+}
+
+int qr_op_set_coeffs(qr_op *op, const double *coeff) {
+    if (!op || !coeff) return fail(QR_EINVAL, "qr_op_set_coeffs: null argument");
+    int rc = check_device(op);
+    if (rc) return rc;
+    QR_CUDA(cudaDeviceSynchronize(), "qr_op_set_coeffs sync");
+    static const cd m[4] = {{1.0, 0.0}, {0.0, -1.0}, {-1.0, 0.0}, {0.0, 1.0}};
+    for (uint64_t k = 0; k < op->T; ++k) {
+        const cd a = m[op->ph[k] & 3];
+        const cd b{coeff[2 * k], coeff[2 * k + 1]};
+        op->cp[k].re = a.re * b.re - a.im * b.im;
+        op->cp[k].im = a.re * b.im + a.im * b.re;
+    }
+    for (uint64_t i = 0; i < op->T; ++i) op->tc[i] = op->cp[op->csr_order[i]];
+    op->csr_uploaded = false;
+    if (!op->mx.empty()) {
+        for (auto &c : op->mc) c = cd{0.0, 0.0};
+        std::vector<bool> seen(op->mx.size(), false);
+        for (uint64_t k = 0; k < op->T; ++k) {
+            const uint32_t mi = op->mmap[k];
+            if (!seen[mi]) {
+                op->mc[mi] = op->cp[k];
+                seen[mi] = true;
+            } else {
+                op->mc[mi].re += op->cp[k].re;
+                op->mc[mi].im += op->cp[k].im;
+            }
+        }
+    }
+    for (int d = 0; d < 2; ++d)
+        for (int j = 0; j < 2; ++j) {
+            Plan &pl = op->plans[d][j];
+            pl.built = false;
+            pl.groups.release();
+            pl.tables.release();
+            pl.fat_z.release();
+            pl.fat_c.release();
+            pl.blk_hi.release();
+            pl.blk_g0.release();
+            pl.diag.release();
+            pl.sub.release();
+        }
+    return QR_OK;
+}
+
+int qr_vdot(int32_t n, int32_t dtype, const void *a, const void *b, int32_t nstates, double *out,
+            void *stream) {
+    if (!a || !b || !out) return fail(QR_EINVAL, "qr_vdot: null argument");
+    if (n < 1 || n > 40) return fail(QR_EINVAL, "qr_vdot: n=%d outside [1, 40]", n);
+    if (dtype != QR_C128 && dtype != QR_C64C) return fail(QR_EINVAL, "qr_vdot: bad dtype");
+    if (nstates < 1) return fail(QR_EINVAL, "qr_vdot: nstates=%d < 1", nstates);
+    int dev = 0, nsm = 0;
+    QR_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    QR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const uint64_t N = 1ull << n;
+    const uint32_t nblk = vdot_blocks(N, nsm);
+    void *partial = nullptr;
+    QR_CUDA(cudaMallocAsync(&partial, (size_t)nstates * nblk * sizeof(double2), st),
+            "vdot scratch");
+    cudaError_t e = launch_vdot(dtype, N, a, b, nstates, static_cast<double2 *>(partial), nblk,
+                                reinterpret_cast<double2 *>(out), st);
+    cudaFreeAsync(partial, st);
+    if (e != cudaSuccess) return cuda_fail(e, "vdot launch");
+    return QR_OK;
+}
+
+int qr_expect(qr_op *op, int32_t dtype, const void *psi, int32_t nstates, double *out,
+              void *stream) {
+    if (!op || !psi || !out) return fail(QR_EINVAL, "qr_expect: null argument");
+    if (dtype != QR_C128 && dtype != QR_C64C) return fail(QR_EINVAL, "qr_expect: bad dtype");
+    if (nstates < 1) return fail(QR_EINVAL, "qr_expect: nstates=%d < 1", nstates);
+    int rc = check_device(op);
+    if (rc) return rc;
+    const size_t esz = dtype == QR_C128 ? 16 : 8;
+    const uint64_t bytes = (uint64_t)nstates * op->N * esz;
+    if (op->expect_y.bytes < bytes) QR_CUDA(op->expect_y.alloc(bytes), "alloc expect buffer");
+    rc = qr_apply(op, dtype, psi, op->expect_y.p, nstates, 0, stream);
+    if (rc) return rc;
+    return qr_vdot(op->n, dtype, psi, op->expect_y.p, nstates, out, stream);
+}
+
+int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32_t nstates,
+                 double *out, void *stream) {
+    if (!op || !psi || !g || !out) return fail(QR_EINVAL, "qr_term_grad: null argument");
+    if (dtype != QR_C128 && dtype != QR_C64C) return fail(QR_EINVAL, "qr_term_grad: bad dtype");
+    if (nstates < 1) return fail(QR_EINVAL, "qr_term_grad: nstates=%d < 1", nstates);
+    if (op->n > 40) return fail(QR_EINVAL, "qr_term_grad: n=%d too large", op->n);
+    int rc = check_device(op);
+    if (rc) return rc;
+    if (op->mx.empty()) merge_terms(op);
+    if (!op->grad_uploaded) {
+        QR_CUDA(op->d_mx.upload(op->mx), "upload merged x");
+        QR_CUDA(op->d_mz.upload(op->mz), "upload merged z");
+        QR_CUDA(op->d_mmap.upload(op->mmap), "upload term map");
+        QR_CUDA(op->d_ph.upload(op->ph), "upload phases");
+        op->grad_uploaded = true;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const uint32_t nstr = (uint32_t)op->mx.size();
+    uint64_t nchunk = ((uint64_t)op->nsm * 8 + nstr - 1) / nstr;
+    const uint64_t maxc = op->N >= 4096 ? op->N / 4096 : 1;
+    if (nchunk > maxc) nchunk = maxc;
+    if (nchunk < 1) nchunk = 1;
+    const uint64_t chunk = (op->N + nchunk - 1) / nchunk;
+    void *scratch = nullptr;
+    const size_t pbytes = (size_t)nstr * nchunk * sizeof(double2);
+    QR_CUDA(cudaMallocAsync(&scratch, pbytes + (size_t)nstr * sizeof(double2), st),
+            "term-grad scratch");
+    double2 *partial = static_cast<double2 *>(scratch);
+    double2 *R = partial + (size_t)nstr * nchunk;
+    cudaError_t e = launch_term_grad(dtype, op->N, nstates, op->d_mx.as<uint64_t>(),
+                                     op->d_mz.as<uint64_t>(), nstr, psi, g, partial,
+                                     (uint32_t)nchunk, chunk, R, op->T, op->d_mmap.as<uint32_t>(),
+                                     op->d_ph.as<uint8_t>(), reinterpret_cast<double2 *>(out), st);
+    cudaFreeAsync(scratch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "term-grad launch");
     return QR_OK;
 }
 

@@ -1,0 +1,214 @@
+// qr_reduce.cu -- FP64 reductions over state vectors on sm_103a:
+//   * <a, b> per state (qr_vdot, and <psi|H|psi> through qr_expect),
+//   * per-string coefficient gradients R_m = sum_r (-1)^popc(r & z_m)
+//     conj(psi[r ^ x_m]) g[r] (qr_term_grad).
+// Partial sums are written per block into stream-ordered scratch and summed
+// by a second kernel in a fixed order, so results are deterministic.
+#include "qr_common.cuh"
+
+namespace qr {
+
+constexpr int kRedThreads = 256;
+
+// Block-wide FP64 complex sum; result valid in thread 0.
+__device__ __forceinline__ double2 block_sum(double re, double im, double2 *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = make_double2(re, im);
+    __syncthreads();
+    double2 r = make_double2(0.0, 0.0);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            r.x += sh[i].x;
+            r.y += sh[i].y;
+        }
+    }
+    __syncthreads();
+    return r;
+}
+
+// partial[s * nblk + blk] = sum over this block's slice of conj(a) b.
+// c64 inputs: FP32 products, FP64 accumulation.  c128: FP64 throughout.
+template <bool F32>
+__global__ void __launch_bounds__(kRedThreads) vdot_partial_kernel(uint64_t N, const void *a_,
+                                                                   const void *b_, uint32_t nblk,
+                                                                   double2 *partial) {
+    __shared__ double2 sh[kRedThreads / 32];
+    const uint32_t s = blockIdx.y;
+    double re = 0.0, im = 0.0;
+    const uint64_t stride = (uint64_t)nblk * blockDim.x;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += stride) {
+        if constexpr (F32) {
+            const float2 a = static_cast<const float2 *>(a_)[s * N + r];
+            const float2 b = static_cast<const float2 *>(b_)[s * N + r];
+            re += (double)fmaf(a.x, b.x, a.y * b.y);
+            im += (double)fmaf(a.x, b.y, -a.y * b.x);
+        } else {
+            const double2 a = static_cast<const double2 *>(a_)[s * N + r];
+            const double2 b = static_cast<const double2 *>(b_)[s * N + r];
+            re = fma(a.x, b.x, fma(a.y, b.y, re));
+            im = fma(a.x, b.y, fma(-a.y, b.x, im));
+        }
+    }
+    const double2 t = block_sum(re, im, sh);
+    if (threadIdx.x == 0) partial[(size_t)s * nblk + blockIdx.x] = t;
+}
+
+// out[s] = sum_i partial[s * nblk + i] (fixed order: thread-strided, then
+// the block sum).
+__global__ void __launch_bounds__(kRedThreads) sum_partials_kernel(const double2 *partial,
+                                                                   uint32_t nblk, double2 *out) {
+    __shared__ double2 sh[kRedThreads / 32];
+    const uint32_t s = blockIdx.x;
+    double re = 0.0, im = 0.0;
+    for (uint32_t i = threadIdx.x; i < nblk; i += blockDim.x) {
+        re += partial[(size_t)s * nblk + i].x;
+        im += partial[(size_t)s * nblk + i].y;
+    }
+    const double2 t = block_sum(re, im, sh);
+    if (threadIdx.x == 0) out[s] = t;
+}
+
+uint32_t vdot_blocks(uint64_t N, int nsm) {
+    uint64_t b = (N + (uint64_t)kRedThreads * 16 - 1) / ((uint64_t)kRedThreads * 16);
+    const uint64_t cap = (uint64_t)nsm * 4;
+    if (b > cap) b = cap;
+    if (b == 0) b = 1;
+    return (uint32_t)b;
+}
+
+cudaError_t launch_vdot(int dtype, uint64_t N, const void *a, const void *b, int nstates,
+                        double2 *partial, uint32_t nblk, double2 *out, cudaStream_t st) {
+    const dim3 grid(nblk, (unsigned)nstates);
+    if (dtype == 1)
+        vdot_partial_kernel<true><<<grid, kRedThreads, 0, st>>>(N, a, b, nblk, partial);
+    else
+        vdot_partial_kernel<false><<<grid, kRedThreads, 0, st>>>(N, a, b, nblk, partial);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    sum_partials_kernel<<<(unsigned)nstates, kRedThreads, 0, st>>>(partial, nblk, out);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- term grads
+// One block per (string m, chunk c): sum over the chunk's rows r of
+// (-1)^popc(r & z_m) conj(psi[r ^ x_m]) g[r], over all states.  c64 inputs:
+// FP32 products and per-thread FP32 sums over <= kGradPerThread rows, then
+// FP64 across threads and chunks.  partial[m * nchunk + c].
+constexpr int kGradPerThread = 32;
+
+template <bool F32>
+__global__ void __launch_bounds__(kRedThreads) term_grad_partial_kernel(
+    uint64_t N, int nstates, const uint64_t *sx, const uint64_t *sz, uint32_t nstr,
+    const void *psi_, const void *g_, uint64_t chunk, uint32_t nchunk, double2 *partial) {
+    __shared__ double2 sh[kRedThreads / 32];
+    for (uint32_t m = blockIdx.y; m < nstr; m += gridDim.y) {
+        const uint64_t x = sx[m], z = sz[m];
+        double re = 0.0, im = 0.0;
+        for (uint32_t c = blockIdx.x; c < nchunk; c += gridDim.x) {
+            const uint64_t r0 = (uint64_t)c * chunk, r1 = (r0 + chunk < N) ? r0 + chunk : N;
+            for (int s = 0; s < nstates; ++s) {
+                if constexpr (F32) {
+                    const float2 *psi = static_cast<const float2 *>(psi_) + (size_t)s * N;
+                    const float2 *g = static_cast<const float2 *>(g_) + (size_t)s * N;
+                    float fr = 0.f, fi = 0.f;
+                    int k = 0;
+                    for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+                        const float2 p = psi[r ^ x];
+                        const float2 gg = g[r];
+                        // conj(p) * g
+                        float pr = fmaf(p.x, gg.x, p.y * gg.y);
+                        float pi = fmaf(p.x, gg.y, -p.y * gg.x);
+                        if (__popcll(r & z) & 1) {
+                            pr = -pr;
+                            pi = -pi;
+                        }
+                        fr += pr;
+                        fi += pi;
+                        if (++k == kGradPerThread) {
+                            re += (double)fr;
+                            im += (double)fi;
+                            fr = fi = 0.f;
+                            k = 0;
+                        }
+                    }
+                    re += (double)fr;
+                    im += (double)fi;
+                } else {
+                    const double2 *psi = static_cast<const double2 *>(psi_) + (size_t)s * N;
+                    const double2 *g = static_cast<const double2 *>(g_) + (size_t)s * N;
+                    for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+                        const double2 p = psi[r ^ x];
+                        const double2 gg = g[r];
+                        double pr = fma(p.x, gg.x, p.y * gg.y);
+                        double pi = fma(p.x, gg.y, -p.y * gg.x);
+                        if (__popcll(r & z) & 1) {
+                            pr = -pr;
+                            pi = -pi;
+                        }
+                        re += pr;
+                        im += pi;
+                    }
+                }
+            }
+        }
+        const double2 t = block_sum(re, im, sh);
+        if (threadIdx.x == 0) partial[(size_t)m * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// out[k] = conj(unit(phase_k)) * R[map[k]], unit = (1, -i, -1, +i)[phase].
+__global__ void __launch_bounds__(kRedThreads) term_grad_scatter_kernel(uint64_t T,
+                                                                        const uint32_t *map,
+                                                                        const uint8_t *phase,
+                                                                        const double2 *R,
+                                                                        double2 *out) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < T;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const double2 v = R[map[k]];
+        double2 o;
+        switch (phase[k] & 3) {
+            case 0: o = v; break;                                   // conj(1) = 1
+            case 1: o = make_double2(-v.y, v.x); break;             // conj(-i) = i
+            case 2: o = make_double2(-v.x, -v.y); break;            // -1
+            default: o = make_double2(v.y, -v.x); break;            // conj(i) = -i
+        }
+        out[k] = o;
+    }
+}
+
+cudaError_t launch_term_grad(int dtype, uint64_t N, int nstates, const uint64_t *sx,
+                             const uint64_t *sz, uint32_t nstr, const void *psi, const void *g,
+                             double2 *partial, uint32_t nchunk, uint64_t chunk, double2 *R,
+                             uint64_t T, const uint32_t *map, const uint8_t *phase, double2 *out,
+                             cudaStream_t st) {
+    const unsigned gy = nstr < 65535u ? nstr : 65535u;
+    const dim3 grid(nchunk, gy);
+    if (dtype == 1)
+        term_grad_partial_kernel<true><<<grid, kRedThreads, 0, st>>>(N, nstates, sx, sz, nstr, psi,
+                                                                     g, chunk, nchunk, partial);
+    else
+        term_grad_partial_kernel<false><<<grid, kRedThreads, 0, st>>>(N, nstates, sx, sz, nstr,
+                                                                      psi, g, chunk, nchunk,
+                                                                      partial);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    sum_partials_kernel<<<nstr, kRedThreads, 0, st>>>(partial, nchunk, R);
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    uint64_t gb = (T + kRedThreads - 1) / kRedThreads;
+    if (gb > 4096) gb = 4096;
+    term_grad_scatter_kernel<<<(unsigned)gb, kRedThreads, 0, st>>>(T, map, phase, R, out);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace qr

@@ -31,7 +31,7 @@ from . import _lib
 from ._lib import QR_C128, QR_C64C, QR_MEM_HOST, QrError, check
 
 __all__ = ["Pauli", "SparsePauliOp", "SpMat", "PauliOperator", "spmat_dot_densevec",
-           "csr_matrix", "QrError", "parse_mode"]
+           "csr_matrix", "QrError", "parse_mode", "vdot"]
 
 _LABEL_RE = re.compile(r"^([+-]?)1?([ij]?)([IXYZ]+)$")
 
@@ -243,6 +243,49 @@ class PauliOperator:
                                    int(bool(adjoint)), st))
         return y
 
+    def set_coeffs(self, coeffs):
+        """Replace the coefficients (same terms); plans are rebuilt lazily."""
+        c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+        if c.shape != (self.nterms,):
+            raise ValueError("expected %d coefficients" % self.nterms)
+        check(_lib.load().qr_op_set_coeffs(self._h, c.ctypes.data))
+        self._c = c
+
+    @staticmethod
+    def _dtype_of(t):
+        import torch
+        if t.dtype == torch.complex64:
+            return QR_C64C
+        if t.dtype == torch.complex128:
+            return QR_C128
+        raise TypeError("states must be complex64 or complex128")
+
+    def expect(self, psi):
+        """<psi|H|psi> per state (FP64 reduction), complex128 CUDA tensor."""
+        import torch
+        N = 1 << self.n
+        p = psi.contiguous()
+        ns = p.numel() // N
+        out = torch.empty(ns, dtype=torch.complex128, device=p.device)
+        st = torch.cuda.current_stream(p.device).cuda_stream
+        check(_lib.load().qr_expect(self._h, self._dtype_of(p), p.data_ptr(), ns,
+                                    out.data_ptr(), st))
+        return out
+
+    def term_grad(self, psi, g):
+        """sum_s <P_k psi_s, g_s> for every input term k (complex128 tensor)."""
+        import torch
+        N = 1 << self.n
+        p, gg = psi.contiguous(), g.contiguous()
+        if p.dtype != gg.dtype or p.shape != gg.shape:
+            raise ValueError("psi and g must have the same dtype and shape")
+        ns = p.numel() // N
+        out = torch.empty(self.nterms, dtype=torch.complex128, device=p.device)
+        st = torch.cuda.current_stream(p.device).cuda_stream
+        check(_lib.load().qr_term_grad(self._h, self._dtype_of(p), p.data_ptr(), gg.data_ptr(),
+                                       ns, out.data_ptr(), st))
+        return out
+
     def sync_check(self, stream=None):
         import torch
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
@@ -445,6 +488,24 @@ def spmat_dot_densevec(spmat: SpMat, x):
     check(_lib.load().qr_csr_spmv(shape[0], shape[1], indptr.data_ptr(), indices.data_ptr(),
                                   data.data_ptr(), xd.data_ptr(), yd.data_ptr(), st))
     return yd.cpu().numpy()
+
+
+def vdot(a, b):
+    """<a_s, b_s> per state in FP64 for CUDA tensors of 2^n (or S x 2^n)
+    complex64 / complex128 amplitudes; complex128 tensor of S values."""
+    import torch
+    if a.dtype != b.dtype or a.shape != b.shape:
+        raise ValueError("a and b must have the same dtype and shape")
+    N = a.shape[-1]
+    n = N.bit_length() - 1
+    if N != 1 << n:
+        raise ValueError("last dimension must be a power of two")
+    ns = a.numel() // N
+    out = torch.empty(ns, dtype=torch.complex128, device=a.device)
+    st = torch.cuda.current_stream(a.device).cuda_stream
+    check(_lib.load().qr_vdot(n, PauliOperator._dtype_of(a), a.contiguous().data_ptr(),
+                              b.contiguous().data_ptr(), ns, out.data_ptr(), st))
+    return out
 
 
 def csr_matrix(m: SpMat):
