@@ -55,6 +55,7 @@ class _PauliApply(torch.autograd.Function):
         ctx.c_host = c_host
         ctx.real = not coeffs.is_complex()
         ctx.cdtype = coeffs.dtype
+        ctx.cdevice = coeffs.device
         return y
 
     @staticmethod
@@ -67,7 +68,7 @@ class _PauliApply(torch.autograd.Function):
             grad_psi = op.apply(gy, adjoint=True)
         if ctx.needs_input_grad[0]:
             tg = op.term_grad(psi.contiguous(), gy)
-            grad_c = (tg.real if ctx.real else tg).to(ctx.cdtype)
+            grad_c = (tg.real if ctx.real else tg).to(device=ctx.cdevice, dtype=ctx.cdtype)
         return grad_c, grad_psi, None
 
 
