@@ -136,6 +136,29 @@ int qr_op_set_coeffs(qr_op *op, const double *coeff);
 int qr_vdot(int32_t n, int32_t dtype, const void *a, const void *b, int32_t nstates,
             double *out, void *stream);
 
+/* Allocation-free variant of qr_vdot.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory while they run: hosts whose
+ * device memory is reserved up front by another allocator (a framework's
+ * caching allocator or a fixed per-process budget), and latency-critical
+ * loops that must not take the synchronisation or pool growth that
+ * cudaMalloc / cudaMallocAsync can bring.  Same inputs, output and FP64
+ * result as qr_vdot; the per-block partial sums live in a fixed
+ * 256 KiB (QR_VDOT_NOALLOC_MAX_PARTIALS double2 entries) __device__ array that
+ * every GPU loading this library holds until process exit, and no call
+ * allocates or frees anything.
+ *  - The first call on a device looks up that array's device address
+ *    (cudaGetSymbolAddress, with the device current) and caches it; make
+ *    that first call before any stream capture.
+ *  - nstates may be at most QR_VDOT_NOALLOC_MAX_PARTIALS (QR_EINVAL
+ *    otherwise); the block count per state shrinks as nstates grows.
+ *  - All calls share the one array: calls whose kernels overlap on the GPU
+ *    (other streams, other host threads) race and must be serialised by the
+ *    caller. */
+#define QR_VDOT_NOALLOC_MAX_PARTIALS 16384
+int qr_vdot_noalloc(int32_t n, int32_t dtype, const void *a, const void *b, int32_t nstates,
+                    double *out, void *stream);
+
 /* out[s] = <psi_s| H |psi_s> in FP64 (2 doubles per state, device pointer);
  * H psi is formed in an operator-owned device buffer.  New: no reference
  * counterpart (spmat_dot_densevec + numpy vdot in qrusty's sandbox). */

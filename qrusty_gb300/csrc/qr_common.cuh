@@ -72,6 +72,9 @@ struct ApplyArgs {
 // Device error codes written to the error word.
 enum : int { kErrNone = 0, kErrMbarTimeout = 1, kErrCsrPos = 2 };
 
+// Records msg as the calling thread's last error (qr_last_error) and returns code.
+int set_error(int code, const char *msg);
+
 // Per-process launch counter (all launches issued through this library).
 void count_launch(uint64_t k = 1);
 

@@ -42,6 +42,7 @@ static int fail(int code, const char *fmt, ...) {
 static int cuda_fail(cudaError_t e, const char *what) {
     return fail(QR_ECUDA, "%s: %s", what, cudaGetErrorString(e));
 }
+int set_error(int code, const char *msg) { return fail(code, "%s", msg); }
 
 #define QR_CUDA(call, what)                          \
     do {                                             \

@@ -4,6 +4,10 @@
 //     conj(psi[r ^ x_m]) g[r] (qr_term_grad).
 // Partial sums are written per block into stream-ordered scratch and summed
 // by a second kernel in a fixed order, so results are deterministic.
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/qrusty_gpu.h"
 #include "qr_common.cuh"
 
 namespace qr {
@@ -212,3 +216,80 @@ cudaError_t launch_term_grad(int dtype, uint64_t N, int nstates, const uint64_t 
 }
 
 }  // namespace qr
+
+namespace qr {
+
+// ---------------------------------------------------------------- no-alloc vdot
+// Fixed scratch of the allocation-free inner product: one FP64 complex
+// partial sum per (state, block).  A file-scope __device__ array, so every
+// GPU that loads this library holds these 256 KiB until the process exits.
+constexpr uint32_t kNoAllocPartials = QR_VDOT_NOALLOC_MAX_PARTIALS;
+static __device__ __align__(256) double2 g_vdot_scratch[kNoAllocPartials];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+double2 *g_scratch_ptr[kMaxDevices] = {};
+int g_scratch_nsm[kMaxDevices] = {};
+
+// Device address of g_vdot_scratch on the current device.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up
+// once per device with cudaGetSymbolAddress (device current) and cached.
+int noalloc_scratch(double2 **out, int *nsm) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(QR_ECUDA, "qr_vdot_noalloc: cudaGetDevice failed");
+    if (dev < 0 || dev >= kMaxDevices)
+        return set_error(QR_ESTATE, "qr_vdot_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_vdot_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            char buf[256];
+            snprintf(buf, sizeof(buf), "qr_vdot_noalloc: cudaGetSymbolAddress failed: %s",
+                     cudaGetErrorString(e));
+            return set_error(QR_ECUDA, buf);
+        }
+        int n = 0;
+        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return set_error(QR_ECUDA, "qr_vdot_noalloc: device attribute");
+        g_scratch_ptr[dev] = static_cast<double2 *>(p);
+        g_scratch_nsm[dev] = n;
+    }
+    *out = g_scratch_ptr[dev];
+    *nsm = g_scratch_nsm[dev];
+    return QR_OK;
+}
+}  // namespace
+
+}  // namespace qr
+
+extern "C" int qr_vdot_noalloc(int32_t n, int32_t dtype, const void *a, const void *b,
+                               int32_t nstates, double *out, void *stream) {
+    using namespace qr;
+    if (!a || !b || !out) return set_error(QR_EINVAL, "qr_vdot_noalloc: null argument");
+    if (n < 1 || n > 40) return set_error(QR_EINVAL, "qr_vdot_noalloc: n outside [1, 40]");
+    if (dtype != QR_C128 && dtype != QR_C64C)
+        return set_error(QR_EINVAL, "qr_vdot_noalloc: dtype must be QR_C128 or QR_C64C");
+    if (nstates < 1) return set_error(QR_EINVAL, "qr_vdot_noalloc: nstates < 1");
+    if ((uint32_t)nstates > kNoAllocPartials)
+        return set_error(QR_EINVAL,
+                         "qr_vdot_noalloc: nstates exceeds QR_VDOT_NOALLOC_MAX_PARTIALS (16384); "
+                         "use qr_vdot");
+    double2 *scratch = nullptr;
+    int nsm = 0;
+    int rc = noalloc_scratch(&scratch, &nsm);
+    if (rc) return rc;
+    const uint64_t N = 1ull << n;
+    uint32_t nblk = vdot_blocks(N, nsm);
+    const uint32_t cap = kNoAllocPartials / (uint32_t)nstates;  // >= 1 by the check above
+    if (nblk > cap) nblk = cap;
+    // Every (state, block) slot used below is written by the partial-sum
+    // kernel before the second kernel reads it, so nothing is cleared.
+    cudaError_t e = launch_vdot(dtype, N, a, b, nstates, scratch, nblk,
+                                reinterpret_cast<double2 *>(out),
+                                static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return set_error(QR_ECUDA, "qr_vdot_noalloc: kernel launch failed");
+    return QR_OK;
+}
