@@ -319,8 +319,8 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 }
 
 // ---------------------------------------------------------------- c64c kernel
-// Compensated complex64 path.  512 threads x AMPS = 8 amplitudes per 4096-
-// amplitude tile; thread t owns r_lo = t + 512 m.  The host splits every
+// Compensated complex64 path.  256 threads x AMPS = 16 amplitudes per 4096-
+// amplitude tile; thread t owns r_lo = t + 256 m.  The host splits every
 // x-group into sub-groups whose z masks agree on the register bits
 // [kTb, kTb + log2 AMPS), so for a thread the sub-group's factor is
 //     D_m = (-1)^popc(m & zm) * Dt,   Dt = (-1)^popc(r0 & z0) * tab[u],
@@ -330,17 +330,18 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 // amplitude is one shared-memory load and two packed FMAs:
 //     A_m += (+-Dt.re) * p,  B_m += (+-Dt.im) * p      (fma.rn.f32x2)
 // and y = A + iB is folded into the running (hi, lo) two-sum pair every
-// kFlush partner tiles.
+// kFlush partner tiles; hi stays in registers, the error term lo (touched
+// only at a fold) lives in shared memory.
 //
 // Pipeline: a kC64Stages-deep ring of partner tiles filled by 1-D TMA bulk
 // copies.  Warps run decoupled: each waits on the stage's full mbarrier,
 // consumes it, and counts itself out on a shared counter; the last warp out
 // refills the stage with the tile kC64Stages steps ahead.  No CTA-wide
 // barrier sits on the steady-state path.
-constexpr int kTb = 9;          // log2(threads) whenever AMPS >= 2
+constexpr int kTb = 8;          // log2(threads) whenever AMPS >= 2
 constexpr int kMsh = kTb + 3;   // byte shift of the register index m
 constexpr int kFlush = 8;       // partner tiles per compensated fold
-constexpr int kC64Threads = 512;
+constexpr int kC64Threads = 256;
 constexpr int kC64Stages = 6;
 
 template <bool WIDE>
@@ -462,7 +463,8 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
     const uint32_t t = threadIdx.x;
     const uint32_t lane = t & 31;
     const uint32_t tile_bytes = (1u << a.b) * 8u;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)kC64Stages * tile_bytes);
+    float2 *s_lo = reinterpret_cast<float2 *>(smem_raw + (size_t)kC64Stages * tile_bytes);
+    uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * blockDim.x);
     uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kC64Stages);
 
     const float2 *psi = static_cast<const float2 *>(a.psi);
@@ -501,7 +503,8 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
     }
     __syncthreads();
 
-    float2 A[AMPS], B[AMPS], hi[AMPS], lo[AMPS];
+    float2 A[AMPS], B[AMPS], hi[AMPS];
+    float2 *mylo = s_lo + t;  // lo[m] at mylo[m * threads]
     const SubDescC64 *subs = a.sub;
     const uint32_t nsub = a.nsub;
     // loop state advanced incrementally (no division on the steady path)
@@ -518,7 +521,10 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
         const uint64_t r0 = (q << a.b) | t;
         if (j == 0) {
 #pragma unroll
-            for (int m = 0; m < AMPS; ++m) A[m] = B[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
+            for (int m = 0; m < AMPS; ++m) {
+                A[m] = B[m] = hi[m] = make_float2(0.f, 0.f);
+                mylo[m * threads] = make_float2(0.f, 0.f);
+            }
         }
         if (!mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
             if (lane == 0) atomicExch(a.err, kErrMbarTimeout);
@@ -568,17 +574,21 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
             for (int m = 0; m < AMPS; ++m) {
                 const float yr = __fsub_rn(A[m].x, B[m].y);
                 const float yi = __fadd_rn(A[m].y, B[m].x);
-                two_sum_into(hi[m].x, lo[m].x, yr);
-                two_sum_into(hi[m].y, lo[m].y, yi);
+                float2 lm = mylo[m * threads];
+                two_sum_into(hi[m].x, lm.x, yr);
+                two_sum_into(hi[m].y, lm.y, yi);
+                mylo[m * threads] = lm;
                 A[m] = B[m] = make_float2(0.f, 0.f);
             }
         }
         if (last) {
             float2 *yo = y + st * a.N + (q << a.b);
 #pragma unroll
-            for (int m = 0; m < AMPS; ++m)
+            for (int m = 0; m < AMPS; ++m) {
+                const float2 lm = mylo[m * threads];
                 yo[t + threads * (uint32_t)m] =
-                    make_float2(__fadd_rn(hi[m].x, lo[m].x), __fadd_rn(hi[m].y, lo[m].y));
+                    make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
+            }
         }
 
         // this warp is done with stage s; the last warp out refills it
@@ -614,7 +624,8 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
 template <int AMPS, bool WIDE>
 static cudaError_t launch_c64c_w(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
     const uint32_t tile_bytes = (1u << a.b) * 8u;
-    const size_t smem = (size_t)kC64Stages * tile_bytes + kC64Stages * (sizeof(uint64_t) + 4);
+    const size_t smem = (size_t)kC64Stages * tile_bytes + (size_t)AMPS * threads * 8u +
+                        kC64Stages * (sizeof(uint64_t) + 4);
     auto kern = apply_c64c<AMPS, WIDE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);

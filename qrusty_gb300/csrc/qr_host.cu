@@ -312,7 +312,7 @@ int build_plan(qr_op *op, int dtype, int adjoint) {
     const int n = op->n;
     const bool f32 = dtype == QR_C64C;
     pl.b = std::min(n, 12);
-    const int tmax = f32 ? 512 : 256;
+    const int tmax = f32 ? 256 : 256;
     pl.threads = std::min(1 << pl.b, tmax);
     pl.amps = (1 << pl.b) / pl.threads;
     pl.tb = 0;
