@@ -382,20 +382,27 @@ __device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                           const unsigned char *sm, uint32_t off, float2 D,
                                           const SubDescC64 *ndp, uint64_t r0n, uint32_t t,
                                           uint32_t tmask, int tb, GroupState &next) {
+    // Phase 1: all partner loads (independent, so their latency overlaps).
+    // XM: the sub-group's x has register bits, so partners are permuted by
+    // XOR; otherwise the offsets are compile-time immediates.
+    float2 p[AMPS];
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
+        p[m] = *reinterpret_cast<const float2 *>(sm + o);
+    }
+    // Phase 2: the next sub-group's setup (its own load/parity chain).
     const SubDescC64 nd = *ndp;
+    next = group_setup<WIDE>(nd, r0n, t, tmask, tb);
+    // Phase 3: packed FMAs with the compile-time sign pattern.
     const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
     const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
 #pragma unroll
     for (int m = 0; m < AMPS; ++m) {
-        // XM: the sub-group's x has register bits, so partners are permuted by
-        // XOR; otherwise the offsets are compile-time immediates.
-        const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
-        const float2 p = *reinterpret_cast<const float2 *>(sm + o);
         const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
-        A[m] = __ffma2_rn(neg ? an : ap, p, A[m]);
-        B[m] = __ffma2_rn(neg ? bn : bp, p, B[m]);
+        A[m] = __ffma2_rn(neg ? an : ap, p[m], A[m]);
+        B[m] = __ffma2_rn(neg ? bn : bp, p[m], B[m]);
     }
-    next = group_setup<WIDE>(nd, r0n, t, tmask, tb);
 }
 
 template <int AMPS, bool WIDE>
