@@ -175,6 +175,27 @@ int qr_expect(qr_op *op, int32_t dtype, const void *psi, int32_t nstates, double
 int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32_t nstates,
                  double *out, void *stream);
 
+/* Batched H psi: many operators, each with its own states, in ONE
+ * persistent kernel launch over a work list of (operator, state, amplitude
+ * tile) items, replayed from a CUDA graph.  Compensated complex64 only.
+ * New: no reference counterpart (qrusty applies one operator at a time).
+ *
+ * qr_batch_create: ops[i] (all on the current device, n <= 32) with
+ * nstates[i] states each.  The operators must outlive the batch, and their
+ * coefficients must not change while it exists.
+ * qr_batch_apply: psi[i] / y[i] are device pointers to operator i's
+ * nstates[i] complex64 states (back to back).  The first call chooses the
+ * amplitude-tile width by timing each candidate on the given buffers (the
+ * autotuner; y is overwritten) and captures the launch into a CUDA graph;
+ * every call launches that graph on `stream`.  A call whose pointers differ
+ * from the previous call's synchronises `stream` before uploading them. */
+typedef struct qr_batch qr_batch;
+int qr_batch_create(int32_t nops, qr_op *const *ops, const int32_t *nstates, qr_batch **out);
+int qr_batch_destroy(qr_batch *b);
+int qr_batch_apply(qr_batch *b, const void *const *psi, void *const *y, void *stream);
+/* Tile width the autotuner chose (log2 amplitudes; 0 before the first apply). */
+int qr_batch_tile_bits(const qr_batch *b);
+
 /* Message of the calling thread's last failure ("" if none).  Copies at
  * most len-1 bytes plus a terminating NUL; returns the full length. */
 int qr_last_error(char *buf, size_t len);

@@ -4,8 +4,8 @@
 package for this path (Pauli, SparsePauliOp, SpMat, spmat_dot_densevec,
 csr_matrix), backed by libqrusty_gpu.so (C ABI: include/qrusty_gpu.h).
 """
-from .pyqrusty import (Pauli, PauliOperator, QrError, SparsePauliOp, SpMat, csr_matrix,
+from .pyqrusty import (Batch, Pauli, PauliOperator, QrError, SparsePauliOp, SpMat, csr_matrix,
                        parse_mode, spmat_dot_densevec, vdot)
 
 __all__ = ["Pauli", "SparsePauliOp", "SpMat", "spmat_dot_densevec", "csr_matrix",
-           "PauliOperator", "QrError", "parse_mode", "vdot"]
+           "PauliOperator", "QrError", "parse_mode", "vdot", "Batch"]

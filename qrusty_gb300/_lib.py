@@ -27,7 +27,8 @@ QR_C64C = 1
 EXPORTS = (
     "qr_op_create", "qr_op_destroy", "qr_op_get_info", "qr_csr_size", "qr_csr_build",
     "qr_apply", "qr_check", "qr_apply_host", "qr_csr_spmv", "qr_op_set_coeffs", "qr_vdot",
-    "qr_expect", "qr_term_grad", "qr_vdot_noalloc", "qr_last_error", "qr_launch_count",
+    "qr_expect", "qr_term_grad", "qr_vdot_noalloc", "qr_batch_create", "qr_batch_destroy",
+    "qr_batch_apply", "qr_batch_tile_bits", "qr_last_error", "qr_launch_count",
 )
 
 
@@ -78,6 +79,10 @@ def load(build_if_missing: bool = True):
     L.qr_vdot.argtypes = [i32, i32, vp, vp, i32, vp, vp]
     L.qr_expect.argtypes = [vp, i32, vp, i32, vp, vp]
     L.qr_vdot_noalloc.argtypes = [i32, i32, vp, vp, i32, vp, vp]
+    L.qr_batch_create.argtypes = [i32, vp, vp, C.POINTER(vp)]
+    L.qr_batch_destroy.argtypes = [vp]
+    L.qr_batch_apply.argtypes = [vp, vp, vp, vp]
+    L.qr_batch_tile_bits.argtypes = [vp]
     L.qr_term_grad.argtypes = [vp, i32, vp, vp, i32, vp, vp]
     L.qr_last_error.argtypes = [C.c_char_p, C.c_size_t]
     for name in EXPORTS:

@@ -650,6 +650,214 @@ static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStr
     return launch_c64c_w<AMPS, false>(a, threads, nsm, st);
 }
 
+// ---------------------------------------------------------------- batched c64c
+// Many operators (different n, term counts and state counts) in ONE
+// persistent launch over a host-built work list of (operator, state, tile)
+// items.  Same partner-tile ring and inner step as apply_c64c; the operator's
+// parameters come from a device array per item, tiles of operators with
+// n < 12 use the first 2^n amplitudes of a stage, and the warp that refills a
+// stage walks the work list six steps ahead to find the tile to load.
+template <int AMPS, int ZM, bool XM>
+__device__ __forceinline__ void mloop_plain(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                            const unsigned char *sm, uint32_t off, float2 D) {
+    float2 p[AMPS];
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
+        p[m] = *reinterpret_cast<const float2 *>(sm + o);
+    }
+    const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
+    const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
+        A[m] = __ffma2_rn(neg ? an : ap, p[m], A[m]);
+        B[m] = __ffma2_rn(neg ? bn : bp, p[m], B[m]);
+    }
+}
+
+template <int AMPS>
+__device__ __forceinline__ void mloop_plain_dispatch(uint32_t key, float2 (&A)[AMPS],
+                                                     float2 (&B)[AMPS], const unsigned char *sm,
+                                                     uint32_t off, float2 D) {
+#define QR_ZM_CASE(k)                                                                   \
+    case k:                                                                             \
+        if constexpr ((k & 15) < AMPS) mloop_plain<AMPS, (k & 15), (k >> 4) != 0>(A, B, sm, off, D); \
+        break;
+    switch (key) {
+        QR_ZM_CASE(0) QR_ZM_CASE(1) QR_ZM_CASE(2) QR_ZM_CASE(3)
+        QR_ZM_CASE(4) QR_ZM_CASE(5) QR_ZM_CASE(6) QR_ZM_CASE(7)
+        QR_ZM_CASE(8) QR_ZM_CASE(9) QR_ZM_CASE(10) QR_ZM_CASE(11)
+        QR_ZM_CASE(12) QR_ZM_CASE(13) QR_ZM_CASE(14) QR_ZM_CASE(15)
+        QR_ZM_CASE(16) QR_ZM_CASE(17) QR_ZM_CASE(18) QR_ZM_CASE(19)
+        QR_ZM_CASE(20) QR_ZM_CASE(21) QR_ZM_CASE(22) QR_ZM_CASE(23)
+        QR_ZM_CASE(24) QR_ZM_CASE(25) QR_ZM_CASE(26) QR_ZM_CASE(27)
+        QR_ZM_CASE(28) QR_ZM_CASE(29) QR_ZM_CASE(30) QR_ZM_CASE(31)
+        default: break;
+    }
+#undef QR_ZM_CASE
+}
+
+template <int AMPS>
+__global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr uint32_t kStageBytes = 4096u * 8u;
+    const uint32_t threads = blockDim.x;
+    const uint32_t nwarps = threads >> 5;
+    const uint32_t t = threadIdx.x;
+    const uint32_t lane = t & 31;
+    float2 *s_lo = reinterpret_cast<float2 *>(smem_raw + (size_t)kC64Stages * kStageBytes);
+    uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kC64Stages);
+    const uint32_t stride = gridDim.x;
+    if (blockIdx.x >= a.nitems) return;
+
+    // step cursor (item index, block of that item's operator) -> next step
+    auto advance = [&](uint32_t &ik, uint32_t &j) {
+        if (++j == a.ops[a.items[ik].op].nblocks) {
+            j = 0;
+            ik += stride;
+        }
+    };
+    auto issue = [&](uint32_t ik, uint32_t j, int s) {
+        const BatchItem it = a.items[ik];
+        const BatchOp &o = a.ops[it.op];
+        const uint32_t bytes = (1u << o.b) * 8u;
+        const float2 *src =
+            a.psi[it.op] + (uint64_t)it.state * o.N + (((uint64_t)it.tile ^ o.blk_hi[j]) << o.b);
+        mbar_expect_tx(&full[s], bytes);
+        bulk_g2s(smem_raw + (size_t)s * kStageBytes, src, bytes, &full[s]);
+    };
+    if (t == 0) {
+        for (int s = 0; s < kC64Stages; ++s) {
+            mbar_init(&full[s], 1);
+            cnt[s] = 0;
+        }
+        mbar_fence_init();
+        uint32_t ik = blockIdx.x, j = 0;
+        for (int s = 0; s < kC64Stages && ik < a.nitems; ++s) {
+            issue(ik, j, s);
+            advance(ik, j);
+        }
+    }
+    __syncthreads();
+
+    float2 A[AMPS], B[AMPS], hi[AMPS];
+    float2 *mylo = s_lo + t;
+    uint32_t ik = blockIdx.x, j = 0, s = 0, par = 0;
+    while (ik < a.nitems) {
+        const BatchItem it = a.items[ik];
+        const BatchOp &o = a.ops[it.op];
+        const uint32_t tmask = (uint32_t)o.tact - 1;
+        const uint64_t r0 = ((uint64_t)it.tile << o.b) | t;
+        const bool active = t < (uint32_t)o.tact;
+        if (j == 0) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                A[m] = B[m] = hi[m] = make_float2(0.f, 0.f);
+                mylo[m * threads] = make_float2(0.f, 0.f);
+            }
+        }
+        if (!mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
+            if (lane == 0) atomicExch(a.err, kErrMbarTimeout);
+            return;
+        }
+        const uint32_t soff = s * kStageBytes;
+        if ((int)j == o.diag_block && o.diag != nullptr && active) {
+            const float2 *dg = o.diag + ((uint64_t)it.tile << o.b);
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                if (m < o.mcount) {
+                    const uint32_t rl = t + (uint32_t)o.tact * (uint32_t)m;
+                    const float2 d = dg[rl];
+                    const float2 p = *reinterpret_cast<const float2 *>(smem_raw + soff + rl * 8u);
+                    A[m] = __ffma2_rn(make_float2(d.x, d.x), p, A[m]);
+                    B[m] = __ffma2_rn(make_float2(d.y, d.y), p, B[m]);
+                }
+            }
+        }
+        const uint32_t g1 = o.blk_g0[j + 1];
+        for (uint32_t g = o.blk_g0[j]; g < g1; ++g) {
+            const SubDescC64 *sd = o.sub + g;
+            const uint32_t lo = sd->lo, kind = sd->kind;
+            const uint32_t off = soff | ((t ^ (lo & tmask)) << 3) | ((lo >> o.tb) << kMsh);
+            if ((kind >> 8) == 0) {
+                const uint32_t u = parity<false>(r0, sd->beta0) |
+                                   (parity<false>(r0, sd->beta1) << 1);
+                float dx = (u & 2u) ? ((u & 1u) ? sd->tab[6] : sd->tab[4])
+                                    : ((u & 1u) ? sd->tab[2] : sd->tab[0]);
+                float dy = (u & 2u) ? ((u & 1u) ? sd->tab[7] : sd->tab[5])
+                                    : ((u & 1u) ? sd->tab[3] : sd->tab[1]);
+                if (parity<false>(r0, sd->z0)) {
+                    dx = -dx;
+                    dy = -dy;
+                }
+                mloop_plain_dispatch<AMPS>(kind & 31u, A, B, smem_raw, off, make_float2(dx, dy));
+            } else {
+                big_group_c64<AMPS>(A, B, smem_raw, off, o.groups[g], r0, o.tb, o.tables,
+                                    o.fat_z, o.fat_c);
+            }
+        }
+        const bool last = (j == o.nblocks - 1);
+        if (last || (j % kFlush) == kFlush - 1) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const float yr = __fsub_rn(A[m].x, B[m].y);
+                const float yi = __fadd_rn(A[m].y, B[m].x);
+                float2 lm = mylo[m * threads];
+                two_sum_into(hi[m].x, lm.x, yr);
+                two_sum_into(hi[m].y, lm.y, yi);
+                mylo[m * threads] = lm;
+                A[m] = B[m] = make_float2(0.f, 0.f);
+            }
+        }
+        if (last && active) {
+            float2 *yo = a.y[it.op] + (uint64_t)it.state * o.N + ((uint64_t)it.tile << o.b);
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                if (m < o.mcount) {
+                    const float2 lm = mylo[m * threads];
+                    yo[t + (uint32_t)o.tact * (uint32_t)m] =
+                        make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            const uint32_t old = atomicAdd(&cnt[s], 1u);
+            if (old == nwarps - 1) {
+                cnt[s] = 0;
+                uint32_t ik2 = ik, j2 = j;
+                for (int k = 0; k < kC64Stages && ik2 < a.nitems; ++k) advance(ik2, j2);
+                if (ik2 < a.nitems) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue(ik2, j2, (int)s);
+                }
+            }
+        }
+        if (++s == kC64Stages) {
+            s = 0;
+            par ^= 1u;
+        }
+        advance(ik, j);
+    }
+}
+
+cudaError_t launch_batch_c64c(const BatchArgs &a, int nsm, cudaStream_t st) {
+    const size_t smem = (size_t)kC64Stages * 4096u * 8u + (size_t)16 * kC64Threads * 8u +
+                        kC64Stages * (sizeof(uint64_t) + 4);
+    auto kern = apply_c64c_batch<16>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid = a.nitems < (uint32_t)nsm ? a.nitems : (uint32_t)nsm;
+    if (grid == 0) return cudaSuccess;
+    kern<<<grid, kC64Threads, smem, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <typename Real, int AMPS, bool COMP>
 static cudaError_t launch_one(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
     const uint32_t tile_bytes = (1u << a.b) * (uint32_t)sizeof(Cplx<Real>);

@@ -69,6 +69,34 @@ struct ApplyArgs {
 
 
 
+// One operator of a batched compensated-c64 launch (device copy).
+struct BatchOp {
+    uint64_t N, ntiles;
+    int32_t b, tb, mcount, tact;      // tile bits, log2(active threads), amps used, threads used
+    uint32_t nblocks, nsub;
+    int32_t diag_block, pad;
+    const SubDescC64 *sub;
+    const GroupDesc *groups;
+    const float2 *tables;
+    const uint64_t *fat_z;
+    const float2 *fat_c;
+    const uint64_t *blk_hi;
+    const uint32_t *blk_g0;
+    const float2 *diag;
+};
+struct BatchItem {
+    uint32_t op, state, tile, pad;
+};
+struct BatchArgs {
+    const BatchOp *ops;
+    const BatchItem *items;
+    uint32_t nitems;
+    const float2 *const *psi;  // per operator: its first state; state s at + s * N
+    float2 *const *y;
+    int *err;
+};
+cudaError_t launch_batch_c64c(const BatchArgs &a, int nsm, cudaStream_t st);
+
 // Device error codes written to the error word.
 enum : int { kErrNone = 0, kErrMbarTimeout = 1, kErrCsrPos = 2 };
 

@@ -132,6 +132,7 @@ struct qr_op {
     bool grad_uploaded = false;
     DevBuf expect_y;                    // H psi buffer of qr_expect
     Plan plans[2][2];  // [dtype][adjoint]
+    Plan bplans[13];   // compensated-c64 plans with an explicit tile width (batched launches)
     DevBuf d_err;
     // host-call staging
     cudaStream_t hstream = nullptr;
@@ -305,13 +306,13 @@ struct SubGroup {
     std::vector<cd> fc;
 };
 
-int build_plan(qr_op *op, int dtype, int adjoint) {
-    Plan &pl = op->plans[dtype][adjoint];
+int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
+    Plan &pl = tile_bits < 0 ? op->plans[dtype][adjoint] : op->bplans[tile_bits];
     if (pl.built) return QR_OK;
     if (op->mx.empty()) merge_terms(op);
     const int n = op->n;
     const bool f32 = dtype == QR_C64C;
-    pl.b = std::min(n, 12);
+    pl.b = tile_bits < 0 ? std::min(n, 12) : std::min(n, tile_bits);
     const int tmax = f32 ? 256 : 256;
     pl.threads = std::min(1 << pl.b, tmax);
     pl.amps = (1 << pl.b) / pl.threads;
@@ -863,6 +864,17 @@ int qr_op_set_coeffs(qr_op *op, const double *coeff) {
     for (int d = 0; d < 2; ++d)
         for (int j = 0; j < 2; ++j) {
             Plan &pl = op->plans[d][j];
+            for (Plan &bp : op->bplans) {
+                bp.built = false;
+                bp.groups.release();
+                bp.tables.release();
+                bp.fat_z.release();
+                bp.fat_c.release();
+                bp.blk_hi.release();
+                bp.blk_g0.release();
+                bp.diag.release();
+                bp.sub.release();
+            }
             pl.built = false;
             pl.groups.release();
             pl.tables.release();
@@ -948,6 +960,211 @@ int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32
                                      op->d_ph.as<uint8_t>(), reinterpret_cast<double2 *>(out), st);
     cudaFreeAsync(scratch, st);
     if (e != cudaSuccess) return cuda_fail(e, "term-grad launch");
+    return QR_OK;
+}
+
+}  // extern "C"
+
+struct qr_batch {
+    int device = 0, nsm = 0;
+    std::vector<qr_op *> ops;
+    std::vector<int32_t> nstates;
+    int tile_bits = 0;
+    DevBuf d_ops, d_items, d_ptrs, d_err;
+    uint32_t nitems = 0;
+    std::vector<const void *> cur_psi;
+    std::vector<void *> cur_y;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap = nullptr;
+};
+
+namespace {
+
+// Operator tables and the work list for tile width tb; items are ordered by
+// decreasing per-tile work so the persistent CTAs' round-robin balances.
+int batch_build(qr_batch *bt, int tb) {
+    std::vector<BatchOp> bo(bt->ops.size());
+    std::vector<std::pair<double, size_t>> cost;
+    for (size_t i = 0; i < bt->ops.size(); ++i) {
+        qr_op *op = bt->ops[i];
+        int rc = build_plan(op, QR_C64C, 0, tb);
+        if (rc) return rc;
+        const Plan &pl = op->bplans[tb];
+        BatchOp &o = bo[i];
+        memset(&o, 0, sizeof(o));
+        o.N = op->N;
+        o.b = pl.b;
+        o.tb = pl.tb;
+        o.mcount = pl.amps;
+        o.tact = pl.threads;
+        o.ntiles = op->N >> pl.b;
+        o.nblocks = pl.nblocks;
+        o.nsub = pl.nsub;
+        o.diag_block = pl.diag_block;
+        o.sub = pl.sub.as<SubDescC64>();
+        o.groups = pl.groups.as<GroupDesc>();
+        o.tables = pl.tables.as<float2>();
+        o.fat_z = pl.fat_z.as<uint64_t>();
+        o.fat_c = pl.fat_c.as<float2>();
+        o.blk_hi = pl.blk_hi.as<uint64_t>();
+        o.blk_g0 = pl.blk_g0.as<uint32_t>();
+        o.diag = pl.has_diag ? pl.diag.as<float2>() : nullptr;
+        cost.push_back({(double)(pl.nsub + 2 * pl.nblocks) * (double)(1u << pl.b), i});
+    }
+    std::stable_sort(cost.begin(), cost.end(),
+                     [](const std::pair<double, size_t> &a, const std::pair<double, size_t> &b) {
+                         return a.first > b.first;
+                     });
+    std::vector<BatchItem> items;
+    for (auto &c : cost) {
+        const size_t i = c.second;
+        for (int32_t st = 0; st < bt->nstates[i]; ++st)
+            for (uint64_t q = 0; q < bo[i].ntiles; ++q)
+                items.push_back(BatchItem{(uint32_t)i, (uint32_t)st, (uint32_t)q, 0u});
+    }
+    if (items.size() > 0xffffffffull) return fail(QR_EINVAL, "qr_batch: work list too long");
+    bt->nitems = (uint32_t)items.size();
+    QR_CUDA(bt->d_ops.upload(bo), "upload batch operators");
+    QR_CUDA(bt->d_items.upload(items), "upload batch work list");
+    bt->tile_bits = tb;
+    return QR_OK;
+}
+
+BatchArgs batch_args(qr_batch *bt) {
+    BatchArgs a;
+    a.ops = bt->d_ops.as<BatchOp>();
+    a.items = bt->d_items.as<BatchItem>();
+    a.nitems = bt->nitems;
+    float2 **pp = bt->d_ptrs.as<float2 *>();
+    a.psi = pp;
+    a.y = pp + bt->ops.size();
+    a.err = bt->d_err.as<int>();
+    return a;
+}
+
+int batch_upload_ptrs(qr_batch *bt, const void *const *psi, void *const *y, cudaStream_t st) {
+    const size_t n = bt->ops.size();
+    bool same = bt->cur_psi.size() == n;
+    for (size_t i = 0; same && i < n; ++i) same = bt->cur_psi[i] == psi[i] && bt->cur_y[i] == y[i];
+    if (same) return QR_OK;
+    for (size_t i = 0; i < n; ++i) {
+        if (!psi[i] || !y[i]) return fail(QR_EINVAL, "qr_batch_apply: null state pointer");
+        if ((reinterpret_cast<uintptr_t>(psi[i]) | reinterpret_cast<uintptr_t>(y[i])) & 15)
+            return fail(QR_EINVAL, "qr_batch_apply: states must be 16-byte aligned");
+    }
+    QR_CUDA(cudaStreamSynchronize(st), "qr_batch_apply sync before pointer update");
+    std::vector<const void *> h(2 * n);
+    for (size_t i = 0; i < n; ++i) {
+        h[i] = psi[i];
+        h[n + i] = y[i];
+    }
+    QR_CUDA(cudaMemcpy(bt->d_ptrs.p, h.data(), h.size() * sizeof(void *), cudaMemcpyHostToDevice),
+            "upload batch pointers");
+    bt->cur_psi.assign(psi, psi + n);
+    bt->cur_y.assign(y, y + n);
+    return QR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qr_batch_create(int32_t nops, qr_op *const *ops, const int32_t *nstates, qr_batch **out) {
+    if (!out || !ops || !nstates || nops < 1) return fail(QR_EINVAL, "qr_batch_create: bad arguments");
+    *out = nullptr;
+    int dev = -1;
+    QR_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    for (int32_t i = 0; i < nops; ++i) {
+        if (!ops[i]) return fail(QR_EINVAL, "qr_batch_create: null operator %d", i);
+        if (ops[i]->device != dev)
+            return fail(QR_ESTATE, "qr_batch_create: operator %d is on another device", i);
+        if (ops[i]->n > 32) return fail(QR_EINVAL, "qr_batch_create: operator %d has n > 32", i);
+        if (nstates[i] < 1) return fail(QR_EINVAL, "qr_batch_create: nstates[%d] < 1", i);
+    }
+    qr_batch *bt = new (std::nothrow) qr_batch();
+    if (!bt) return fail(QR_ENOMEM, "qr_batch_create: out of host memory");
+    bt->device = dev;
+    bt->ops.assign(ops, ops + nops);
+    bt->nstates.assign(nstates, nstates + nops);
+    cudaError_t e = cudaDeviceGetAttribute(&bt->nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = bt->d_ptrs.alloc(2 * (size_t)nops * sizeof(void *));
+    if (e == cudaSuccess) e = bt->d_err.alloc(sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(bt->d_err.p, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bt->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete bt;
+        return cuda_fail(e, "qr_batch_create");
+    }
+    *out = bt;
+    return QR_OK;
+}
+
+int qr_batch_destroy(qr_batch *bt) {
+    if (!bt) return QR_OK;
+    if (bt->exec) cudaGraphExecDestroy(bt->exec);
+    if (bt->graph) cudaGraphDestroy(bt->graph);
+    if (bt->cap) cudaStreamDestroy(bt->cap);
+    delete bt;
+    return QR_OK;
+}
+
+int qr_batch_tile_bits(const qr_batch *bt) { return bt ? bt->tile_bits : 0; }
+
+int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *stream) {
+    if (!bt || !psi || !y) return fail(QR_EINVAL, "qr_batch_apply: null argument");
+    int dev = -1;
+    QR_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev != bt->device) return fail(QR_ESTATE, "qr_batch_apply: wrong current device");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = batch_upload_ptrs(bt, psi, y, st);
+    if (rc) return rc;
+    if (!bt->exec) {
+        // autotuner: time each candidate tile width on these buffers
+        int best = -1;
+        float best_ms = 0.f;
+        cudaEvent_t e0, e1;
+        QR_CUDA(cudaEventCreate(&e0), "event");
+        QR_CUDA(cudaEventCreate(&e1), "event");
+        for (int tb : {12, 11, 10}) {
+            rc = batch_build(bt, tb);
+            if (rc) break;
+            BatchArgs a = batch_args(bt);
+            cudaError_t e = launch_batch_c64c(a, bt->nsm, bt->cap);
+            if (e == cudaSuccess) e = cudaEventRecord(e0, bt->cap);
+            for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = launch_batch_c64c(a, bt->nsm, bt->cap);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, bt->cap);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "qr_batch autotune");
+                break;
+            }
+            if (best < 0 || ms < best_ms) {
+                best = tb;
+                best_ms = ms;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc) return rc;
+        rc = batch_build(bt, best);
+        if (rc) return rc;
+        BatchArgs a = batch_args(bt);
+        QR_CUDA(cudaStreamBeginCapture(bt->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+        cudaError_t e = launch_batch_c64c(a, bt->nsm, bt->cap);
+        cudaError_t e2 = cudaStreamEndCapture(bt->cap, &bt->graph);
+        if (e != cudaSuccess) return cuda_fail(e, "batch launch under capture");
+        if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
+        QR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0), "graph instantiate");
+        QR_CUDA(cudaStreamSynchronize(bt->cap), "autotune sync");
+        int h = 0;
+        QR_CUDA(cudaMemcpy(&h, bt->d_err.p, sizeof(int), cudaMemcpyDeviceToHost), "error word");
+        if (h) return fail(QR_EKERNEL, "batched kernel reported error %d", h);
+    }
+    QR_CUDA(cudaGraphLaunch(bt->exec, st), "graph launch");
+    count_launch();
     return QR_OK;
 }
 

@@ -31,7 +31,7 @@ from . import _lib
 from ._lib import QR_C128, QR_C64C, QR_MEM_HOST, QrError, check
 
 __all__ = ["Pauli", "SparsePauliOp", "SpMat", "PauliOperator", "spmat_dot_densevec",
-           "csr_matrix", "QrError", "parse_mode", "vdot"]
+           "csr_matrix", "QrError", "parse_mode", "vdot", "Batch"]
 
 _LABEL_RE = re.compile(r"^([+-]?)1?([ij]?)([IXYZ]+)$")
 
@@ -488,6 +488,59 @@ def spmat_dot_densevec(spmat: SpMat, x):
     check(_lib.load().qr_csr_spmv(shape[0], shape[1], indptr.data_ptr(), indices.data_ptr(),
                                   data.data_ptr(), xd.data_ptr(), yd.data_ptr(), st))
     return yd.cpu().numpy()
+
+
+class Batch:
+    """Many operators, each with its own complex64 states, applied in ONE
+    persistent kernel launch replayed from a CUDA graph (qr_batch_*).  The
+    first ``apply`` autotunes the amplitude-tile width on the given buffers."""
+
+    def __init__(self, ops, nstates):
+        self.ops = list(ops)
+        self.nstates = [int(s) for s in nstates]
+        if len(self.ops) != len(self.nstates) or not self.ops:
+            raise ValueError("ops and nstates must be non-empty and of equal length")
+        n = len(self.ops)
+        hs = (C.c_void_p * n)(*[op.handle.value for op in self.ops])
+        ns = (C.c_int32 * n)(*self.nstates)
+        h = C.c_void_p()
+        check(_lib.load().qr_batch_create(n, hs, ns, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().qr_batch_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def tile_bits(self) -> int:
+        return int(_lib.load().qr_batch_tile_bits(self._h))
+
+    def apply(self, psis, ys, stream=None):
+        """psis[i], ys[i]: CUDA complex64 tensors of nstates[i] x 2^n_i amplitudes."""
+        import torch
+        n = len(self.ops)
+        if len(psis) != n or len(ys) != n:
+            raise ValueError("one psi and one y per operator")
+        for i, (p, y) in enumerate(zip(psis, ys)):
+            want = self.nstates[i] << self.ops[i].n
+            for tns in (p, y):
+                if tns.dtype != torch.complex64 or not tns.is_cuda or not tns.is_contiguous():
+                    raise TypeError("batched states must be contiguous CUDA complex64 tensors")
+                if tns.numel() != want:
+                    raise ValueError("operator %d expects %d amplitudes" % (i, want))
+        pp = (C.c_void_p * n)(*[p.data_ptr() for p in psis])
+        yy = (C.c_void_p * n)(*[y.data_ptr() for y in ys])
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(_lib.load().qr_batch_apply(self._h, pp, yy, st))
+        return ys
 
 
 def vdot(a, b):
