@@ -1152,7 +1152,7 @@ int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *s
         rc = batch_build(bt, best);
         if (rc) return rc;
         BatchArgs a = batch_args(bt);
-        QR_CUDA(cudaStreamBeginCapture(bt->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+        QR_CUDA(cudaStreamBeginCapture(bt->cap, cudaStreamCaptureModeRelaxed), "begin capture");
         cudaError_t e = launch_batch_c64c(a, bt->nsm, bt->cap);
         cudaError_t e2 = cudaStreamEndCapture(bt->cap, &bt->graph);
         if (e != cudaSuccess) return cuda_fail(e, "batch launch under capture");
