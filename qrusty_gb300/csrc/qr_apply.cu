@@ -628,6 +628,247 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
     }
 }
 
+// ---------------------------------------------------------------- c64c, tile table
+// The production compensated-c64 kernel.  Same tiles, thread layout, partner
+// ring and two-sum folding as apply_c64c, with the per-sub-group work split
+// by who can do it once:
+//   * per output tile (cooperatively, into shared memory): for every
+//     sub-group the tile-index parity of z0 / beta0,1 applied to its table,
+//     stored pre-duplicated as (re, re, im, im) for the packed FMAs;
+//   * per thread: the parities of its thread index against 8-bit masks
+//     (skipped when the sub-group's masks miss the thread bits), one 16-byte
+//     table read, the partner offset;
+//   * per run of sub-groups with equal register-bit sign pattern: one
+//     dispatch to a compile-time instantiation.
+constexpr int kTabStages = 5;
+constexpr uint32_t kTabMaxSub = 512;  // per-tile table entries (64 B each)
+
+template <int AMPS, int ZM, bool XM>
+__device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                        const unsigned char *sm, uint32_t soff,
+                                        const float4 *s_tab, const uint2 *tdesc, uint32_t g0,
+                                        uint32_t g1, uint32_t t, uint32_t tmask, int tb) {
+    for (uint32_t g = g0; g < g1; ++g) {
+        const uint2 d = tdesc[g];
+        uint32_t u = 0, sg = 0;
+        if (d.x >> 24) {
+            sg = (uint32_t)__popc(t & (d.y & 0xffu)) & 1u;
+            u = ((uint32_t)__popc(t & ((d.y >> 8) & 0xffu)) & 1u) |
+                (((uint32_t)__popc(t & ((d.y >> 16) & 0xffu)) & 1u) << 1);
+        }
+        float4 T = s_tab[g * 4 + u];
+        if (sg) {
+            T.x = -T.x;
+            T.y = -T.y;
+            T.z = -T.z;
+            T.w = -T.w;
+        }
+        const uint32_t lo = d.x & 0xffffu;
+        const uint32_t off = soff | ((t ^ (lo & tmask)) << 3) | ((lo >> tb) << kMsh);
+        float2 p[AMPS];
+#pragma unroll
+        for (int m = 0; m < AMPS; ++m) {
+            const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
+            p[m] = *reinterpret_cast<const float2 *>(sm + o);
+        }
+        const float2 ap = make_float2(T.x, T.y), bp = make_float2(T.z, T.w);
+        const float2 an = make_float2(-T.x, -T.y), bn = make_float2(-T.z, -T.w);
+#pragma unroll
+        for (int m = 0; m < AMPS; ++m) {
+            const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
+            A[m] = __ffma2_rn(neg ? an : ap, p[m], A[m]);
+            B[m] = __ffma2_rn(neg ? bn : bp, p[m], B[m]);
+        }
+    }
+}
+
+template <int AMPS>
+__device__ __forceinline__ void run_tab_dispatch(uint32_t key, float2 (&A)[AMPS],
+                                                 float2 (&B)[AMPS], const unsigned char *sm,
+                                                 uint32_t soff, const float4 *s_tab,
+                                                 const uint2 *tdesc, uint32_t g0, uint32_t g1,
+                                                 uint32_t t, uint32_t tmask, int tb) {
+#define QR_RUN_CASE(k)                                                                    \
+    case k:                                                                               \
+        if constexpr ((k & 15) < AMPS)                                                    \
+            run_tab<AMPS, (k & 15), (k >> 4) != 0>(A, B, sm, soff, s_tab, tdesc, g0, g1, t, \
+                                                    tmask, tb);                           \
+        break;
+    switch (key) {
+        QR_RUN_CASE(0) QR_RUN_CASE(1) QR_RUN_CASE(2) QR_RUN_CASE(3)
+        QR_RUN_CASE(4) QR_RUN_CASE(5) QR_RUN_CASE(6) QR_RUN_CASE(7)
+        QR_RUN_CASE(8) QR_RUN_CASE(9) QR_RUN_CASE(10) QR_RUN_CASE(11)
+        QR_RUN_CASE(12) QR_RUN_CASE(13) QR_RUN_CASE(14) QR_RUN_CASE(15)
+        QR_RUN_CASE(16) QR_RUN_CASE(17) QR_RUN_CASE(18) QR_RUN_CASE(19)
+        QR_RUN_CASE(20) QR_RUN_CASE(21) QR_RUN_CASE(22) QR_RUN_CASE(23)
+        QR_RUN_CASE(24) QR_RUN_CASE(25) QR_RUN_CASE(26) QR_RUN_CASE(27)
+        QR_RUN_CASE(28) QR_RUN_CASE(29) QR_RUN_CASE(30) QR_RUN_CASE(31)
+        default: break;
+    }
+#undef QR_RUN_CASE
+}
+
+template <int AMPS, bool WIDE>
+__global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const uint32_t threads = blockDim.x;
+    const uint32_t nwarps = threads >> 5;
+    const uint32_t t = threadIdx.x;
+    const uint32_t lane = t & 31;
+    const uint32_t tile_bytes = (1u << a.b) * 8u;
+    float4 *s_tab = reinterpret_cast<float4 *>(smem_raw + (size_t)kTabStages * tile_bytes);
+    float2 *s_lo = reinterpret_cast<float2 *>(s_tab + 4 * (size_t)a.nsub);
+    uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kTabStages);
+    volatile uint32_t *s_abort = cnt + kTabStages;
+
+    const float2 *psi = static_cast<const float2 *>(a.psi);
+    float2 *y = static_cast<float2 *>(a.y);
+    const float2 *diag = static_cast<const float2 *>(a.diag);
+    const uint32_t nb = a.nblocks;
+    const uint32_t tmask = threads - 1;
+    const int tb = a.tb;
+
+    const uint64_t first = blockIdx.x;
+    const uint64_t my_items =
+        a.nitems > first ? (a.nitems - first + gridDim.x - 1) / gridDim.x : 0;
+    const uint64_t total = my_items * nb;
+    if (total == 0) return;
+
+    auto issue = [&](uint64_t L) {
+        const uint64_t k = L / nb;
+        const uint32_t j = (uint32_t)(L - k * nb);
+        const uint64_t item = first + k * gridDim.x;
+        const uint64_t st = item / a.ntiles;
+        const uint64_t q = item - st * a.ntiles;
+        const float2 *src = psi + st * a.N + ((q ^ a.blk_hi[j]) << a.b);
+        const int s = (int)(L % (uint64_t)kTabStages);
+        mbar_expect_tx(&full[s], tile_bytes);
+        bulk_g2s(smem_raw + (size_t)s * tile_bytes, src, tile_bytes, &full[s]);
+    };
+    if (t == 0) {
+        for (int s = 0; s < kTabStages; ++s) {
+            mbar_init(&full[s], 1);
+            cnt[s] = 0;
+        }
+        *s_abort = 0;
+        mbar_fence_init();
+        const uint64_t pro = total < (uint64_t)kTabStages ? total : (uint64_t)kTabStages;
+        for (uint64_t L = 0; L < pro; ++L) issue(L);
+    }
+    __syncthreads();
+
+    float2 A[AMPS], B[AMPS], hi[AMPS];
+    float2 *mylo = s_lo + t;
+    uint32_t j = 0, s = 0, par = 0;
+    uint64_t st = first / a.ntiles;
+    uint64_t q = first - st * a.ntiles;
+
+    for (uint64_t L = 0; L < total; ++L) {
+        if (j == 0) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                A[m] = B[m] = hi[m] = make_float2(0.f, 0.f);
+                mylo[m * threads] = make_float2(0.f, 0.f);
+            }
+            // per-tile table: every warp has finished the previous tile
+            __syncthreads();
+            for (uint32_t g = t; g < a.nsub; g += threads) {
+                const TileDataC64 &d = a.tdata[g];
+                const uint32_t uq = parity<WIDE>(q, d.b0h) | (parity<WIDE>(q, d.b1h) << 1);
+                const float sq = parity<WIDE>(q, d.z0h) ? -1.f : 1.f;
+#pragma unroll
+                for (uint32_t u = 0; u < 4; ++u) {
+                    const float2 v = d.T[u ^ uq];
+                    s_tab[g * 4 + u] = make_float4(sq * v.x, sq * v.x, sq * v.y, sq * v.y);
+                }
+            }
+            __syncthreads();
+        }
+        // A wait that expires sets the abort flag; from then on every warp
+        // skips waits and work but still reaches each tile barrier.
+        bool skip = *s_abort != 0;
+        if (!skip && !mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
+            if (lane == 0) {
+                atomicExch(a.err, kErrMbarTimeout);
+                *s_abort = 1;
+            }
+            skip = true;
+        }
+        skip = __any_sync(0xffffffffu, skip);
+        const uint32_t soff = s * tile_bytes;
+
+        if (!skip && (int)j == a.diag_block && diag != nullptr) {
+            const float2 *dg = diag + (q << a.b);
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const uint32_t rl = t + threads * (uint32_t)m;
+                const float2 d = dg[rl];
+                const float2 p = *reinterpret_cast<const float2 *>(smem_raw + soff + rl * 8u);
+                A[m] = __ffma2_rn(make_float2(d.x, d.x), p, A[m]);
+                B[m] = __ffma2_rn(make_float2(d.y, d.y), p, B[m]);
+            }
+        }
+
+        const uint32_t r1 = skip ? 0u : a.blk_r0[j + 1];
+        for (uint32_t r = a.blk_r0[j]; r < r1; ++r)
+            run_tab_dispatch<AMPS>(a.run_key[r], A, B, smem_raw, soff, s_tab, a.tdesc,
+                                   a.run_g0[r], a.run_g0[r + 1], t, tmask, tb);
+
+        const bool last = (j == nb - 1);
+        if (last || (j % kFlush) == kFlush - 1) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const float yr = __fsub_rn(A[m].x, B[m].y);
+                const float yi = __fadd_rn(A[m].y, B[m].x);
+                float2 lm = mylo[m * threads];
+                two_sum_into(hi[m].x, lm.x, yr);
+                two_sum_into(hi[m].y, lm.y, yi);
+                mylo[m * threads] = lm;
+                A[m] = B[m] = make_float2(0.f, 0.f);
+            }
+        }
+        if (last) {
+            float2 *yo = y + st * a.N + (q << a.b);
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const float2 lm = mylo[m * threads];
+                yo[t + threads * (uint32_t)m] =
+                    make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
+            }
+        }
+
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            const uint32_t old = atomicAdd(&cnt[s], 1u);
+            if (old == nwarps - 1) {
+                cnt[s] = 0;
+                if (L + (uint64_t)kTabStages < total && *s_abort == 0) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue(L + (uint64_t)kTabStages);
+                }
+            }
+        }
+        if (++s == kTabStages) {
+            s = 0;
+            par ^= 1u;
+        }
+        if (++j == nb) {
+            j = 0;
+            q += gridDim.x;
+            while (q >= a.ntiles) {
+                q -= a.ntiles;
+                ++st;
+            }
+        }
+    }
+    if (*s_abort && t == 0) {
+        // bounded drain of copies that may still target this CTA's stages
+        for (int k = 0; k < kTabStages; ++k) mbar_wait_bounded(&full[k], 0, kWaitLimitNs / 8);
+    }
+}
+
 template <int AMPS, bool WIDE>
 static cudaError_t launch_c64c_w(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
     const uint32_t tile_bytes = (1u << a.b) * 8u;
@@ -644,8 +885,28 @@ static cudaError_t launch_c64c_w(const ApplyArgs &a, int threads, int nsm, cudaS
     return cudaGetLastError();
 }
 
+template <int AMPS, bool WIDE>
+static cudaError_t launch_c64c_tab(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
+    const uint32_t tile_bytes = (1u << a.b) * 8u;
+    const size_t smem = (size_t)kTabStages * tile_bytes + (size_t)a.nsub * 64u +
+                        (size_t)AMPS * threads * 8u + kTabStages * (sizeof(uint64_t) + 4) + 4;
+    auto kern = apply_c64c_tab<AMPS, WIDE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    uint64_t grid = a.nitems < (uint64_t)nsm ? a.nitems : (uint64_t)nsm;
+    if (grid == 0) return cudaSuccess;
+    kern<<<(unsigned)grid, threads, smem, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <int AMPS>
 static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
+    if (a.nsub <= kTabMaxSub) {
+        if (a.n > 32) return launch_c64c_tab<AMPS, true>(a, threads, nsm, st);
+        return launch_c64c_tab<AMPS, false>(a, threads, nsm, st);
+    }
     if (a.n > 32) return launch_c64c_w<AMPS, true>(a, threads, nsm, st);
     return launch_c64c_w<AMPS, false>(a, threads, nsm, st);
 }

@@ -42,6 +42,13 @@ struct alignas(16) SubDescC64 {
     float tab[8];  // inline table: (re, im) x 4
 };
 
+// Per-sub-group data of the per-tile table of the compensated-c64 kernel:
+// the masks' tile-index parts (>> b) and the FP32 table T[u] of the factor.
+struct alignas(16) TileDataC64 {
+    uint64_t z0h, b0h, b1h, pad;
+    float2 T[4];
+};
+
 struct ApplyArgs {
     const void *psi;
     void *y;
@@ -65,6 +72,14 @@ struct ApplyArgs {
     // compensated-c64 plan: one SubDescC64 per sub-group (see qr_apply.cu)
     const SubDescC64 *sub;
     uint32_t nsub;
+    // per-tile-table kernel: per sub-group an 8-byte thread descriptor
+    // {lo | key << 16 | tvar << 24, z0_t | beta0_t << 8 | beta1_t << 16} and
+    // its TileDataC64; sub-groups of a block in runs of equal key
+    const uint2 *tdesc;
+    const TileDataC64 *tdata;
+    const uint32_t *blk_r0;   // runs of block j: [blk_r0[j], blk_r0[j+1])
+    const uint32_t *run_g0;   // sub-groups of run r: [run_g0[r], run_g0[r+1])
+    const uint32_t *run_key;  // key = zm | xm << 4
 };
 
 

@@ -97,6 +97,7 @@ struct Plan {
     // compensated-c64 kernel tables
     uint32_t nsub = 0;
     DevBuf sub;
+    DevBuf tdesc, tdata, blk_r0, run_g0, run_key;
 };
 
 }  // namespace qr
@@ -247,7 +248,7 @@ void merge_terms(qr_op *op) {
 // and the coordinates of every term's difference in that basis.
 struct Span {
     std::vector<uint64_t> basis;
-    std::vector<uint32_t> coord;  // per term
+    std::vector<uint64_t> coord;  // per term
     bool overflow = false;
 };
 Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
@@ -256,7 +257,7 @@ Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
     sp.coord.resize(zs.size());
     for (size_t k = 0; k < zs.size(); ++k) {
         uint64_t v = zs[k] ^ z0;
-        uint32_t c = 0;
+        uint64_t c = 0;
         // basis kept in order of insertion; reduce by descending pivot
         std::vector<size_t> ord(sp.basis.size());
         for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
@@ -267,7 +268,7 @@ Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
             const int piv = 63 - __builtin_clzll(bv);
             if ((v >> piv) & 1ull) {
                 v ^= bv;
-                c |= 1u << i;
+                c |= 1ull << i;
             }
         }
         if (v != 0) {
@@ -275,7 +276,7 @@ Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
                 sp.overflow = true;
                 return sp;
             }
-            c |= 1u << sp.basis.size();
+            c |= 1ull << sp.basis.size();
             sp.basis.push_back(v);
         }
         sp.coord[k] = c;
@@ -377,7 +378,36 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
             }
             parts[pi].push_back(k);
         }
+        // c64c: split further until every sub-group has rank <= 2 (terms whose
+        // z differences agree beyond the first two basis vectors)
+        std::vector<std::vector<size_t>> pieces;
         for (const auto &part : parts) {
+            if (!f32) {
+                pieces.push_back(part);
+                continue;
+            }
+            std::vector<uint64_t> zs;
+            for (size_t k : part) zs.push_back(op->mz[k]);
+            Span full = gf2_span(zs, 64);
+            if (full.basis.size() <= 2) {
+                pieces.push_back(part);
+                continue;
+            }
+            std::vector<uint64_t> hk;
+            std::vector<std::vector<size_t>> hp;
+            for (size_t kk = 0; kk < part.size(); ++kk) {
+                const uint64_t key = full.coord[kk] >> 2;
+                size_t pi = 0;
+                while (pi < hk.size() && hk[pi] != key) ++pi;
+                if (pi == hk.size()) {
+                    hk.push_back(key);
+                    hp.emplace_back();
+                }
+                hp[pi].push_back(part[kk]);
+            }
+            for (auto &h : hp) pieces.push_back(std::move(h));
+        }
+        for (const auto &part : pieces) {
             std::vector<uint64_t> zs;
             for (size_t k : part) zs.push_back(op->mz[k]);
             Span sp = gf2_span(zs, kDMax);
@@ -394,7 +424,7 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
                     cd acc{0.0, 0.0};
                     for (size_t kk = 0; kk < part.size(); ++kk) {
                         const cd v = c[part[kk]];
-                        if (__builtin_popcount(u & sp.coord[kk]) & 1) {
+                        if (__builtin_popcountll(u & sp.coord[kk]) & 1) {
                             acc.re -= v.re;
                             acc.im -= v.im;
                         } else {
@@ -419,9 +449,13 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     // order: partner tile ascending, then (c64c) run key zm with fat last
     std::vector<size_t> ord(subs.size());
     for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+    auto runkey = [&](const SubGroup &g) -> uint32_t {
+        if (g.d == kFat || g.d > 2) return 0xffffffffu;
+        return (g.zm & 15u) | (((g.lo >> pl.tb) != 0 ? 1u : 0u) << 4);
+    };
     std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
         if (subs[a].hi != subs[b].hi) return subs[a].hi < subs[b].hi;
-        return f32 && subs[a].zm < subs[b].zm;
+        return f32 && runkey(subs[a]) < runkey(subs[b]);
     });
     std::vector<uint64_t> bhi;
     std::vector<uint32_t> bg0;
@@ -498,6 +532,53 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         }
     }
     if (f32) {
+        // per-tile-table kernel arrays
+        std::vector<uint2> td;
+        std::vector<TileDataC64> tdd;
+        std::vector<uint32_t> r0v, rg0, rkey;
+        const uint64_t tmask_t = (uint64_t)pl.threads - 1;
+        for (size_t i = 0; i < ord.size(); ++i) {
+            const SubGroup &sg = subs[ord[i]];
+            const uint64_t b0 = sg.d > 0 && sg.d != kFat ? sg.beta[0] : 0;
+            const uint64_t b1 = sg.d > 1 && sg.d != kFat ? sg.beta[1] : 0;
+            const uint32_t zt = (uint32_t)(sg.z0 & tmask_t), bt0 = (uint32_t)(b0 & tmask_t),
+                           bt1 = (uint32_t)(b1 & tmask_t);
+            const uint32_t tvar = (zt | bt0 | bt1) != 0 ? 1u : 0u;
+            const uint32_t key = runkey(sg) & 31u;
+            td.push_back(make_uint2(sg.lo | (key << 16) | (tvar << 24),
+                                    zt | (bt0 << 8) | (bt1 << 16)));
+            TileDataC64 d;
+            memset(&d, 0, sizeof(d));
+            d.z0h = sg.z0 >> pl.b;
+            d.b0h = b0 >> pl.b;
+            d.b1h = b1 >> pl.b;
+            for (size_t u = 0; u < sg.table.size() && u < 4; ++u)
+                d.T[u] = make_float2((float)sg.table[u].re, (float)sg.table[u].im);
+            tdd.push_back(d);
+        }
+        for (uint32_t j = 0; j < pl.nblocks; ++j) {
+            r0v.push_back((uint32_t)rkey.size());
+            for (uint32_t g = bg0[j]; g < bg0[j + 1]; ++g) {
+                const uint32_t k = runkey(subs[ord[g]]) & 31u;
+                if (g == bg0[j] || k != rkey.back()) {
+                    rkey.push_back(k);
+                    rg0.push_back(g);
+                }
+            }
+        }
+        r0v.push_back((uint32_t)rkey.size());
+        rg0.push_back((uint32_t)ord.size());
+        if (td.empty()) {
+            td.push_back(make_uint2(0, 0));
+            TileDataC64 z;
+            memset(&z, 0, sizeof(z));
+            tdd.push_back(z);
+        }
+        QR_CUDA(pl.tdesc.upload(td), "upload thread descriptors");
+        QR_CUDA(pl.tdata.upload(tdd), "upload tile data");
+        QR_CUDA(pl.blk_r0.upload(r0v), "upload block runs");
+        QR_CUDA(pl.run_g0.upload(rg0), "upload runs");
+        QR_CUDA(pl.run_key.upload(rkey), "upload run keys");
         pl.nsub = (uint32_t)ord.size();
         if (sd.empty()) {
             SubDescC64 z;
@@ -786,6 +867,11 @@ int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates
     a.err = op->d_err.as<int>();
     a.sub = pl.sub.as<SubDescC64>();
     a.nsub = pl.nsub;
+    a.tdesc = pl.tdesc.as<uint2>();
+    a.tdata = pl.tdata.as<TileDataC64>();
+    a.blk_r0 = pl.blk_r0.as<uint32_t>();
+    a.run_g0 = pl.run_g0.as<uint32_t>();
+    a.run_key = pl.run_key.as<uint32_t>();
     if (pl.nblocks == 0) {
         // operator without terms reachable here cannot happen (T >= 1); keep y defined
         QR_CUDA(cudaMemsetAsync(y, 0, bytes, static_cast<cudaStream_t>(stream)), "zero y");
@@ -884,6 +970,11 @@ int qr_op_set_coeffs(qr_op *op, const double *coeff) {
             pl.blk_g0.release();
             pl.diag.release();
             pl.sub.release();
+            pl.tdesc.release();
+            pl.tdata.release();
+            pl.blk_r0.release();
+            pl.run_g0.release();
+            pl.run_key.release();
         }
     return QR_OK;
 }
