@@ -338,10 +338,13 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 // consumes it, and counts itself out on a shared counter; the last warp out
 // refills the stage with the tile kC64Stages steps ahead.  No CTA-wide
 // barrier sits on the steady-state path.
-constexpr int kTb = 8;          // log2(threads) whenever AMPS >= 2
+#ifndef QR_C64_TB
+#define QR_C64_TB 8
+#endif
+constexpr int kTb = QR_C64_TB;  // log2(threads) whenever AMPS >= 2
 constexpr int kMsh = kTb + 3;   // byte shift of the register index m
 constexpr int kFlush = 8;       // partner tiles per compensated fold
-constexpr int kC64Threads = 256;
+constexpr int kC64Threads = 1 << kTb;
 constexpr int kC64Stages = 6;
 
 template <bool WIDE>
@@ -652,9 +655,9 @@ __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
         const uint2 d = tdesc[g];
         uint32_t u = 0, sg = 0;
         if (d.x >> 24) {
-            sg = (uint32_t)__popc(t & (d.y & 0xffu)) & 1u;
-            u = ((uint32_t)__popc(t & ((d.y >> 8) & 0xffu)) & 1u) |
-                (((uint32_t)__popc(t & ((d.y >> 16) & 0xffu)) & 1u) << 1);
+            sg = (uint32_t)__popc(t & (d.y & 0x3ffu)) & 1u;
+            u = ((uint32_t)__popc(t & ((d.y >> 10) & 0x3ffu)) & 1u) |
+                (((uint32_t)__popc(t & ((d.y >> 20) & 0x3ffu)) & 1u) << 1);
         }
         float4 T = s_tab[g * 4 + u];
         if (sg) {

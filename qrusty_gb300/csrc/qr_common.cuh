@@ -73,7 +73,7 @@ struct ApplyArgs {
     const SubDescC64 *sub;
     uint32_t nsub;
     // per-tile-table kernel: per sub-group an 8-byte thread descriptor
-    // {lo | key << 16 | tvar << 24, z0_t | beta0_t << 8 | beta1_t << 16} and
+    // {lo | key << 16 | tvar << 24, z0_t | beta0_t << 10 | beta1_t << 20} and
     // its TileDataC64; sub-groups of a block in runs of equal key
     const uint2 *tdesc;
     const TileDataC64 *tdata;

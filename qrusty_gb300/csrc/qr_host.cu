@@ -314,7 +314,10 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     const int n = op->n;
     const bool f32 = dtype == QR_C64C;
     pl.b = tile_bits < 0 ? std::min(n, 12) : std::min(n, tile_bits);
-    const int tmax = f32 ? 256 : 256;
+#ifndef QR_C64_TB
+#define QR_C64_TB 8
+#endif
+    const int tmax = f32 ? (1 << QR_C64_TB) : 256;
     pl.threads = std::min(1 << pl.b, tmax);
     pl.amps = (1 << pl.b) / pl.threads;
     pl.tb = 0;
@@ -546,7 +549,7 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
             const uint32_t tvar = (zt | bt0 | bt1) != 0 ? 1u : 0u;
             const uint32_t key = runkey(sg) & 31u;
             td.push_back(make_uint2(sg.lo | (key << 16) | (tvar << 24),
-                                    zt | (bt0 << 8) | (bt1 << 16)));
+                                    zt | (bt0 << 10) | (bt1 << 20)));
             TileDataC64 d;
             memset(&d, 0, sizeof(d));
             d.z0h = sg.z0 >> pl.b;
