@@ -19,6 +19,18 @@ Arms:
 
 Multi-GPU (torchrun, N > 1): replicas -- every rank applies the operator to
 its own state (weak scaling, no data-path collective); max time over ranks.
+
+Secondary workloads (--workload, one JSON line each, 1 GPU):
+  chain   the 22-qubit TFIM+XXZ chain (85 terms), same metric.
+  batch   256 uneven operators (n 10-20, 50-5,000 terms) x 8 complex64 states
+          in ONE graph-replayed persistent launch, against one complex128
+          launch per operator.  term*amp/s summed over operators and states.
+  grad    y = H(c) psi, L = Re<y, w>, backward to c (2,000 terms) and psi
+          (n = 20, complex64): one training step per step.
+  vec     the eigensolver-loop helpers (axpby, axpy, ax, precond2) over 2^26
+          complex128 / complex64 elements: GB/s against the HBM peak.
+  csr     device CSR build (indptr, indices, data) of the chain at n = 22:
+          bytes written per second, and the oracle's CPU build beside it.
 """
 from __future__ import annotations
 
@@ -355,6 +367,221 @@ def run_gpu_arm(args, t, desc):
         dist.destroy_process_group()
 
 
+# ----------------------------------------------------------------------------- secondary
+def _events_time(fn, steps, warmup, stream):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def _base_line(args, metric, value, unit, ms, dtype, config, **kw):
+    out = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+           "config": config}
+    out.update(kw)
+    return out
+
+
+def run_batch(args):
+    import torch
+    from qrusty_gb300 import Batch, PauliOperator, _lib
+    from qrusty_gb300 import workloads as W
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    terms = W.cfg3()
+    ns = 8
+    t0 = time.perf_counter()
+    ops = [PauliOperator(t.n, t.x, t.z, t.phase, t.coeff) for t in terms]
+    t_create = time.perf_counter() - t0
+    g = torch.Generator(device=dev).manual_seed(7)
+    psis, ys, psis128, ys128 = [], [], [], []
+    for t in terms:
+        p = torch.complex(torch.randn(ns << t.n, device=dev, generator=g),
+                          torch.randn(ns << t.n, device=dev, generator=g))
+        psis.append(p)
+        ys.append(torch.empty_like(p))
+        psis128.append(p.to(torch.complex128))
+        ys128.append(torch.empty_like(psis128[-1]))
+    units = sum(t.T * (ns << t.n) for t in terms)
+    alg = sum((W.alg_blocks(t, 13) + 1) * (ns << t.n) * 8 for t in terms)
+    t0 = time.perf_counter()
+    b = Batch(ops, [ns] * len(ops))
+    b.apply(psis, ys)  # autotune + graph capture
+    torch.cuda.synchronize()
+    t_tune = time.perf_counter() - t0
+    l0 = _lib.launch_count()
+    ms_b = _events_time(lambda: b.apply(psis, ys), args.steps, args.warmup, stream)
+    launches = (_lib.launch_count() - l0) / (args.steps + args.warmup)
+
+    def per_op(ps, outs):
+        for op, p, y in zip(ops, ps, outs):
+            op.apply(p, out=y)
+    s2 = max(3, args.steps // 5)
+    ms_128 = _events_time(lambda: per_op(psis128, ys128), s2, 3, stream)
+    ms_64 = _events_time(lambda: per_op(psis, ys), s2, 3, stream)
+    # accuracy: batched c64c against per-operator c128 on the same states
+    b.apply(psis, ys)
+    per_op(psis128, ys128)
+    torch.cuda.synchronize()
+    worst = max(float(torch.linalg.vector_norm(y.to(torch.complex128) - r)
+                      / torch.linalg.vector_norm(r)) for y, r in zip(ys, ys128))
+    hbm, peak_kind = peaks()
+    ach = alg / (ms_b / 1e3) / 1e9
+    out = _base_line(
+        args, "batched Pauli-sum H·ψ term·amp/s (sum over operators and states)",
+        units / (ms_b / 1e3), UNIT, ms_b, "c64c (fp32 + two-sum)",
+        {"workload": "256 operators, n ~ U{10..20}, T ~ U{50..5000} random letters (seed %d), "
+                     "8 complex64 states each" % (W.SEED0 + 3),
+         "operators": len(terms), "states_per_op": ns,
+         "amplitudes_total": int(sum(ns << t.n for t in terms)),
+         "tile_bits_autotuned": b.tile_bits,
+         "l2": "total state %d MiB; no flush" % (sum((ns << t.n) * 8 for t in terms) >> 20)},
+        roofline={"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                  "frac": ach / hbm, "traffic": None, "alg_bytes_per_launch": alg,
+                  "alg_bytes_rule": "sum over ops of (P+1)*states*2^n*8", "peak_source": peak_kind},
+        per_op_c128={"ms_per_step": ms_128, "launches_per_step": len(ops),
+                     "value": units / (ms_128 / 1e3)},
+        per_op_c64c={"ms_per_step": ms_64, "value": units / (ms_64 / 1e3)},
+        speedup_vs_per_op_c128=ms_128 / ms_b,
+        rel_err={"batched_c64c_vs_c128_worst_op": worst},
+        setup_s={"create_ops": t_create, "autotune_and_capture": t_tune},
+        gpu_launches=launches)
+    print(json.dumps(out), flush=True)
+
+
+def run_grad(args):
+    import torch
+    from qrusty_gb300 import workloads as W
+    from qrusty_gb300.autograd import PauliTerms, pauli_apply
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    t, psi, w = W.cfg4()
+    terms = PauliTerms(t.n, t.x, t.z, t.phase)
+    c = torch.tensor(t.coeff.real, dtype=torch.float64, requires_grad=True)
+    p = torch.from_numpy(psi.astype(np.complex64)).to(dev).requires_grad_(True)
+    wd = torch.from_numpy(w.astype(np.complex64)).to(dev)
+
+    def step():
+        c.grad = None
+        p.grad = None
+        y = pauli_apply(c, p, terms)
+        torch.vdot(y, wd).real.backward()
+        with torch.no_grad():
+            c.add_(c.grad, alpha=-1e-3)  # an SGD update: the next step sees new coefficients
+
+    ms = _events_time(step, args.steps, args.warmup, stream)
+    N = 1 << t.n
+    out = _base_line(
+        args, "differentiable H(c)·ψ training step term·amp/s (forward terms x amplitudes / step)",
+        t.T * N / (ms / 1e3), UNIT, ms, "c64c forward / adjoint, fp64 reductions",
+        {"workload": "n=%d, %d random-letter terms, real c, complex64 psi, L = Re<H(c)psi, w> "
+                     "(seed %d)" % (t.n, t.T, W.SEED0 + 4),
+         "step": "forward + backward (grad_c, grad_psi) + SGD update of c",
+         "l2": "state 8 MiB: L2-resident"})
+    print(json.dumps(out), flush=True)
+
+
+def run_vec(args):
+    import ctypes as C
+    import torch
+    from qrusty_gb300 import _lib
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    st = stream.cuda_stream
+    L = _lib.load()
+    N = 1 << args.n
+    hbm, peak_kind = peaks()
+    res = {}
+    a = (C.c_double * 2)(0.5, -1.25)
+    b = (C.c_double * 2)(-0.75, 0.5)
+    for name, dt, tdt, esz in (("c128", _lib.QR_C128, torch.complex128, 16),
+                               ("c64", _lib.QR_C64C, torch.complex64, 8)):
+        x = torch.randn(N, dtype=tdt, device=dev)
+        y = torch.randn(N, dtype=tdt, device=dev)
+        z = torch.empty_like(x)
+        fns = {
+            "axpby": (lambda: L.qr_axpby(dt, N, a, x.data_ptr(), b, y.data_ptr(), z.data_ptr(), st),
+                      3),
+            "axpy": (lambda: L.qr_axpy(dt, N, a, x.data_ptr(), y.data_ptr(), z.data_ptr(), st), 3),
+            "ax": (lambda: L.qr_ax(dt, N, a, x.data_ptr(), z.data_ptr(), st), 2),
+            "precond2": (lambda: L.qr_precond2(dt, N, x.data_ptr(), y.data_ptr(), a, 1e-12,
+                                               z.data_ptr(), st), 3),
+        }
+        for op, (fn, passes) in fns.items():
+            ms = _events_time(fn, args.steps, args.warmup, stream)
+            gbs = passes * N * esz / (ms / 1e3) / 1e9
+            res["%s_%s" % (op, name)] = {"ms": ms, "GB/s": gbs, "frac": gbs / hbm}
+        del x, y, z
+    head = res["axpby_c128"]
+    out = _base_line(
+        args, "axpby z = a x + b y GB/s (HBM-bound vector helper)", head["GB/s"], "GB/s",
+        head["ms"], "c128",
+        {"workload": "axpby / axpy / ax / precond2 over 2^%d elements" % args.n,
+         "l2": "inputs %d MiB > L2; no flush" % ((N * 16) >> 20)},
+        roofline={"bound": "hbm", "achieved": head["GB/s"], "peak": hbm, "unit": "GB/s",
+                  "frac": head["GB/s"] / hbm, "traffic": None,
+                  "alg_bytes_per_launch": 48 * N, "alg_bytes_rule": "read x, y + write z",
+                  "peak_source": peak_kind},
+        all=res)
+    print(json.dumps(out), flush=True)
+
+
+def run_csr(args):
+    import torch
+    from qrusty_gb300 import PauliOperator
+    from qrusty_gb300 import workloads as W
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    n = args.n if args.n != 26 else 22
+    t, _ = W.cfg1(with_state=False, n=n)
+    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
+    nr, nz = op.csr_size()
+    indptr = torch.empty(nr + 1, dtype=torch.int64, device=dev)
+    indices = torch.empty(nz, dtype=torch.int64, device=dev)
+    data = torch.empty(nz, dtype=torch.complex128, device=dev)
+    from qrusty_gb300 import _lib
+    L = _lib.load()
+    st = stream.cuda_stream
+    fn = lambda: _lib.check(L.qr_csr_build(op.handle, indptr.data_ptr(), indices.data_ptr(),
+                                           data.data_ptr(), _lib.QR_MEM_DEVICE, st))
+    ms = _events_time(fn, args.steps, args.warmup, stream)
+    op.sync_check()
+    written = 8 * (nr + 1) + 24 * nz
+    hbm, peak_kind = peaks()
+    gbs = written / (ms / 1e3) / 1e9
+    out = _base_line(
+        args, "rowwise CSR build nnz/s (indptr, indices, data on the device)",
+        nz / (ms / 1e3), "nnz/s", ms, "u64 indices, c128 data",
+        {"workload": "tfim+xxz open chain n=%d, %d terms, G=%d (seed %d)"
+                     % (n, t.T, nz // nr, W.SEED0 + 1),
+         "nnz": int(nz), "bytes_written": int(written)},
+        roofline={"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                  "frac": gbs / hbm, "traffic": None, "alg_bytes_per_launch": written,
+                  "alg_bytes_rule": "8(N+1) + 24 nnz written", "peak_source": peak_kind})
+    if not args.no_cpu:
+        from oracle import oracle as O
+        O.build()
+        rows = min(nr, args.cpu_rows * 4)
+        cp = O.make_params(t.phase, t.coeff)
+        nth = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        O.csr_build(t.n, t.x, t.z, cp, step=1024, nthreads=nth, rows=(0, rows))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": rows * (nz // nr) / dt, "unit": "nnz/s", "cores": nth,
+                               "kind": "port",
+                               "sample": "rows [0, %d) of 2^%d, make_row chunks of 1024" % (rows, n)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__,
                                  formatter_class=argparse.RawDescriptionHelpFormatter)
@@ -362,7 +589,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["jw", "chain"], default="jw")
+    ap.add_argument("--workload", choices=["jw", "chain", "batch", "grad", "vec", "csr"],
+                    default="jw")
     ap.add_argument("--n", type=int, default=26)
     ap.add_argument("--pairs", type=int, default=8000)
     ap.add_argument("--zterms", type=int, default=2000)
@@ -374,6 +602,11 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and not args.quick:
         raise SystemExit("--warmup must be >= 3")
+    if args.workload in ("batch", "grad", "vec", "csr"):
+        if args.impl == "reference":
+            raise SystemExit("--impl reference measures the headline workloads (jw, chain)")
+        {"batch": run_batch, "grad": run_grad, "vec": run_vec, "csr": run_csr}[args.workload](args)
+        return
     if args.workload == "chain" and args.n == 26:
         args.n = 22
     t, desc = make_terms(args)

@@ -196,6 +196,40 @@ int qr_batch_apply(qr_batch *b, const void *const *psi, void *const *y, void *st
 /* Tile width the autotuner chose (log2 amplitudes; 0 before the first apply). */
 int qr_batch_tile_bits(const qr_batch *b);
 
+/* Vector helpers of the eigensolver loop, element-wise over len complex
+ * elements of device memory (dtype QR_C128: complex128, arithmetic
+ * bit-identical to num-complex's; QR_C64C: complex64, the same sequence in
+ * FP32 with the scalars rounded to float).  Scalars a, b, e are host
+ * pointers to (re, im) doubles.  z / out may be the same buffer as an input.
+ *
+ * qr_axpby: z = a x + b y      -- qrusty/src/accel.rs:374-379 (axpby),
+ *                                  pyqrusty/src/lib.rs:523-535
+ * qr_axpy:  z = a x + y        -- qrusty/src/accel.rs:381-386 (axpy)
+ * qr_ax:    z = a x            -- qrusty/src/accel.rs:388-393 (ax)
+ * qr_precond2: out = dx / reg(diag - e, tol), where reg(v) = tol + 0i when
+ *           |v| < tol (|v| = hypot) and v otherwise -- pyqrusty/src/lib.rs:
+ *           457-469 (precond2), :580-592 (binding) and :436-440 (reg). */
+int qr_axpby(int32_t dtype, uint64_t len, const double *a, const void *x, const double *b,
+             const void *y, void *z, void *stream);
+int qr_axpy(int32_t dtype, uint64_t len, const double *a, const void *x, const void *y, void *z,
+            void *stream);
+int qr_ax(int32_t dtype, uint64_t len, const double *a, const void *x, void *z, void *stream);
+int qr_precond2(int32_t dtype, uint64_t len, const void *diag, const void *dx, const double *e,
+                double tol, void *out, void *stream);
+
+/* Diagonal of a device CSR matrix (complex128 data): out[r] = the stored
+ * entry of row r at column r, 0 if none, for r < min(nrows, ncols) --
+ * SpMat.diagonal(), pyqrusty/src/lib.rs:118-125 (sprs diag().to_dense());
+ * with it, qr_precond2 is pyqrusty's precond (pyqrusty/src/lib.rs:442-455). */
+int qr_csr_diagonal(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
+                    const uint64_t *indices, const double *data, double *out, void *stream);
+
+/* Diagonal of H without building the CSR: out[r] = the terms with x = 0
+ * folded in input order as make_row folds them (qrusty/src/accel.rs:
+ * 171-210), so for QR_C128 it equals the diagonal of qr_csr_build's matrix
+ * bit for bit; QR_C64C rounds that FP64 value to complex64.  2^n elements. */
+int qr_op_diagonal(qr_op *op, int32_t dtype, void *out, void *stream);
+
 /* Message of the calling thread's last failure ("" if none).  Copies at
  * most len-1 bytes plus a terminating NUL; returns the full length. */
 int qr_last_error(char *buf, size_t len);

@@ -35,7 +35,7 @@ def build(force: bool = False) -> str:
         return _LIB
     tmp = _LIB + ".tmp%d" % os.getpid()
     cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-pthread",
-           "-ffp-contract=off", "-o", tmp, _SRC]
+           "-ffp-contract=off", "-o", tmp, _SRC, "-lm"]
     subprocess.check_call(cmd)
     os.replace(tmp, _LIB)
     return _LIB
@@ -76,6 +76,12 @@ def lib():
         L.or_term_grad.argtypes = [C.c_size_t, C.c_int, _u64p, _u64p, _u8p, _f64p, _f64p, _f64p,
                                    C.c_int]
         L.or_term_grad.restype = None
+        L.or_vec.argtypes = [C.c_int, C.c_int, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p,
+                             _f64p, C.c_void_p, C.c_double]
+        L.or_vec.restype = None
+        L.or_op_diagonal.argtypes = [C.c_size_t, _u64p, _u64p, _f64p, C.c_uint64, C.c_uint64,
+                                     _f64p]
+        L.or_op_diagonal.restype = None
         _lib = L
     return _lib
 
@@ -184,4 +190,33 @@ def term_grad(n, x, z, phase, psi, g, nthreads=None):
     gg = np.ascontiguousarray(g, dtype=np.complex128).view(np.float64)
     out = np.empty(2 * len(x), dtype=np.float64)
     lib().or_term_grad(len(x), n, z, x, ph, p, gg, out, nthreads or default_threads())
+    return out.view(np.complex128)
+
+
+_VEC_OPS = {"axpby": 0, "axpy": 1, "ax": 2, "precond2": 3}
+
+
+def vec(op, x, y=None, a=0j, b=0j, tol=0.0):
+    """Element-wise helper ``op`` (axpby / axpy / ax / precond2) on complex128
+    or complex64 arrays; precond2 takes x = diag, y = dx, a = e."""
+    x = np.ascontiguousarray(x)
+    if x.dtype not in (np.complex128, np.complex64):
+        raise TypeError("complex128 or complex64 arrays")
+    f32 = x.dtype == np.complex64
+    yv = None if y is None else np.ascontiguousarray(y, dtype=x.dtype)
+    z = np.empty_like(x)
+    av = np.array([complex(a).real, complex(a).imag])
+    bv = np.array([complex(b).real, complex(b).imag])
+    lib().or_vec(_VEC_OPS[op], int(f32), x.size, x.ctypes.data,
+                 None if yv is None else yv.ctypes.data, z.ctypes.data, av,
+                 bv.ctypes.data if op == "axpby" else None, float(tol))
+    return z
+
+
+def op_diagonal(x, z, cprime, row0, nrows):
+    out = np.empty(2 * nrows)
+    lib().or_op_diagonal(len(x), np.ascontiguousarray(z, dtype=np.uint64),
+                         np.ascontiguousarray(x, dtype=np.uint64),
+                         np.ascontiguousarray(cprime, dtype=np.complex128).view(np.float64),
+                         int(row0), int(nrows), out)
     return out.view(np.complex128)

@@ -405,3 +405,76 @@ void or_term_grad(size_t T, int n, const uint64_t *z, const uint64_t *x, const u
     atomic_init(&c.next, 0);
     run_pool(nthreads, tg_worker, &c);
 }
+
+/* ------------------------------------------------------------------ */
+/* Vector helpers of the eigensolver loop, element-wise:               */
+/*   op 0 axpby z = a x + b y   qrusty/src/accel.rs:374-379            */
+/*   op 1 axpy  z = a x + y     qrusty/src/accel.rs:381-386            */
+/*   op 2 ax    z = a x         qrusty/src/accel.rs:388-393            */
+/*   op 3 precond2 z = y / reg(x - a, tol)  pyqrusty/src/lib.rs:457-469 */
+/*        reg(v) = tol + 0i if |v| < tol else v  (:436-440), |v| = hypot */
+/* num-complex 0.4 arithmetic: a*b as c_mul, a/b = ((ar br + ai bi)/n,  */
+/* (ai br - ar bi)/n) with n = br^2 + bi^2.  f32 = 1: the same sequence */
+/* in float with the scalars rounded to float (complex64 data).         */
+/* ------------------------------------------------------------------ */
+#include <math.h>
+
+#define OR_VEC_BODY(R, HYPOT)                                                     \
+    do {                                                                          \
+        const R *X = (const R *)x, *Y = (const R *)y;                             \
+        R *Z = (R *)z;                                                            \
+        const R ar = (R)a[0], ai = (R)a[1];                                       \
+        const R br = b ? (R)b[0] : (R)0, bi = b ? (R)b[1] : (R)0, tl = (R)tol;    \
+        for (size_t i = 0; i < len; ++i) {                                        \
+            const R xr = X[2 * i], xi = X[2 * i + 1];                             \
+            const R yr = op != 2 ? Y[2 * i] : (R)0, yi = op != 2 ? Y[2 * i + 1] : (R)0; \
+            R zr, zi;                                                             \
+            if (op == 3) {                                                        \
+                R dr = xr - ar, di = xi - ai;                                     \
+                if (HYPOT(dr, di) < tl) { dr = tl; di = (R)0; }                   \
+                const R ns = dr * dr + di * di;                                   \
+                zr = (yr * dr + yi * di) / ns;                                    \
+                zi = (yi * dr - yr * di) / ns;                                    \
+            } else {                                                              \
+                const R ur = ar * xr - ai * xi, ui = ar * xi + ai * xr;           \
+                if (op == 2) { zr = ur; zi = ui; }                                \
+                else if (op == 1) { zr = ur + yr; zi = ui + yi; }                 \
+                else {                                                            \
+                    const R vr = br * yr - bi * yi, vi = br * yi + bi * yr;       \
+                    zr = ur + vr; zi = ui + vi;                                   \
+                }                                                                 \
+            }                                                                     \
+            Z[2 * i] = zr; Z[2 * i + 1] = zi;                                     \
+        }                                                                         \
+    } while (0)
+
+void or_vec(int op, int f32, size_t len, const void *x, const void *y, void *z,
+            const double *a, const double *b, double tol)
+{
+    if (f32) OR_VEC_BODY(float, hypotf);
+    else OR_VEC_BODY(double, hypot);
+}
+
+/* Diagonal of the operator's matrix, rows [row0, row0 + nrows): the value */
+/* make_row (qrusty/src/accel.rs:171-210) places at column r of row r --    */
+/* the terms with x = 0 in input order, left-folded from the first; 0 when  */
+/* no term has x = 0 (the row then stores no diagonal entry).               */
+void or_op_diagonal(size_t T, const uint64_t *z, const uint64_t *x, const double *cprime,
+                    uint64_t row0, uint64_t nrows, double *out)
+{
+    const cplx *cp = (const cplx *)cprime;
+    for (uint64_t i = 0; i < nrows; ++i) {
+        const uint64_t r = row0 + i;
+        cplx v = {0.0, 0.0};
+        int first = 1;
+        for (size_t k = 0; k < T; ++k) {
+            if (x[k] != 0) continue;
+            cplx t = cp[k];
+            if (__builtin_popcountll(r & z[k]) & 1) t = c_neg(t);
+            if (first) { v = t; first = 0; }
+            else v = c_add(v, t);
+        }
+        out[2 * i] = v.re;
+        out[2 * i + 1] = v.im;
+    }
+}

@@ -4,8 +4,9 @@
 package for this path (Pauli, SparsePauliOp, SpMat, spmat_dot_densevec,
 csr_matrix), backed by libqrusty_gpu.so (C ABI: include/qrusty_gpu.h).
 """
-from .pyqrusty import (Batch, Pauli, PauliOperator, QrError, SparsePauliOp, SpMat, csr_matrix,
-                       parse_mode, spmat_dot_densevec, vdot)
+from .pyqrusty import (Batch, Pauli, PauliOperator, QrError, SparsePauliOp, SpMat, ax, axpby,
+                       axpy, csr_matrix, parse_mode, precond, precond2, spmat_dot_densevec, vdot)
 
 __all__ = ["Pauli", "SparsePauliOp", "SpMat", "spmat_dot_densevec", "csr_matrix",
-           "PauliOperator", "QrError", "parse_mode", "vdot", "Batch"]
+           "PauliOperator", "QrError", "parse_mode", "vdot", "Batch", "axpby", "axpy", "ax",
+           "precond", "precond2"]

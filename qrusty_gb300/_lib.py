@@ -28,7 +28,8 @@ EXPORTS = (
     "qr_op_create", "qr_op_destroy", "qr_op_get_info", "qr_csr_size", "qr_csr_build",
     "qr_apply", "qr_check", "qr_apply_host", "qr_csr_spmv", "qr_op_set_coeffs", "qr_vdot",
     "qr_expect", "qr_term_grad", "qr_vdot_noalloc", "qr_batch_create", "qr_batch_destroy",
-    "qr_batch_apply", "qr_batch_tile_bits", "qr_last_error", "qr_launch_count",
+    "qr_batch_apply", "qr_batch_tile_bits", "qr_axpby", "qr_axpy", "qr_ax", "qr_precond2",
+    "qr_csr_diagonal", "qr_op_diagonal", "qr_last_error", "qr_launch_count",
 )
 
 
@@ -84,6 +85,12 @@ def load(build_if_missing: bool = True):
     L.qr_batch_apply.argtypes = [vp, vp, vp, vp]
     L.qr_batch_tile_bits.argtypes = [vp]
     L.qr_term_grad.argtypes = [vp, i32, vp, vp, i32, vp, vp]
+    L.qr_axpby.argtypes = [i32, u64, vp, vp, vp, vp, vp, vp]
+    L.qr_axpy.argtypes = [i32, u64, vp, vp, vp, vp, vp]
+    L.qr_ax.argtypes = [i32, u64, vp, vp, vp, vp]
+    L.qr_precond2.argtypes = [i32, u64, vp, vp, vp, C.c_double, vp, vp]
+    L.qr_csr_diagonal.argtypes = [u64, u64, vp, vp, vp, vp, vp]
+    L.qr_op_diagonal.argtypes = [vp, i32, vp, vp]
     L.qr_last_error.argtypes = [C.c_char_p, C.c_size_t]
     for name in EXPORTS:
         getattr(L, name).restype = C.c_int

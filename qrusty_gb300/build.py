@@ -18,7 +18,7 @@ OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libqrusty_gpu.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
-SOURCES = ["qr_host.cu", "qr_apply.cu", "qr_csr.cu", "qr_reduce.cu"]
+SOURCES = ["qr_host.cu", "qr_apply.cu", "qr_csr.cu", "qr_reduce.cu", "qr_vec.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
          "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", INCLUDE]

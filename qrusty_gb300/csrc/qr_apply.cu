@@ -338,14 +338,18 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 // consumes it, and counts itself out on a shared counter; the last warp out
 // refills the stage with the tile kC64Stages steps ahead.  No CTA-wide
 // barrier sits on the steady-state path.
-#ifndef QR_C64_TB
-#define QR_C64_TB 8
-#endif
-constexpr int kTb = QR_C64_TB;  // log2(threads) whenever AMPS >= 2
-constexpr int kMsh = kTb + 3;   // byte shift of the register index m
-constexpr int kFlush = 8;       // partner tiles per compensated fold
+// Single-operator kernels run 512 threads x 8 amplitudes per 4096-amplitude
+// tile (16 warps per SM hide more latency than 8 warps x 16 amplitudes,
+// and fewer register bits leave fewer sign patterns to split on); the
+// batched kernel keeps 256 x 16, its register budget at 512 threads spills.
+constexpr int kTb = kC64ThreadBits;       // log2(threads) whenever AMPS >= 2
+constexpr int kMsh = kTb + 3;             // byte shift of the register index m
+constexpr int kFlush = 8;                 // partner tiles per compensated fold
 constexpr int kC64Threads = 1 << kTb;
 constexpr int kC64Stages = 6;
+constexpr int kBatchTb = kBatchThreadBits;
+constexpr int kBatchMsh = kBatchTb + 3;
+constexpr int kBatchThreads = 1 << kBatchTb;
 
 template <bool WIDE>
 __device__ __forceinline__ uint32_t parity(uint64_t r, uint64_t m) {
@@ -434,7 +438,7 @@ __device__ __forceinline__ void mloop_dispatch(uint32_t zm, float2 (&A)[AMPS], f
 }
 
 // Rank 3-4 (table) or term-by-term ("fat") sub-group through GroupDesc.
-template <int AMPS>
+template <int AMPS, int MSH = kMsh>
 __device__ __forceinline__ void big_group_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                            const unsigned char *sm, uint32_t off,
                                            const GroupDesc &gd, uint64_t r0, int tb,
@@ -459,7 +463,7 @@ __device__ __forceinline__ void big_group_c64(float2 (&A)[AMPS], float2 (&B)[AMP
                 di += ng ? -ck.y : ck.y;
             }
         }
-        const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << kMsh)));
+        const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << MSH)));
         A[m] = __ffma2_rn(make_float2(dr, dr), p, A[m]);
         B[m] = __ffma2_rn(make_float2(di, di), p, B[m]);
     }
@@ -927,7 +931,7 @@ __device__ __forceinline__ void mloop_plain(float2 (&A)[AMPS], float2 (&B)[AMPS]
     float2 p[AMPS];
 #pragma unroll
     for (int m = 0; m < AMPS; ++m) {
-        const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
+        const uint32_t o = XM ? (off ^ ((uint32_t)m << kBatchMsh)) : (off + ((uint32_t)m << kBatchMsh));
         p[m] = *reinterpret_cast<const float2 *>(sm + o);
     }
     const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
@@ -963,7 +967,7 @@ __device__ __forceinline__ void mloop_plain_dispatch(uint32_t key, float2 (&A)[A
 }
 
 template <int AMPS>
-__global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchArgs a) {
+__global__ void __launch_bounds__(kBatchThreads, 1) apply_c64c_batch(const BatchArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr uint32_t kStageBytes = 4096u * 8u;
     const uint32_t threads = blockDim.x;
@@ -1044,7 +1048,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
         for (uint32_t g = o.blk_g0[j]; g < g1; ++g) {
             const SubDescC64 *sd = o.sub + g;
             const uint32_t lo = sd->lo, kind = sd->kind;
-            const uint32_t off = soff | ((t ^ (lo & tmask)) << 3) | ((lo >> o.tb) << kMsh);
+            const uint32_t off = soff | ((t ^ (lo & tmask)) << 3) | ((lo >> o.tb) << kBatchMsh);
             if ((kind >> 8) == 0) {
                 const uint32_t u = parity<false>(r0, sd->beta0) |
                                    (parity<false>(r0, sd->beta1) << 1);
@@ -1058,7 +1062,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
                 }
                 mloop_plain_dispatch<AMPS>(kind & 31u, A, B, smem_raw, off, make_float2(dx, dy));
             } else {
-                big_group_c64<AMPS>(A, B, smem_raw, off, o.groups[g], r0, o.tb, o.tables,
+                big_group_c64<AMPS, kBatchMsh>(A, B, smem_raw, off, o.groups[g], r0, o.tb, o.tables,
                                     o.fat_z, o.fat_c);
             }
         }
@@ -1109,7 +1113,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
 }
 
 cudaError_t launch_batch_c64c(const BatchArgs &a, int nsm, cudaStream_t st) {
-    const size_t smem = (size_t)kC64Stages * 4096u * 8u + (size_t)16 * kC64Threads * 8u +
+    const size_t smem = (size_t)kC64Stages * 4096u * 8u + (size_t)16 * kBatchThreads * 8u +
                         kC64Stages * (sizeof(uint64_t) + 4);
     auto kern = apply_c64c_batch<16>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1117,7 +1121,7 @@ cudaError_t launch_batch_c64c(const BatchArgs &a, int nsm, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     const uint32_t grid = a.nitems < (uint32_t)nsm ? a.nitems : (uint32_t)nsm;
     if (grid == 0) return cudaSuccess;
-    kern<<<grid, kC64Threads, smem, st>>>(a);
+    kern<<<grid, kBatchThreads, smem, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }
@@ -1162,7 +1166,6 @@ cudaError_t launch_apply(int dtype, const ApplyArgs &a, int amps, int threads, i
         case 2: return launch_c64c<2>(a, threads, nsm, st);
         case 4: return launch_c64c<4>(a, threads, nsm, st);
         case 8: return launch_c64c<8>(a, threads, nsm, st);
-        case 16: return launch_c64c<16>(a, threads, nsm, st);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -115,6 +115,11 @@ cudaError_t launch_batch_c64c(const BatchArgs &a, int nsm, cudaStream_t st);
 // Device error codes written to the error word.
 enum : int { kErrNone = 0, kErrMbarTimeout = 1, kErrCsrPos = 2 };
 
+// log2 of the thread count of the compensated-complex64 kernels: the
+// single-operator kernels and the batched kernel (see qr_apply.cu).
+constexpr int kC64ThreadBits = 9;
+constexpr int kBatchThreadBits = 8;
+
 // Records msg as the calling thread's last error (qr_last_error) and returns code.
 int set_error(int code, const char *msg);
 
@@ -146,6 +151,14 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st);
 cudaError_t launch_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
                             const uint64_t *indices, const double *data, const double *v,
                             double *y, int nsm, cudaStream_t st);
+
+// qr_vec.cu (op: 0 axpby, 1 axpy, 2 ax, 3 precond2)
+cudaError_t launch_vec_op(int op, int f32, uint64_t len, const void *x, const void *y, void *z,
+                          const double *a, const double *b, double tol, int nsm, cudaStream_t st);
+cudaError_t launch_csr_diag(uint64_t nd, const uint64_t *indptr, const uint64_t *indices,
+                            const double *data, double *out, int nsm, cudaStream_t st);
+cudaError_t launch_op_diag(uint64_t N, uint32_t nt, const uint64_t *tz, const double *tc, void *out,
+                           int f32, int nsm, cudaStream_t st);
 
 // qr_reduce.cu
 uint32_t vdot_blocks(uint64_t N, int nsm);

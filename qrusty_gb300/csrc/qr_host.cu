@@ -314,10 +314,7 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     const int n = op->n;
     const bool f32 = dtype == QR_C64C;
     pl.b = tile_bits < 0 ? std::min(n, 12) : std::min(n, tile_bits);
-#ifndef QR_C64_TB
-#define QR_C64_TB 8
-#endif
-    const int tmax = f32 ? (1 << QR_C64_TB) : 256;
+    const int tmax = !f32 ? 256 : (1 << (tile_bits < 0 ? kC64ThreadBits : kBatchThreadBits));
     pl.threads = std::min(1 << pl.b, tmax);
     pl.amps = (1 << pl.b) / pl.threads;
     pl.tb = 0;
@@ -919,6 +916,81 @@ int qr_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr, const ui
     QR_CUDA(launch_csr_spmv(nrows, ncols, indptr, indices, data, v, y, nsm,
                             static_cast<cudaStream_t>(stream)),
             "csr spmv launch");
+    return QR_OK;
+}
+
+// ---------------------------------------------------------------- vector helpers
+static int current_nsm(int *nsm) {
+    int dev = 0;
+    QR_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    QR_CUDA(cudaDeviceGetAttribute(nsm, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    return QR_OK;
+}
+
+static int vec_call(const char *name, int op, int32_t dtype, uint64_t len, const void *x,
+                    const void *y, void *z, const double *a, const double *b, double tol,
+                    void *stream) {
+    if (dtype != QR_C128 && dtype != QR_C64C)
+        return fail(QR_EINVAL, "%s: dtype must be QR_C128 or QR_C64C", name);
+    if (len == 0) return QR_OK;
+    if (!x || !z || (op != 2 && !y) || !a) return fail(QR_EINVAL, "%s: null argument", name);
+    int nsm = 0;
+    int rc = current_nsm(&nsm);
+    if (rc) return rc;
+    QR_CUDA(launch_vec_op(op, dtype == QR_C64C, len, x, y, z, a, b, tol, nsm,
+                          static_cast<cudaStream_t>(stream)),
+            name);
+    return QR_OK;
+}
+
+int qr_axpby(int32_t dtype, uint64_t len, const double *a, const void *x, const double *b,
+             const void *y, void *z, void *stream) {
+    if (len && !b) return fail(QR_EINVAL, "qr_axpby: null argument");
+    return vec_call("qr_axpby", 0, dtype, len, x, y, z, a, b, 0.0, stream);
+}
+
+int qr_axpy(int32_t dtype, uint64_t len, const double *a, const void *x, const void *y, void *z,
+            void *stream) {
+    return vec_call("qr_axpy", 1, dtype, len, x, y, z, a, nullptr, 0.0, stream);
+}
+
+int qr_ax(int32_t dtype, uint64_t len, const double *a, const void *x, void *z, void *stream) {
+    return vec_call("qr_ax", 2, dtype, len, x, nullptr, z, a, nullptr, 0.0, stream);
+}
+
+int qr_precond2(int32_t dtype, uint64_t len, const void *diag, const void *dx, const double *e,
+                double tol, void *out, void *stream) {
+    return vec_call("qr_precond2", 3, dtype, len, diag, dx, out, e, nullptr, tol, stream);
+}
+
+int qr_csr_diagonal(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
+                    const uint64_t *indices, const double *data, double *out, void *stream) {
+    const uint64_t nd = nrows < ncols ? nrows : ncols;
+    if (nd == 0) return QR_OK;
+    if (!indptr || !indices || !data || !out)
+        return fail(QR_EINVAL, "qr_csr_diagonal: null argument");
+    int nsm = 0;
+    int rc = current_nsm(&nsm);
+    if (rc) return rc;
+    QR_CUDA(launch_csr_diag(nd, indptr, indices, data, out, nsm,
+                            static_cast<cudaStream_t>(stream)),
+            "csr diagonal launch");
+    return QR_OK;
+}
+
+int qr_op_diagonal(qr_op *op, int32_t dtype, void *out, void *stream) {
+    if (!op || !out) return fail(QR_EINVAL, "qr_op_diagonal: null argument");
+    if (dtype != QR_C128 && dtype != QR_C64C)
+        return fail(QR_EINVAL, "qr_op_diagonal: dtype must be QR_C128 or QR_C64C");
+    int rc = check_device(op);
+    if (rc) return rc;
+    rc = upload_csr_tables(op);
+    if (rc) return rc;
+    // groups are sorted by x ascending, so an x = 0 group is group 0
+    const uint32_t nt = (op->G > 0 && op->gx[0] == 0) ? op->goff[1] - op->goff[0] : 0;
+    QR_CUDA(launch_op_diag(op->N, nt, op->d_tz.as<uint64_t>(), op->d_tc.as<double>(), out,
+                           dtype == QR_C64C, op->nsm, static_cast<cudaStream_t>(stream)),
+            "operator diagonal launch");
     return QR_OK;
 }
 

@@ -13,10 +13,12 @@ with every numeric result computed by the sm_103a kernels behind the C ABI
 * ``SpMat`` (pyqrusty/src/lib.rs:33-214): CSR holder with ``export``
 * ``spmat_dot_densevec`` (pyqrusty/src/lib.rs:476-491): GPU CSR * vector
 * ``csr_matrix`` (pyqrusty/python/pyqrusty/__init__.py:14-17)
+* the eigensolver-loop vector helpers ``axpby`` / ``axpy`` / ``ax``
+  (qrusty/src/accel.rs:374-393), ``precond`` / ``precond2``
+  (pyqrusty/src/lib.rs:436-469) and ``SpMat.diagonal`` (:118-125), on the GPU
 
 Out of scope here (matrix algebra around the path, not the path):
-MatrixMarket I/O, ``+``/``-``/``scale`` on SpMat, ``a_spmat_p_b_spmat``,
-``axpby``/``axpy``/``ax``, ``precond``/``precond2``.
+MatrixMarket I/O, ``+``/``-``/``scale`` on SpMat, ``a_spmat_p_b_spmat``.
 """
 from __future__ import annotations
 
@@ -31,7 +33,8 @@ from . import _lib
 from ._lib import QR_C128, QR_C64C, QR_MEM_HOST, QrError, check
 
 __all__ = ["Pauli", "SparsePauliOp", "SpMat", "PauliOperator", "spmat_dot_densevec",
-           "csr_matrix", "QrError", "parse_mode", "vdot", "Batch"]
+           "csr_matrix", "QrError", "parse_mode", "vdot", "Batch", "axpby", "axpy", "ax",
+           "precond", "precond2"]
 
 _LABEL_RE = re.compile(r"^([+-]?)1?([ij]?)([IXYZ]+)$")
 
@@ -286,6 +289,17 @@ class PauliOperator:
                                        ns, out.data_ptr(), st))
         return out
 
+    def diagonal(self, dtype=None, device=None):
+        """Diagonal of H (2^n entries) without building the CSR: for
+        complex128 equal bit for bit to the diagonal of ``csr_device()``."""
+        import torch
+        dtype = torch.complex128 if dtype is None else dtype
+        dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+        out = torch.empty(1 << self.n, dtype=dtype, device=dev)
+        st = torch.cuda.current_stream(out.device).cuda_stream
+        check(_lib.load().qr_op_diagonal(self._h, self._dtype_of(out), out.data_ptr(), st))
+        return out
+
     def sync_check(self, stream=None):
         import torch
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
@@ -418,16 +432,10 @@ class SpMat:
         return len(self._get("cannot get NNZ of an exported sparse matrix")[1])
 
     def diagonal(self):
-        shape, data, indices, indptr = self._get(
-            "SpMat.diagonal(): already-exported sparse matrix")
-        n = min(shape)
-        out = np.zeros(n, dtype=np.complex128)
-        for r in range(n):
-            lo, hi = int(indptr[r]), int(indptr[r + 1])
-            hit = np.nonzero(indices[lo:hi] == r)[0]
-            if len(hit):
-                out[r] = data[lo + hit[0]]
-        return out
+        """Stored diagonal, 0 where a row has none (pyqrusty/src/lib.rs:118-125),
+        extracted on the GPU (qr_csr_diagonal).  numpy complex128."""
+        shape = self._get("SpMat.diagonal(): already-exported sparse matrix")[0]
+        return _spmat_diag_device(self).cpu().numpy()
 
     def __repr__(self) -> str:
         if self._it is None:
@@ -488,6 +496,104 @@ def spmat_dot_densevec(spmat: SpMat, x):
     check(_lib.load().qr_csr_spmv(shape[0], shape[1], indptr.data_ptr(), indices.data_ptr(),
                                   data.data_ptr(), xd.data_ptr(), yd.data_ptr(), st))
     return yd.cpu().numpy()
+
+
+def _spmat_diag_device(spmat: "SpMat"):
+    import torch
+    shape = spmat._it[0]
+    indptr, indices, data = spmat._device()
+    nd = min(shape)
+    out = torch.empty(nd, dtype=torch.complex128, device=data.device)
+    st = torch.cuda.current_stream(data.device).cuda_stream
+    check(_lib.load().qr_csr_diagonal(shape[0], shape[1], indptr.data_ptr(), indices.data_ptr(),
+                                      data.data_ptr(), out.data_ptr(), st))
+    return out
+
+
+def _vec_operand(v, name):
+    """(CUDA tensor, came-from-numpy) for a 1-D complex vector argument."""
+    import torch
+    if isinstance(v, torch.Tensor):
+        if not v.is_cuda:
+            raise TypeError("%s: tensors must be on a CUDA device" % name)
+        if v.dtype not in (torch.complex64, torch.complex128):
+            raise TypeError("%s: tensors must be complex64 or complex128" % name)
+        return v.contiguous(), False
+    a = np.ascontiguousarray(np.asarray(v, dtype=np.complex128))
+    if a.ndim != 1:
+        raise ValueError("%s: expected a 1-D array" % name)
+    return torch.from_numpy(a).to("cuda"), True
+
+
+def _scalar2(c):
+    c = complex(c)
+    return (C.c_double * 2)(c.real, c.imag)
+
+
+def _vec_call(name, fn, a, x, y=None, b=None, tol=None):
+    import torch
+    xd, host = _vec_operand(x, name)
+    yd = None
+    if y is not None:
+        yd, yhost = _vec_operand(y, name)
+        host = host and yhost
+        if yd.dtype != xd.dtype or yd.device != xd.device:
+            yd = yd.to(device=xd.device, dtype=xd.dtype)
+        if yd.numel() != xd.numel():
+            raise Exception("%s: vectors of different lengths (%d, %d)"
+                            % (name, xd.numel(), yd.numel()))
+    z = torch.empty_like(xd)
+    dt = QR_C64C if xd.dtype == torch.complex64 else QR_C128
+    st = torch.cuda.current_stream(xd.device).cuda_stream
+    L = _lib.load()
+    if fn == "axpby":
+        check(L.qr_axpby(dt, xd.numel(), _scalar2(a), xd.data_ptr(), _scalar2(b), yd.data_ptr(),
+                         z.data_ptr(), st))
+    elif fn == "axpy":
+        check(L.qr_axpy(dt, xd.numel(), _scalar2(a), xd.data_ptr(), yd.data_ptr(), z.data_ptr(),
+                        st))
+    elif fn == "ax":
+        check(L.qr_ax(dt, xd.numel(), _scalar2(a), xd.data_ptr(), z.data_ptr(), st))
+    else:  # precond2: x = diag, y = dx, a = e
+        check(L.qr_precond2(dt, xd.numel(), xd.data_ptr(), yd.data_ptr(), _scalar2(a),
+                            float(tol), z.data_ptr(), st))
+    return z.cpu().numpy() if host else z
+
+
+def axpby(a, x, b, y):
+    """a*x + b*y element-wise (qrusty/src/accel.rs:374-379).  numpy in ->
+    numpy out (complex128); CUDA tensors in -> tensor out, same dtype."""
+    return _vec_call("axpby", "axpby", a, x, y=y, b=b)
+
+
+def axpy(a, x, y):
+    """a*x + y element-wise (qrusty/src/accel.rs:381-386)."""
+    return _vec_call("axpy", "axpy", a, x, y=y)
+
+
+def ax(a, x):
+    """a*x element-wise (qrusty/src/accel.rs:388-393)."""
+    return _vec_call("ax", "ax", a, x)
+
+
+def precond2(diag, dx, e, tol):
+    """dx / reg(diag - e, tol), reg(v) = tol where |v| < tol
+    (pyqrusty/src/lib.rs:436-440, 457-469)."""
+    return _vec_call("precond2", "precond2", e, diag, y=dx, tol=tol)
+
+
+def precond(spmat: "SpMat", dx, e, tol):
+    """precond2 with the matrix's stored diagonal (pyqrusty/src/lib.rs:442-455,
+    binding :563-577)."""
+    if spmat._it is None:
+        raise Exception("cannot call precond with an exported sparse matrix")
+    d = _spmat_diag_device(spmat)
+    dxd, host = _vec_operand(dx, "precond")
+    if dxd.numel() != d.numel():
+        raise Exception("precond: vector length %d != diagonal length %d"
+                        % (dxd.numel(), d.numel()))
+    out = _vec_call("precond", "precond2", e, d.to(dxd.dtype), y=dxd, tol=tol)
+    return out.cpu().numpy() if host else out
 
 
 class Batch:

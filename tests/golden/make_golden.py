@@ -1,4 +1,10 @@
-"""Generate tests/golden/hamiltonians.npz from the reference's own fixtures.
+"""Generate tests/golden/*.npz from the reference's own fixtures.
+
+hamiltonians.npz -- the molecular test Hamiltonians (see below).
+precond.npz      -- the precond known-answer vectors of
+                    pyqrusty/tests/test_it.py:285-313 (tol, dx, e, rv: the
+                    reference's printed result of dx / reg(H2.diag - e, tol)),
+                    read from the test module's top-level assignments.
 
 The qrusty reference keeps its molecular test Hamiltonians as Python source
 (pyqrusty/tests/H_fixtures.py: ``build_spop(labels, coeffs)`` calls over
@@ -12,6 +18,7 @@ script is only re-run by hand, in a checkout that has the reference:
 """
 from __future__ import annotations
 
+import ast
 import os
 import sys
 import types
@@ -45,6 +52,23 @@ def load_fixtures(ref_root: str):
     return {k: ns[k] for k in KEEP}
 
 
+PRECOND_NAMES = ("tol", "dx", "e", "rv")
+
+
+def load_precond_vectors(ref_root: str):
+    """Evaluate only the top-level ``tol = / dx = / e = / rv =`` assignments of
+    pyqrusty/tests/test_it.py (numpy literals), nothing else of the module."""
+    path = os.path.join(ref_root, "pyqrusty", "tests", "test_it.py")
+    with open(path) as f:
+        tree = ast.parse(f.read(), path)
+    keep = [node for node in tree.body if isinstance(node, ast.Assign)
+            and len(node.targets) == 1 and isinstance(node.targets[0], ast.Name)
+            and node.targets[0].id in PRECOND_NAMES]
+    ns: dict = {"np": np}
+    exec(compile(ast.Module(body=keep, type_ignores=[]), path, "exec"), ns)
+    return {k: ns[k] for k in PRECOND_NAMES}
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QRUSTY_REF", "")
     if not ref_root:
@@ -58,6 +82,11 @@ def main():
     np.savez_compressed(dst, **out)
     for name, op in fx.items():
         print(name, len(op.labels), "terms,", len(op.labels[0]), "qubits")
+    print("wrote", dst)
+    pv = load_precond_vectors(ref_root)
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "precond.npz")
+    np.savez_compressed(dst, tol=np.float64(pv["tol"]), dx=np.asarray(pv["dx"], np.complex128),
+                        e=np.complex128(pv["e"]), rv=np.asarray(pv["rv"], np.complex128))
     print("wrote", dst)
 
 

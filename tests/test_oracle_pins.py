@@ -10,8 +10,13 @@ re-running the reference's known-answer tests against it:
                                   pyqrusty/tests/test_H.py:32-48 (fixtures from
                                   pyqrusty/tests/H_fixtures.py, tests/golden/)
   * CSR SpMV vs a second SpMV     qrusty/src/lib.rs:888-919, test_it.py:218-230
+  * axpby / axpy / ax known answers pyqrusty/tests/test_it.py:232-276
+  * precond / precond2 on H2       pyqrusty/tests/test_it.py:278-313 (the
+                                  reference's printed rv, tests/golden/precond.npz)
 plus structural invariants of make_row's output (accel.rs:171-210).
 """
+import os
+
 import numpy as np
 import pytest
 import scipy.sparse as sps
@@ -142,3 +147,84 @@ def test_spmv_vs_scipy(oracle, golden, name):
     _, x, z, ph, c = terms_of_labels(labels, coeffs)
     y2 = oracle.apply(n, x, z, oracle.make_params(ph, c), v)
     assert np.array_equal(y, y2)
+
+
+# ---------------------------------------------------------------- vector helpers
+X4 = np.array([1.0 + 2j, 2.0 + 3j, 3.0 + 4j, 4.0 + 5j])
+
+
+def test_vector_helper_known_answers(oracle):
+    """test_it.py:232-276: a = i, b = 1 on the 4-element vector (exact in
+    binary, so equality), and 2^20 random entries against numpy's formula."""
+    y = np.ones(4, dtype=complex)
+    assert np.array_equal(oracle.vec("axpby", X4, y, 1j, 1.0), 1j * X4 + 1.0 * y)
+    assert np.array_equal(oracle.vec("axpy", X4, y, 1j), 1j * X4 + y)
+    assert np.array_equal(oracle.vec("ax", X4, None, 1j), 1j * X4)
+    rng = np.random.default_rng(11)
+    xs = rng.random(1 << 20) + rng.random(1 << 20) * 1j
+    ys = rng.random(1 << 20) + rng.random(1 << 20) * 1j
+    a, b = 0.3 - 1.7j, -2.5 + 0.25j
+    assert np.allclose(oracle.vec("axpby", xs, ys, a, b), a * xs + b * ys, rtol=0, atol=1e-14)
+    assert np.allclose(oracle.vec("axpy", xs, ys, a), a * xs + ys, rtol=0, atol=1e-14)
+    assert np.allclose(oracle.vec("ax", xs, None, a), a * xs, rtol=0, atol=1e-14)
+
+
+def _h2_diagonal(oracle, golden):
+    labels, coeffs = golden["H2"]
+    n, (indptr, indices, data) = oracle_csr(oracle, labels, coeffs)
+    d = np.zeros(1 << n, dtype=complex)
+    for r in range(1 << n):
+        lo, hi = int(indptr[r]), int(indptr[r + 1])
+        hit = np.nonzero(indices[lo:hi] == r)[0]
+        if len(hit):
+            d[r] = data[lo + hit[0]]
+    return d
+
+
+def test_precond_golden(oracle, golden):
+    """precond2(H2.diagonal(), dx, e, tol) against the result the reference
+    printed in its test (9 significant digits) and against its numpy
+    restatement dx / reg(diag - e, tol) (test_it.py:270-313)."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "precond.npz"))
+    d = _h2_diagonal(oracle, golden)
+    got = oracle.vec("precond2", d, g["dx"], complex(g["e"]), tol=float(g["tol"]))
+    assert np.allclose(got, g["rv"], rtol=1e-8, atol=1e-300)
+    v = d - complex(g["e"])
+    v = np.where(np.abs(v) < float(g["tol"]), float(g["tol"]), v)
+    assert np.allclose(got, g["dx"] / v, rtol=1e-15, atol=0)
+
+
+def test_precond_regularises_small_pivots(oracle):
+    diag = np.array([1.0 + 0j, 2.0 + 1e-20j, 3.0 + 0j])
+    dx = np.array([1.0 + 1j, 1.0 + 1j, 1.0 + 1j])
+    got = oracle.vec("precond2", diag, dx, 2.0, tol=1e-6)
+    assert got[1] == (1.0 + 1j) / 1e-6
+    assert got[0] == (1.0 + 1j) / (-1.0) and got[2] == (1.0 + 1j) / 1.0
+
+
+def test_vector_helpers_complex64(oracle):
+    """complex64: the same sequence in float; a, b rounded to float."""
+    rng = np.random.default_rng(12)
+    xs = (rng.random(1001) + rng.random(1001) * 1j).astype(np.complex64)
+    ys = (rng.random(1001) + rng.random(1001) * 1j).astype(np.complex64)
+    a = np.complex64(0.3 - 1.7j)
+    got = oracle.vec("axpy", xs, ys, complex(a))
+    assert got.dtype == np.complex64
+    ar, ai = np.float32(a.real), np.float32(a.imag)
+    want_re = (ar * xs.real - ai * xs.imag) + ys.real
+    want_im = (ar * xs.imag + ai * xs.real) + ys.imag
+    assert np.array_equal(got.real, want_re) and np.array_equal(got.imag, want_im)
+
+
+@pytest.mark.parametrize("name", ["H2", "H4", "H6"])
+def test_op_diagonal_is_csr_diagonal(oracle, golden, name):
+    labels, coeffs = golden[name]
+    n, x, z, ph, c = terms_of_labels(labels, coeffs)
+    cp = oracle.make_params(ph, c)
+    indptr, indices, data = oracle.csr_build(n, x, z, cp, nthreads=4)
+    d = oracle.op_diagonal(x, z, cp, 0, 1 << n)
+    for r in range(1 << n):
+        lo, hi = int(indptr[r]), int(indptr[r + 1])
+        hit = np.nonzero(indices[lo:hi] == r)[0]
+        want = data[lo + hit[0]] if len(hit) else 0j
+        assert d[r].tobytes() == np.complex128(want).tobytes()
