@@ -65,6 +65,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """Largest x over the ranks of the default process group (x itself when
+    there is none): a step's time is the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world_size: int, units_per_rank: float, seconds: float) -> float:
+    """Aggregate throughput of replicas: every rank processes units_per_rank
+    in the same (max-over-ranks) time."""
+    return world_size * units_per_rank / seconds
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -255,12 +273,7 @@ def run_gpu_arm(args, t, desc):
         barrier()
         launches = _lib.launch_count() - l0
         per = [a.elapsed_time(b) for a, b in evs]
-        total = e_all0.elapsed_time(e_all1)
-        if ws > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([total], device=dev, dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            total = float(tt.item())
+        total = max_over_ranks(e_all0.elapsed_time(e_all1), dev)
         return total, per, launches
 
     clocks = ClockSampler(dev.index if dev.index is not None else 0)
@@ -300,13 +313,8 @@ def run_gpu_arm(args, t, desc):
         for _ in range(e_steps):
             op.apply(a_in, out=a_out)
         barrier()
-        e_ms = 1e3 * (time.perf_counter() - t0) / e_steps
-        if ws > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([e_ms], device=dev, dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e_ms = float(tt.item())
-        e2e = {"value": ws * T * N / (e_ms / 1e3), "unit": UNIT, "ms_per_step": e_ms,
+        e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0) / e_steps, dev)
+        e2e = {"value": whole_job_rate(ws, T * N, e_ms / 1e3), "unit": UNIT, "ms_per_step": e_ms,
                "h2d_bytes_per_step": N * 8, "d2h_bytes_per_step": N * 8,
                "path": "qr_apply_host (C ABI), pinned host buffers"}
 
@@ -328,7 +336,8 @@ def run_gpu_arm(args, t, desc):
     if tr and tr.get("workload") == desc:
         traffic = tr.get("bytes_per_launch")
     out = {
-        "metric": METRIC, "value": ws * T * N / (ms64 / 1e3), "unit": UNIT, "n_gpus": ws,
+        "metric": METRIC, "value": whole_job_rate(ws, T * N, ms64 / 1e3), "unit": UNIT,
+        "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms64,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64c (fp32 + two-sum)", "data": "synthetic",
@@ -343,7 +352,8 @@ def run_gpu_arm(args, t, desc):
                      "alg_bytes_per_launch": alg64,
                      "alg_bytes_rule": "(P+1)*2^n*8, P=%d distinct x>>13" % P,
                      "peak_source": peak_kind},
-        "c128": {"value": ws * T * N / (ms128 / 1e3), "ms_per_step": ms128, "steps": s128,
+        "c128": {"value": whole_job_rate(ws, T * N, ms128 / 1e3), "ms_per_step": ms128,
+                 "steps": s128,
                  "hbm_achieved_gbs": ach128, "hbm_frac": ach128 / hbm},
         "speedup_c64c_vs_c128": ms128 / ms64,
         "rel_err": {"c64c_vs_c128_full": rel64},
@@ -591,7 +601,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["jw", "chain", "batch", "grad", "vec", "csr"],
                     default="jw")
-    ap.add_argument("--n", type=int, default=26)
+    ap.add_argument("--qubits", "--n", dest="n", type=int, default=26,
+                    help="qubits of the workload (--n is accepted outside torchrun)")
     ap.add_argument("--pairs", type=int, default=8000)
     ap.add_argument("--zterms", type=int, default=2000)
     ap.add_argument("--cpu-rows", type=int, default=1 << 16,

@@ -230,6 +230,52 @@ int qr_csr_diagonal(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
  * bit for bit; QR_C64C rounds that FP64 value to complex64.  2^n elements. */
 int qr_op_diagonal(qr_op *op, int32_t dtype, void *out, void *stream);
 
+/* On-disk CSR formats.  Paths ending in ".gz" are gzip streams (zlib is
+ * loaded at run time), as qrusty/src/util.rs:324-367 opens them.  Arrays are
+ * host (mem = QR_MEM_HOST) or device (QR_MEM_DEVICE, staged through pinned
+ * buffers on `stream`) memory; every call is synchronous.
+ *
+ * rawio -- qrusty/src/rawio.rs:128-179 (rawio::write / rawio::read): mark
+ * "MI" in the writer's byte order, u64 storage (0 CSR, 1 CSC), rows, cols,
+ * then (u64 length, words) for indptr, indices and data (complex128).  A file
+ * from a machine of the other byte order is swapped on reading.
+ * qr_rawio_info reads the sizes (nnz = data length), qr_rawio_read fills
+ * caller-owned arrays of those sizes. */
+typedef struct {
+    uint64_t storage;     /* 0 = CSR, 1 = CSC                              */
+    uint64_t nrows, ncols;
+    uint64_t indptr_len;  /* entries of indptr                             */
+    uint64_t nnz;         /* entries of indices and of data                */
+    int32_t byte_swapped; /* file written with the other byte order       */
+} qr_csr_file_info;
+int qr_rawio_info(const char *path, qr_csr_file_info *info);
+int qr_rawio_read(const char *path, uint64_t *indptr, uint64_t *indices, double *data, int32_t mem,
+                  void *stream);
+int qr_rawio_write(const char *path, uint64_t storage, uint64_t nrows, uint64_t ncols,
+                   const uint64_t *indptr, uint64_t indptr_len, const uint64_t *indices,
+                   const double *data, uint64_t nnz, int32_t mem, void *stream);
+
+/* MatrixMarket -- SpMat.matrixmarket_write / matrixmarket_write_symmetric /
+ * matrixmarket_read (pyqrusty/src/lib.rs:216-260, sprs::io).  Writing: a CSR
+ * matrix as "coordinate complex <symmetry>" (symmetry 0 general,
+ * 1 symmetric, 2 skew-symmetric, 3 hermitian; the symmetric kinds write the
+ * lower triangle, skew the strict lower triangle), 1-based, rows in order,
+ * values as the shortest decimal that reads back to the same double, no
+ * exponent.  Reading: coordinate files of real / integer / complex / pattern
+ * field and any of the four symmetries, mirrored entries added, converted
+ * to CSR with columns ascending and duplicates summed in file order;
+ * qr_mm_open parses into a handle, qr_mm_fetch copies it out,
+ * qr_mm_close frees it. */
+typedef struct qr_csr_file qr_csr_file;
+int qr_mm_write(const char *path, uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
+                const uint64_t *indices, const double *data, int32_t symmetry, int32_t mem,
+                void *stream);
+int qr_mm_open(const char *path, qr_csr_file **out, uint64_t *nrows, uint64_t *ncols,
+               uint64_t *nnz);
+int qr_mm_fetch(const qr_csr_file *f, uint64_t *indptr, uint64_t *indices, double *data,
+                int32_t mem, void *stream);
+int qr_mm_close(qr_csr_file *f);
+
 /* Message of the calling thread's last failure ("" if none).  Copies at
  * most len-1 bytes plus a terminating NUL; returns the full length. */
 int qr_last_error(char *buf, size_t len);

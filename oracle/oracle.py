@@ -220,3 +220,47 @@ def op_diagonal(x, z, cprime, row0, nrows):
                          np.ascontiguousarray(cprime, dtype=np.complex128).view(np.float64),
                          int(row0), int(nrows), out)
     return out.view(np.complex128)
+
+
+# --------------------------------------------------------------------------
+# rawio file layout (qrusty/src/rawio.rs:128-179), restated with numpy
+# --------------------------------------------------------------------------
+def rawio_bytes(storage, nrows, ncols, indptr, indices, data, byteorder="<"):
+    """Bytes of rawio::write (rawio.rs:128-149) as a machine of the given
+    byte order writes them: mark b"MI" in that order, u64 storage / rows /
+    cols, then (u64 length, words) for indptr, indices and data."""
+    u64 = np.dtype(byteorder + "u8")
+    f64 = np.dtype(byteorder + "f8")
+    mark = b"MI" if byteorder == "<" else b"IM"
+    parts = [mark, np.array([storage, nrows, ncols], dtype=u64).tobytes()]
+    for arr, dt in ((np.asarray(indptr, np.uint64), u64), (np.asarray(indices, np.uint64), u64)):
+        parts.append(np.array([len(arr)], dtype=u64).tobytes())
+        parts.append(arr.astype(dt).tobytes())
+    d = np.ascontiguousarray(np.asarray(data, np.complex128)).view(np.float64)
+    parts.append(np.array([len(d) // 2], dtype=u64).tobytes())
+    parts.append(d.astype(f64).tobytes())
+    return b"".join(parts)
+
+
+def rawio_parse(buf):
+    """rawio::read (rawio.rs:151-179): the reader swaps when the mark is not
+    b"MI" in its own (little-endian here) order."""
+    order = "<" if buf[:2] == b"MI" else ">"
+    u64 = np.dtype(order + "u8")
+    storage, nrows, ncols = (int(v) for v in np.frombuffer(buf, u64, 3, 2))
+    if storage > 1:
+        raise ValueError("rawio::read: bad storage found")
+    off = 26
+
+    def record(off, kind):
+        n = int(np.frombuffer(buf, u64, 1, off)[0])
+        words = n * (2 if kind == "c" else 1)
+        dt = np.dtype(order + ("f8" if kind == "c" else "u8"))
+        arr = np.frombuffer(buf, dt, words, off + 8)
+        return arr, off + 8 + arr.nbytes
+
+    indptr, off = record(off, "u")
+    indices, off = record(off, "u")
+    data, off = record(off, "c")
+    return (storage, nrows, ncols, indptr.astype(np.uint64), indices.astype(np.uint64),
+            data.astype(np.float64).view(np.complex128))

@@ -19,6 +19,7 @@ LIB = os.path.join(PKG, "libqrusty_gpu.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 SOURCES = ["qr_host.cu", "qr_apply.cu", "qr_csr.cu", "qr_reduce.cu", "qr_vec.cu"]
+HOST_SOURCES = ["qr_io.cpp"]  # host-only C++ (file formats), compiled by the host compiler
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
          "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", INCLUDE]
@@ -38,6 +39,10 @@ def _stale(target: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def cuda_include() -> str:
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "include")
+
+
 def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     os.makedirs(OBJ, exist_ok=True)
     hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
@@ -49,9 +54,20 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
         if force or _stale(o, [s] + hdrs):
             jobs.append((s, o))
 
+    for src in HOST_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ, src.replace(".cpp", ".o"))
+        if force or _stale(o, [s] + hdrs):
+            jobs.append((s, o))
+
     def compile_one(job):
         s, o = job
-        cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", s, "-o", o + ".tmp"]
+        if s.endswith(".cpp"):
+            cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
+            cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INCLUDE,
+                   "-I", cuda_include(), "-c", s, "-o", o + ".tmp"]
+        else:
+            cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", s, "-o", o + ".tmp"]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -61,12 +77,13 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
             print(r.stdout + r.stderr, file=sys.stderr)
         os.replace(o + ".tmp", o)
 
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES) + len(HOST_SOURCES)) as ex:
         list(ex.map(compile_one, jobs))
     objs = [os.path.join(OBJ, s.replace(".cu", ".o")) for s in SOURCES]
+    objs += [os.path.join(OBJ, s.replace(".cpp", ".o")) for s in HOST_SOURCES]
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-ldl", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

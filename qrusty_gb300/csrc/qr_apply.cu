@@ -647,8 +647,15 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
 //     table read, the partner offset;
 //   * per run of sub-groups with equal register-bit sign pattern: one
 //     dispatch to a compile-time instantiation.
-constexpr int kTabStages = 5;
-constexpr uint32_t kTabMaxSub = 512;  // per-tile table entries (64 B each)
+#ifndef QR_TAB_STAGES
+#define QR_TAB_STAGES 4
+#endif
+constexpr int kTabStages = QR_TAB_STAGES;  // partner-tile ring depth (4 timed best of 3, 4, 5)
+constexpr size_t kMaxSmemPerBlock = 227u * 1024u;  // sm_100-family opt-in limit
+constexpr int kTabEnt = 4;  // per-tile table entries (float4) per sub-group
+constexpr uint32_t kTabMaxSub = 512;
+// full barriers, stage counters and the abort flag, rounded to 8 bytes
+constexpr size_t kTabBarBytes = ((size_t)kTabStages * 12u + 4u + 7u) & ~(size_t)7u;
 
 template <int AMPS, int ZM, bool XM>
 __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
@@ -724,10 +731,22 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
     const uint32_t lane = t & 31;
     const uint32_t tile_bytes = (1u << a.b) * 8u;
     float4 *s_tab = reinterpret_cast<float4 *>(smem_raw + (size_t)kTabStages * tile_bytes);
-    float2 *s_lo = reinterpret_cast<float2 *>(s_tab + 4 * (size_t)a.nsub);
+    float2 *s_lo = reinterpret_cast<float2 *>(s_tab + kTabEnt * (size_t)a.nsub);
     uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
     uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kTabStages);
     volatile uint32_t *s_abort = cnt + kTabStages;
+    // sub-group descriptors, runs (g0 | key << 16) and per-block run ranges,
+    // staged once per CTA
+    uint2 *s_td = reinterpret_cast<uint2 *>(smem_raw + (size_t)kTabStages * tile_bytes +
+                                            (size_t)kTabEnt * 16u * a.nsub +
+                                            (size_t)AMPS * threads * 8u + kTabBarBytes);
+    uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + a.nsub);
+    uint32_t *s_blk = s_run + a.nruns + 1;
+    for (uint32_t i = t; i < a.nsub; i += threads) s_td[i] = a.tdesc[i];
+    for (uint32_t i = t; i <= a.nruns; i += threads)
+        s_run[i] = a.run_g0[i] | (i < a.nruns ? a.run_key[i] << 16 : 0u);
+    for (uint32_t i = t; i <= a.nblocks; i += threads) s_blk[i] = a.blk_r0[i];
+    const uint2 *tdesc = s_td;
 
     const float2 *psi = static_cast<const float2 *>(a.psi);
     float2 *y = static_cast<float2 *>(a.y);
@@ -817,10 +836,14 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
             }
         }
 
-        const uint32_t r1 = skip ? 0u : a.blk_r0[j + 1];
-        for (uint32_t r = a.blk_r0[j]; r < r1; ++r)
-            run_tab_dispatch<AMPS>(a.run_key[r], A, B, smem_raw, soff, s_tab, a.tdesc,
-                                   a.run_g0[r], a.run_g0[r + 1], t, tmask, tb);
+        const uint32_t r1 = skip ? 0u : s_blk[j + 1];
+        uint32_t rw = s_run[s_blk[j]];
+        for (uint32_t r = s_blk[j]; r < r1; ++r) {
+            const uint32_t rn = s_run[r + 1];
+            run_tab_dispatch<AMPS>(rw >> 16, A, B, smem_raw, soff, s_tab, tdesc, rw & 0xffffu,
+                                   rn & 0xffffu, t, tmask, tb);
+            rw = rn;
+        }
 
         const bool last = (j == nb - 1);
         if (last || (j % kFlush) == kFlush - 1) {
@@ -892,11 +915,18 @@ static cudaError_t launch_c64c_w(const ApplyArgs &a, int threads, int nsm, cudaS
     return cudaGetLastError();
 }
 
+template <int AMPS>
+static size_t tab_smem_bytes(const ApplyArgs &a, int threads) {
+    const uint32_t tile_bytes = (1u << a.b) * 8u;
+    size_t smem = (size_t)kTabStages * tile_bytes + (size_t)a.nsub * 16u * kTabEnt +
+                  (size_t)AMPS * threads * 8u + kTabBarBytes;
+    smem += (size_t)a.nsub * 8u + ((size_t)a.nruns + 1 + a.nblocks + 1) * 4u;
+    return smem;
+}
+
 template <int AMPS, bool WIDE>
 static cudaError_t launch_c64c_tab(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
-    const uint32_t tile_bytes = (1u << a.b) * 8u;
-    const size_t smem = (size_t)kTabStages * tile_bytes + (size_t)a.nsub * 64u +
-                        (size_t)AMPS * threads * 8u + kTabStages * (sizeof(uint64_t) + 4) + 4;
+    const size_t smem = tab_smem_bytes<AMPS>(a, threads);
     auto kern = apply_c64c_tab<AMPS, WIDE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -910,7 +940,8 @@ static cudaError_t launch_c64c_tab(const ApplyArgs &a, int threads, int nsm, cud
 
 template <int AMPS>
 static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
-    if (a.nsub <= kTabMaxSub) {
+    // the per-tile-table kernel needs its tables and run lists in shared memory
+    if (a.nsub <= kTabMaxSub && tab_smem_bytes<AMPS>(a, threads) <= kMaxSmemPerBlock) {
         if (a.n > 32) return launch_c64c_tab<AMPS, true>(a, threads, nsm, st);
         return launch_c64c_tab<AMPS, false>(a, threads, nsm, st);
     }

@@ -80,6 +80,7 @@ struct ApplyArgs {
     const uint32_t *blk_r0;   // runs of block j: [blk_r0[j], blk_r0[j+1])
     const uint32_t *run_g0;   // sub-groups of run r: [run_g0[r], run_g0[r+1])
     const uint32_t *run_key;  // key = zm | xm << 4
+    uint32_t nruns;
 };
 
 
@@ -133,15 +134,35 @@ cudaError_t launch_diag(int dtype, int n, int db, uint64_t ntiles, const uint64_
                         const uint32_t *bin_off, uint32_t nbins, const uint64_t *tz,
                         const double *tc, void *out, cudaStream_t st);
 
+// CSR fill.  Per group g (x masks ascending): the sigma values of its
+// position formula, and either a class table -- the term-order fold of
+// the group's +-c'_k for each of the 2^(d+1) sign classes of a row, class
+// bit 0 = parity(r & z0), bit j+1 = parity(r & beta_j) -- or, when the z
+// span has rank > kCsrMaxRank, the term range to fold per row.
+constexpr int kCsrMaxRank = 4;
+constexpr uint32_t kCsrFold = 0xffffffffu;
+struct CsrGroup {
+    uint64_t z0;
+    uint64_t beta[kCsrMaxRank];
+    uint32_t d;       // rank of the z differences, or kCsrFold
+    uint32_t tab;     // first class-table entry (2^(d+1) entries)
+    uint32_t pad0, pad1;
+    uint32_t k0, k1;  // terms [k0, k1) in group-stable order (fold mode)
+};
+static_assert(sizeof(CsrGroup) == 64, "CsrGroup layout");
+
 struct CsrArgs {
     uint64_t N, G;
+    int n;                    // qubits: row bits
     const uint64_t *gx;       // G, ascending
-    const uint32_t *goff;     // G+1
-    const uint64_t *tz;       // terms in group-stable order
+    const CsrGroup *grp;      // G
+    const uint64_t *pmask;    // G: bits b with a nonzero sigma_{g,b}
+    const int32_t *sig;       // G x n: sigma_{g,b} (0 where b is not in pmask)
+    const uint32_t *fold;     // groups in fold mode
+    uint32_t nfold;
+    const double2 *ctab;      // class tables
+    const uint64_t *tz;       // terms in group-stable order (fold mode)
     const double *tc;         // 2 doubles per term
-    const uint32_t *eoff;     // G+1: trie entries per group
-    const uint8_t *ebit;
-    const int64_t *esig;
     uint64_t *indptr, *indices;
     double *data;
     uint64_t row0, nrows;     // rows to fill

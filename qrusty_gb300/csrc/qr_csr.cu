@@ -13,6 +13,13 @@
 // the size of g's sibling subtree at bit b of the binary trie of the x
 // masks (nonzero only at the trie's branching bits).  The host precomputes
 // the (b, sigma) lists; each thread places one (row, group) entry directly.
+//
+// Values without a per-row fold: a group's value in row r depends on r only
+// through the parities of r against the group's z masks, i.e. against z0 and
+// a GF(2) basis beta_1..beta_d of the differences z_k ^ z0.  For d <= 4 the
+// host folds the group's +-c'_k in input order once per class (2^(d+1)
+// classes) -- the same additions in the same order as make_row, hence the
+// same bits -- and the kernel reads the row's class from that table.
 #include "qr_common.cuh"
 
 namespace qr {
@@ -24,38 +31,104 @@ __global__ void __launch_bounds__(256) csr_indptr_kernel(uint64_t N, uint64_t G,
         indptr[r] = r * G;
 }
 
-__global__ void __launch_bounds__(256) csr_fill_kernel(const CsrArgs a) {
-    const uint64_t total = a.nrows * a.G;
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
-         e += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t rr = e / a.G;
-        const uint64_t g = e - rr * a.G;
-        const uint64_t r = a.row0 + rr;
-        int64_t pos = (int64_t)g;
-        for (uint32_t k = a.eoff[g]; k < a.eoff[g + 1]; ++k)
-            if ((r >> a.ebit[k]) & 1ull) pos += a.esig[k];
-        // left fold in input-term order; first term taken as-is
-        const uint32_t k0 = a.goff[g], k1 = a.goff[g + 1];
-        double vr, vi;
-        {
-            const bool neg = (__popcll(r & a.tz[k0]) & 1) != 0;
-            vr = neg ? -a.tc[2 * k0] : a.tc[2 * k0];
-            vi = neg ? -a.tc[2 * k0 + 1] : a.tc[2 * k0 + 1];
+// Rank of column r ^ x_g in row r: g + sum of sigma_{g,b} over the bits b
+// of r in the group's position mask (sig: the group's row of the table).
+__device__ __forceinline__ int32_t csr_pos(uint64_t r, uint32_t g, uint64_t pm,
+                                           const int32_t *sig) {
+    int32_t pos = (int32_t)g;
+    for (uint64_t m = r & pm; m; m &= m - 1) pos += sig[__ffsll((long long)m) - 1];
+    return pos;
+}
+
+__device__ __forceinline__ void csr_store(const CsrArgs &a, uint64_t rr, int32_t pos, uint64_t col,
+                                          double2 v) {
+    if (pos < 0 || (uint64_t)pos >= a.G) {  // cannot happen for a valid trie table
+        atomicExch(a.err, kErrCsrPos);
+        return;
+    }
+    const uint64_t o = rr * a.G + (uint64_t)pos;
+    a.indices[o] = col;
+    reinterpret_cast<double2 *>(a.data)[o] = v;
+}
+
+// Class of row r for group d: bit 0 = parity(r & z0), bit j+1 = parity(r & beta_j).
+__device__ __forceinline__ uint32_t csr_class(const CsrGroup &d, uint64_t r) {
+    uint32_t c = (uint32_t)__popcll(r & d.z0) & 1u;
+#pragma unroll
+    for (int j = 0; j < kCsrMaxRank; ++j)
+        if ((uint32_t)j < d.d) c |= ((uint32_t)__popcll(r & d.beta[j]) & 1u) << (j + 1);
+    return c;
+}
+
+constexpr int kCsrThreads = 256;
+constexpr uint32_t kCsrSmemSig = 12288;  // sigma entries staged in shared memory (48 KB)
+
+// Class-table groups.  G <= 256: thread t owns group g = t % G of row t / G
+// in every pass of 256 / G consecutive rows, so its descriptor and position
+// mask stay in registers and no per-entry division is needed.  G > 256: one
+// row per pass, threads stride the groups.  Fold-mode groups are left to
+// csr_fold_kernel, so no lane of a warp waits on another's long fold.
+__global__ void __launch_bounds__(kCsrThreads) csr_fill_kernel(const CsrArgs a) {
+    extern __shared__ int32_t s_sig[];
+    const uint32_t G = (uint32_t)a.G;
+    const uint64_t nsig = (uint64_t)G * (uint32_t)a.n;
+    const bool staged = nsig <= kCsrSmemSig;
+    if (staged)
+        for (uint32_t i = threadIdx.x; i < nsig; i += kCsrThreads) s_sig[i] = a.sig[i];
+    __syncthreads();
+    const int32_t *sig = staged ? s_sig : a.sig;
+    if (G <= (uint32_t)kCsrThreads) {
+        const uint32_t rpp = kCsrThreads / G;
+        const uint32_t t = threadIdx.x;
+        if (t >= rpp * G) return;  // no barrier follows
+        const uint32_t rs = t / G, g = t - rs * G;
+        const CsrGroup d = a.grp[g];
+        if (d.d == kCsrFold) return;
+        const uint64_t xg = a.gx[g], pm = a.pmask[g];
+        const int32_t *sg = sig + (size_t)g * (uint32_t)a.n;
+        const uint64_t npass = (a.nrows + rpp - 1) / rpp;
+        for (uint64_t p = blockIdx.x; p < npass; p += gridDim.x) {
+            const uint64_t rr = p * rpp + rs;
+            if (rr >= a.nrows) break;
+            const uint64_t r = a.row0 + rr;
+            csr_store(a, rr, csr_pos(r, g, pm, sg), r ^ xg, a.ctab[d.tab + csr_class(d, r)]);
         }
-        for (uint32_t k = k0 + 1; k < k1; ++k) {
-            const bool neg = (__popcll(r & a.tz[k]) & 1) != 0;
-            const double cr = neg ? -a.tc[2 * k] : a.tc[2 * k];
-            const double ci = neg ? -a.tc[2 * k + 1] : a.tc[2 * k + 1];
-            vr = __dadd_rn(vr, cr);
-            vi = __dadd_rn(vi, ci);
+    } else {
+        for (uint64_t rr = blockIdx.x; rr < a.nrows; rr += gridDim.x) {
+            const uint64_t r = a.row0 + rr;
+            for (uint32_t g = threadIdx.x; g < G; g += kCsrThreads) {
+                const CsrGroup d = a.grp[g];
+                if (d.d == kCsrFold) continue;
+                const int32_t pos = csr_pos(r, g, a.pmask[g], sig + (size_t)g * (uint32_t)a.n);
+                csr_store(a, rr, pos, r ^ a.gx[g], a.ctab[d.tab + csr_class(d, r)]);
+            }
         }
-        if (pos < 0 || (uint64_t)pos >= a.G) {  // cannot happen for a valid trie table
-            atomicExch(a.err, kErrCsrPos);
-            continue;
+    }
+}
+
+// Fold-mode groups (z span wider than kCsrMaxRank): one thread per row, all
+// lanes of a warp on the same group, the group's +-c'_k folded in input-term
+// order from the first term (make_row's fold), terms read warp-uniformly.
+__global__ void __launch_bounds__(kCsrThreads) csr_fold_kernel(const CsrArgs a) {
+    for (uint32_t f = blockIdx.y; f < a.nfold; f += gridDim.y) {
+        const uint32_t g = a.fold[f];
+        const CsrGroup d = a.grp[g];
+        const uint64_t xg = a.gx[g], pm = a.pmask[g];
+        const int32_t *sg = a.sig + (size_t)g * (uint32_t)a.n;
+        for (uint64_t rr = blockIdx.x * (uint64_t)kCsrThreads + threadIdx.x; rr < a.nrows;
+             rr += (uint64_t)gridDim.x * kCsrThreads) {
+            const uint64_t r = a.row0 + rr;
+            const uint32_t k0 = d.k0, k1 = d.k1;
+            const bool neg0 = (__popcll(r & a.tz[k0]) & 1) != 0;
+            double vr = neg0 ? -a.tc[2 * k0] : a.tc[2 * k0];
+            double vi = neg0 ? -a.tc[2 * k0 + 1] : a.tc[2 * k0 + 1];
+            for (uint32_t k = k0 + 1; k < k1; ++k) {
+                const bool neg = (__popcll(r & a.tz[k]) & 1) != 0;
+                vr = __dadd_rn(vr, neg ? -a.tc[2 * k] : a.tc[2 * k]);
+                vi = __dadd_rn(vi, neg ? -a.tc[2 * k + 1] : a.tc[2 * k + 1]);
+            }
+            csr_store(a, rr, csr_pos(r, g, pm, sg), r ^ xg, make_double2(vr, vi));
         }
-        const uint64_t o = rr * a.G + (uint64_t)pos;
-        a.indices[o] = r ^ a.gx[g];
-        reinterpret_cast<double2 *>(a.data)[o] = make_double2(vr, vi);
     }
 }
 
@@ -68,11 +141,22 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    const uint64_t total = a.nrows * a.G;
-    if (total == 0) return cudaSuccess;
-    uint64_t g = (total + 255) / 256;
-    if (g > (uint64_t)nsm * 16) g = (uint64_t)nsm * 16;
-    csr_fill_kernel<<<(unsigned)g, 256, 0, st>>>(a);
+    if (a.nrows == 0 || a.G == 0) return cudaSuccess;
+    const uint64_t rpp = a.G <= (uint64_t)kCsrThreads ? (uint64_t)kCsrThreads / a.G : 1;
+    uint64_t g = (a.nrows + rpp - 1) / rpp;
+    if (g > (uint64_t)nsm * 8) g = (uint64_t)nsm * 8;
+    const uint64_t nsig = a.G * (uint64_t)a.n;
+    const size_t smem = nsig <= kCsrSmemSig ? (size_t)nsig * sizeof(int32_t) : 0;
+    csr_fill_kernel<<<(unsigned)g, kCsrThreads, smem, st>>>(a);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || a.nfold == 0) return e;
+    uint64_t gx = (a.nrows + kCsrThreads - 1) / kCsrThreads;
+    const uint32_t gy = a.nfold < 65535u ? a.nfold : 65535u;
+    uint64_t cap = ((uint64_t)nsm * 8 + gy - 1) / gy;
+    if (cap < 1) cap = 1;
+    if (gx > cap) gx = cap;
+    csr_fold_kernel<<<dim3((unsigned)gx, gy), kCsrThreads, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }

@@ -95,7 +95,7 @@ struct Plan {
     bool has_diag = false;
     DevBuf groups, tables, fat_z, fat_c, blk_hi, blk_g0, diag;
     // compensated-c64 kernel tables
-    uint32_t nsub = 0;
+    uint32_t nsub = 0, nruns = 0;
     DevBuf sub;
     DevBuf tdesc, tdata, blk_r0, run_g0, run_key;
 };
@@ -118,11 +118,11 @@ struct qr_op {
     std::vector<uint32_t> goff;
     std::vector<uint64_t> tz;
     std::vector<cd> tc;
-    std::vector<uint32_t> eoff;
-    std::vector<uint8_t> ebit;
-    std::vector<int64_t> esig;
+    std::vector<uint64_t> pmask;        // per group: bits with a nonzero sigma
+    std::vector<int32_t> sig;           // G x n: sigma_{g,b}
     bool csr_uploaded = false;
-    DevBuf d_gx, d_goff, d_tz, d_tc, d_eoff, d_ebit, d_esig;
+    uint32_t nfold = 0;
+    DevBuf d_gx, d_goff, d_tz, d_tc, d_pmask, d_sig, d_grp, d_ctab, d_fold;
     // merged terms (FP64 simplification) for qr_apply; mmap[k] = merged index
     std::vector<uint64_t> mx, mz;
     std::vector<cd> mc;
@@ -187,28 +187,82 @@ int prepare_csr_tables(qr_op *op) {
     op->csr_order = order;
     std::vector<std::vector<std::pair<uint8_t, int64_t>>> ent(op->G);
     build_trie(op->gx, 0, op->G, op->n - 1, ent);
-    op->eoff.assign(1, 0);
-    op->ebit.clear();
-    op->esig.clear();
+    if (op->G >= (1ull << 31)) return fail(QR_EINVAL, "qr_op_create: too many distinct x masks");
+    op->pmask.assign(op->G, 0);
+    op->sig.assign(op->G * (uint64_t)op->n, 0);
     for (uint64_t g = 0; g < op->G; ++g) {
         for (auto &e : ent[g]) {
-            op->ebit.push_back(e.first);
-            op->esig.push_back(e.second);
+            op->pmask[g] |= 1ull << e.first;
+            op->sig[g * op->n + e.first] = (int32_t)e.second;
         }
-        op->eoff.push_back((uint32_t)op->ebit.size());
     }
     return QR_OK;
 }
 
+struct Span {
+    std::vector<uint64_t> basis;
+    std::vector<uint64_t> coord;  // per term
+    bool overflow = false;
+};
+Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax);
+
+// Per group: position-formula range and either the class table (the
+// term-order fold of +-c'_k for every sign class; same additions in the same
+// order as make_row, so the same bits) or the term range for a per-row fold.
+void build_csr_groups(const qr_op *op, std::vector<CsrGroup> &grp, std::vector<cd> &ctab,
+                      std::vector<uint32_t> &fold) {
+    grp.assign(op->G, CsrGroup{});
+    ctab.clear();
+    fold.clear();
+    for (uint64_t g = 0; g < op->G; ++g) {
+        CsrGroup &d = grp[g];
+        const uint32_t k0 = op->goff[g], k1 = op->goff[g + 1];
+        d.k0 = k0;
+        d.k1 = k1;
+        d.z0 = op->tz[k0];
+        std::vector<uint64_t> zs(op->tz.begin() + k0, op->tz.begin() + k1);
+        Span sp = gf2_span(zs, kCsrMaxRank);
+        if (sp.overflow) {
+            d.d = kCsrFold;
+            d.tab = 0;
+            fold.push_back((uint32_t)g);
+            continue;
+        }
+        d.d = (uint32_t)sp.basis.size();
+        for (uint32_t j = 0; j < d.d; ++j) d.beta[j] = sp.basis[j];
+        d.tab = (uint32_t)ctab.size();
+        const uint32_t ncls = 2u << d.d;
+        for (uint32_t c = 0; c < ncls; ++c) {
+            cd v{0.0, 0.0};
+            for (uint32_t k = k0; k < k1; ++k) {
+                const uint64_t sel = 1ull | (sp.coord[k - k0] << 1);
+                const bool neg = (__builtin_popcountll(c & sel) & 1) != 0;
+                const cd t = neg ? cd{-op->tc[k].re, -op->tc[k].im} : op->tc[k];
+                if (k == k0) v = t;
+                else v = cd{v.re + t.re, v.im + t.im};
+            }
+            ctab.push_back(v);
+        }
+    }
+}
+
 int upload_csr_tables(qr_op *op) {
     if (op->csr_uploaded) return QR_OK;
+    std::vector<CsrGroup> grp;
+    std::vector<cd> ctab;
+    std::vector<uint32_t> fold;
+    build_csr_groups(op, grp, ctab, fold);
+    if (ctab.size() > 0xffffffffull) return fail(QR_EINVAL, "qr_csr_build: class tables too large");
     QR_CUDA(op->d_gx.upload(op->gx), "upload gx");
     QR_CUDA(op->d_goff.upload(op->goff), "upload goff");
     QR_CUDA(op->d_tz.upload(op->tz), "upload tz");
     QR_CUDA(op->d_tc.upload(op->tc), "upload tc");
-    QR_CUDA(op->d_eoff.upload(op->eoff), "upload eoff");
-    QR_CUDA(op->d_ebit.upload(op->ebit), "upload ebit");
-    QR_CUDA(op->d_esig.upload(op->esig), "upload esig");
+    QR_CUDA(op->d_pmask.upload(op->pmask), "upload position masks");
+    QR_CUDA(op->d_sig.upload(op->sig), "upload position table");
+    QR_CUDA(op->d_grp.upload(grp), "upload group descriptors");
+    QR_CUDA(op->d_ctab.upload(ctab), "upload class tables");
+    QR_CUDA(op->d_fold.upload(fold), "upload fold groups");
+    op->nfold = (uint32_t)fold.size();
     op->csr_uploaded = true;
     return QR_OK;
 }
@@ -246,11 +300,6 @@ void merge_terms(qr_op *op) {
 
 // GF(2) span of the z differences of one group: basis (pivot = msb, unique)
 // and the coordinates of every term's difference in that basis.
-struct Span {
-    std::vector<uint64_t> basis;
-    std::vector<uint64_t> coord;  // per term
-    bool overflow = false;
-};
 Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
     Span sp;
     const uint64_t z0 = zs[0];
@@ -579,6 +628,7 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         QR_CUDA(pl.blk_r0.upload(r0v), "upload block runs");
         QR_CUDA(pl.run_g0.upload(rg0), "upload runs");
         QR_CUDA(pl.run_key.upload(rkey), "upload run keys");
+        pl.nruns = (uint32_t)rkey.size();
         pl.nsub = (uint32_t)ord.size();
         if (sd.empty()) {
             SubDescC64 z;
@@ -703,7 +753,11 @@ int qr_op_create(int32_t n, uint64_t nterms, const uint64_t *x, const uint64_t *
         delete op;
         return cuda_fail(e, "qr_op_create: no usable CUDA device");
     }
-    prepare_csr_tables(op);
+    int rc = prepare_csr_tables(op);
+    if (rc) {
+        delete op;
+        return rc;
+    }
     e = op->d_err.alloc(sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(op->d_err.p, 0, sizeof(int));
     if (e != cudaSuccess) {
@@ -779,12 +833,15 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, i
     a.N = op->N;
     a.G = op->G;
     a.gx = op->d_gx.as<uint64_t>();
-    a.goff = op->d_goff.as<uint32_t>();
+    a.n = op->n;
+    a.grp = op->d_grp.as<CsrGroup>();
+    a.pmask = op->d_pmask.as<uint64_t>();
+    a.sig = op->d_sig.as<int32_t>();
+    a.fold = op->d_fold.as<uint32_t>();
+    a.nfold = op->nfold;
+    a.ctab = op->d_ctab.as<double2>();
     a.tz = op->d_tz.as<uint64_t>();
     a.tc = op->d_tc.as<double>();
-    a.eoff = op->d_eoff.as<uint32_t>();
-    a.ebit = op->d_ebit.as<uint8_t>();
-    a.esig = op->d_esig.as<int64_t>();
     a.err = op->d_err.as<int>();
     if (mem == QR_MEM_DEVICE) {
         a.indptr = indptr;
@@ -872,6 +929,7 @@ int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates
     a.blk_r0 = pl.blk_r0.as<uint32_t>();
     a.run_g0 = pl.run_g0.as<uint32_t>();
     a.run_key = pl.run_key.as<uint32_t>();
+    a.nruns = pl.nruns;
     if (pl.nblocks == 0) {
         // operator without terms reachable here cannot happen (T >= 1); keep y defined
         QR_CUDA(cudaMemsetAsync(y, 0, bytes, static_cast<cudaStream_t>(stream)), "zero y");

@@ -10,7 +10,9 @@ with every numeric result computed by the sm_103a kernels behind the C ABI
 * ``SparsePauliOp`` (pyqrusty/src/lib.rs:305-433; qrusty/src/lib.rs:345-586)
   with ``to_matrix`` / ``to_matrix_mode`` routed to the GPU CSR builder and
   a matrix-free ``apply`` (H psi on the GPU)
-* ``SpMat`` (pyqrusty/src/lib.rs:33-214): CSR holder with ``export``
+* ``SpMat`` (pyqrusty/src/lib.rs:33-260): CSR holder with ``export``,
+  ``matrixmarket_write / _write_symmetric / _read`` and qrusty's binary
+  ``rawio`` format (qrusty/src/rawio.rs), ".gz" paths compressed
 * ``spmat_dot_densevec`` (pyqrusty/src/lib.rs:476-491): GPU CSR * vector
 * ``csr_matrix`` (pyqrusty/python/pyqrusty/__init__.py:14-17)
 * the eigensolver-loop vector helpers ``axpby`` / ``axpy`` / ``ax``
@@ -18,7 +20,7 @@ with every numeric result computed by the sm_103a kernels behind the C ABI
   (pyqrusty/src/lib.rs:436-469) and ``SpMat.diagonal`` (:118-125), on the GPU
 
 Out of scope here (matrix algebra around the path, not the path):
-MatrixMarket I/O, ``+``/``-``/``scale`` on SpMat, ``a_spmat_p_b_spmat``.
+``+``/``-``/``scale`` on SpMat, ``a_spmat_p_b_spmat``, zero counting.
 """
 from __future__ import annotations
 
@@ -460,6 +462,85 @@ class SpMat:
         self._it = None
         self._dev = None
         return (shape, data, indices, indptr)
+
+    def export_device(self):
+        """``export`` into CUDA tensors: ((rows, cols), data complex128,
+        indices int64, indptr int64) on the current device, reusing the device
+        copy a GPU call already made; the SpMat is left empty."""
+        if self._it is None:
+            raise Exception("cannot export from an already-exported sparse matrix")
+        shape = self._it[0]
+        indptr, indices, data = self._device()
+        self._it = None
+        self._dev = None
+        return (shape, data, indices, indptr)
+
+    # ------------------------------------------------------------ file formats
+    def matrixmarket_write(self, save_path: str) -> None:
+        """MatrixMarket coordinate complex general (pyqrusty/src/lib.rs:216-229);
+        ".gz" paths are gzip-compressed."""
+        self._mm_write(save_path, 0)
+
+    _SYM_MODES = {"": 0, "general": 0, "symmetric": 1, "skew-symmetric": 2, "hermitian": 3}
+
+    def matrixmarket_write_symmetric(self, save_path: str, mode: str = "general") -> None:
+        """Symmetric-storage MatrixMarket (pyqrusty/src/lib.rs:248-260): the
+        lower triangle under a symmetric / skew-symmetric / hermitian header."""
+        if mode not in self._SYM_MODES:
+            raise Exception("matrixmarket_write_symmetric: unrecognized mode %s" % mode)
+        self._mm_write(save_path, self._SYM_MODES[mode])
+
+    def _mm_write(self, path, sym):
+        shape, data, indices, indptr = self._get(
+            "cannot write an already-destroyed sparse matrix")
+        check(_lib.load().qr_mm_write(str(path).encode(), shape[0], shape[1], indptr.ctypes.data,
+                                      indices.ctypes.data, data.ctypes.data, sym,
+                                      _lib.QR_MEM_HOST, None))
+
+    @staticmethod
+    def matrixmarket_read(read_path: str) -> "SpMat":
+        """MatrixMarket coordinate file (any field, any symmetry; ".gz"
+        accepted) to CSR (pyqrusty/src/lib.rs:231-246)."""
+        L = _lib.load()
+        h = C.c_void_p()
+        nr, nc, nz = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        rc = L.qr_mm_open(str(read_path).encode(), C.byref(h), C.byref(nr), C.byref(nc),
+                          C.byref(nz))
+        if rc != 0:
+            raise Exception(_lib.last_error())
+        try:
+            indptr = np.empty(nr.value + 1, dtype=np.uint64)
+            indices = np.empty(nz.value, dtype=np.uint64)
+            data = np.empty(nz.value, dtype=np.complex128)
+            check(L.qr_mm_fetch(h, indptr.ctypes.data, indices.ctypes.data, data.ctypes.data,
+                                _lib.QR_MEM_HOST, None))
+        finally:
+            L.qr_mm_close(h)
+        return SpMat((nr.value, nc.value), data, indices, indptr)
+
+    def rawio_write(self, save_path: str) -> None:
+        """qrusty's binary CSR file (qrusty/src/rawio.rs:128-149)."""
+        shape, data, indices, indptr = self._get(
+            "cannot write an already-destroyed sparse matrix")
+        check(_lib.load().qr_rawio_write(str(save_path).encode(), 0, shape[0], shape[1],
+                                         indptr.ctypes.data, len(indptr), indices.ctypes.data,
+                                         data.ctypes.data, len(data), _lib.QR_MEM_HOST, None))
+
+    @staticmethod
+    def rawio_read(read_path: str) -> "SpMat":
+        """Read qrusty's binary CSR file (qrusty/src/rawio.rs:151-179),
+        either byte order."""
+        L = _lib.load()
+        info = _lib.CsrFileInfo()
+        check(L.qr_rawio_info(str(read_path).encode(), C.byref(info)))
+        if info.storage != 0:
+            raise Exception("rawio_read: CSC storage is not a SpMat")
+        indptr = np.empty(info.indptr_len, dtype=np.uint64)
+        indices = np.empty(info.nnz, dtype=np.uint64)
+        data = np.empty(info.nnz, dtype=np.complex128)
+        check(L.qr_rawio_read(str(read_path).encode(), indptr.ctypes.data, indices.ctypes.data,
+                              data.ctypes.data, _lib.QR_MEM_HOST, None))
+        return SpMat((info.nrows, info.ncols), data, indices, indptr)
 
     def _device(self):
         import torch
