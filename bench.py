@@ -351,6 +351,8 @@ def run_gpu_arm(args, t, desc):
                      "frac": ach64 / hbm, "traffic": traffic,
                      "alg_bytes_per_launch": alg64,
                      "alg_bytes_rule": "(P+1)*2^n*8, P=%d distinct x>>13" % P,
+                     "b_group_bytes": (int(info["ngroups"]) + 1) * N * 8,
+                     "b_group_rule": "(G+1)*2^n*8: one gather pass per distinct x mask",
                      "peak_source": peak_kind},
         "c128": {"value": whole_job_rate(ws, T * N, ms128 / 1e3), "ms_per_step": ms128,
                  "steps": s128,

@@ -100,14 +100,27 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data,
 int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates,
              int32_t adjoint, void *stream);
 
+/* y = alpha * (H psi) + beta * v, fused into the apply kernel's store: the
+ * eigensolver residual H psi - theta psi (alpha = 1, beta = -theta, v = psi)
+ * without a second pass over y.  alpha, beta: host (re, im) doubles.  The
+ * combination is qrusty's axpby (qrusty/src/accel.rs:374-379) applied to
+ * the value qr_apply would store, with num-complex arithmetic (complex128) or
+ * its FP32 form (QR_C64C), so the result equals qr_apply followed by
+ * qr_axpby bit for bit.  v may be y itself; neither may overlap psi. */
+int qr_apply_axpby(qr_op *op, int32_t dtype, const double *alpha, const void *psi,
+                   const double *beta, const void *v, void *y, int32_t nstates, void *stream);
+
 /* Synchronise `stream` and report any error a kernel of this operator
  * recorded on the device (e.g. an expired bounded wait).  The error word is
  * cleared after it is reported. */
 int qr_check(qr_op *op, void *stream);
 
-/* As qr_apply with HOST psi / y: copies psi to the device, applies, copies
- * y back (synchronous).  Device staging buffers are owned by the operator
- * and reused across calls. */
+/* As qr_apply with HOST psi / y (synchronous): copies psi to a device
+ * staging buffer and applies.  When y is page-locked host memory
+ * (cudaHostAlloc / cudaHostRegister) the kernel writes each output tile
+ * straight into it, overlapping the write-back with the computation;
+ * otherwise y goes to a device staging buffer and is copied back.  Staging
+ * buffers are owned by the operator and reused across calls. */
 int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host,
                   int32_t nstates, int32_t adjoint);
 

@@ -29,7 +29,7 @@ EXPORTS = (
     "qr_apply", "qr_check", "qr_apply_host", "qr_csr_spmv", "qr_op_set_coeffs", "qr_vdot",
     "qr_expect", "qr_term_grad", "qr_vdot_noalloc", "qr_batch_create", "qr_batch_destroy",
     "qr_batch_apply", "qr_batch_tile_bits", "qr_axpby", "qr_axpy", "qr_ax", "qr_precond2",
-    "qr_csr_diagonal", "qr_op_diagonal", "qr_rawio_info", "qr_rawio_read", "qr_rawio_write",
+    "qr_csr_diagonal", "qr_op_diagonal", "qr_apply_axpby", "qr_rawio_info", "qr_rawio_read", "qr_rawio_write",
     "qr_mm_write", "qr_mm_open", "qr_mm_fetch", "qr_mm_close", "qr_last_error", "qr_launch_count",
 )
 
@@ -97,6 +97,7 @@ def load(build_if_missing: bool = True):
     L.qr_precond2.argtypes = [i32, u64, vp, vp, vp, C.c_double, vp, vp]
     L.qr_csr_diagonal.argtypes = [u64, u64, vp, vp, vp, vp, vp]
     L.qr_op_diagonal.argtypes = [vp, i32, vp, vp]
+    L.qr_apply_axpby.argtypes = [vp, i32, vp, vp, vp, vp, vp, i32, vp]
     L.qr_rawio_info.argtypes = [C.c_char_p, C.POINTER(CsrFileInfo)]
     L.qr_rawio_read.argtypes = [C.c_char_p, vp, vp, vp, i32, vp]
     L.qr_rawio_write.argtypes = [C.c_char_p, u64, u64, u64, vp, u64, vp, vp, u64, i32, vp]

@@ -298,7 +298,16 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
                 } else {
                     o = acc[m];
                 }
-                yo[t + threads * (uint32_t)m] = o;
+                const uint32_t rl = t + threads * (uint32_t)m;
+                if constexpr (sizeof(Real) == 8) {
+                    if (a.v != nullptr) {  // fused y = alpha (H psi) + beta v
+                        const double2 vv = static_cast<const double2 *>(a.v)[st * a.N + (q << a.b) + rl];
+                        const double2 r = cx_axpby(a.ar, a.ai, make_double2(o.re, o.im), a.br, a.bi, vv);
+                        o.re = r.x;
+                        o.im = r.y;
+                    }
+                }
+                yo[rl] = o;
             }
         }
 
@@ -597,11 +606,16 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
         }
         if (last) {
             float2 *yo = y + st * a.N + (q << a.b);
+            const float2 *vo = a.v ? static_cast<const float2 *>(a.v) + st * a.N + (q << a.b)
+                                   : nullptr;
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
                 const float2 lm = mylo[m * threads];
-                yo[t + threads * (uint32_t)m] =
-                    make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
+                const uint32_t rl = t + threads * (uint32_t)m;
+                float2 o = make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
+                if (vo)  // fused y = alpha (H psi) + beta v, in FP32
+                    o = cx_axpby((float)a.ar, (float)a.ai, o, (float)a.br, (float)a.bi, vo[rl]);
+                yo[rl] = o;
             }
         }
 
@@ -661,32 +675,36 @@ template <int AMPS, int ZM, bool XM>
 __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                         const unsigned char *sm, uint32_t soff,
                                         const float4 *s_tab, const uint2 *tdesc, uint32_t g0,
-                                        uint32_t g1, uint32_t t, uint32_t tmask, int tb) {
+                                        uint32_t g1, uint32_t t, uint32_t t8) {
     for (uint32_t g = g0; g < g1; ++g) {
         const uint2 d = tdesc[g];
+        // thread parities against the three masks, skipped (warp-uniformly)
+        // when the factor does not depend on the thread
         uint32_t u = 0, sg = 0;
-        if (d.x >> 24) {
+        if (d.x >> 31) {
             sg = (uint32_t)__popc(t & (d.y & 0x3ffu)) & 1u;
             u = ((uint32_t)__popc(t & ((d.y >> 10) & 0x3ffu)) & 1u) |
                 (((uint32_t)__popc(t & ((d.y >> 20) & 0x3ffu)) & 1u) << 1);
         }
-        float4 T = s_tab[g * 4 + u];
-        if (sg) {
-            T.x = -T.x;
-            T.y = -T.y;
-            T.z = -T.z;
-            T.w = -T.w;
-        }
-        const uint32_t lo = d.x & 0xffffu;
-        const uint32_t off = soff | ((t ^ (lo & tmask)) << 3) | ((lo >> tb) << kMsh);
+        const float4 T = s_tab[g * 4 + u];
+        // thread sign (-1)^sg on both factor pairs: one packed multiply each
+        const float sv = __uint_as_float(0x3f800000u | (sg << 31));
+        const float2 ap = __fmul2_rn(make_float2(T.x, T.y), make_float2(sv, sv));
+        const float2 bp = __fmul2_rn(make_float2(T.z, T.w), make_float2(sv, sv));
+        // partner byte offset: the XOR part (thread and register bits of lo) is
+        // precomputed per sub-group; the stage offset occupies higher bits
+        const uint32_t off = soff | (t8 ^ (d.x & 0x7fffu));
         float2 p[AMPS];
 #pragma unroll
         for (int m = 0; m < AMPS; ++m) {
             const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
             p[m] = *reinterpret_cast<const float2 *>(sm + o);
         }
-        const float2 ap = make_float2(T.x, T.y), bp = make_float2(T.z, T.w);
-        const float2 an = make_float2(-T.x, -T.y), bn = make_float2(-T.z, -T.w);
+        float2 an = ap, bn = bp;
+        if constexpr (ZM != 0) {
+            an = __fmul2_rn(ap, make_float2(-1.f, -1.f));
+            bn = __fmul2_rn(bp, make_float2(-1.f, -1.f));
+        }
 #pragma unroll
         for (int m = 0; m < AMPS; ++m) {
             const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
@@ -701,12 +719,11 @@ __device__ __forceinline__ void run_tab_dispatch(uint32_t key, float2 (&A)[AMPS]
                                                  float2 (&B)[AMPS], const unsigned char *sm,
                                                  uint32_t soff, const float4 *s_tab,
                                                  const uint2 *tdesc, uint32_t g0, uint32_t g1,
-                                                 uint32_t t, uint32_t tmask, int tb) {
+                                                 uint32_t t, uint32_t t8) {
 #define QR_RUN_CASE(k)                                                                    \
     case k:                                                                               \
         if constexpr ((k & 15) < AMPS)                                                    \
-            run_tab<AMPS, (k & 15), (k >> 4) != 0>(A, B, sm, soff, s_tab, tdesc, g0, g1, t, \
-                                                    tmask, tb);                           \
+            run_tab<AMPS, (k & 15), (k >> 4) != 0>(A, B, sm, soff, s_tab, tdesc, g0, g1, t, t8); \
         break;
     switch (key) {
         QR_RUN_CASE(0) QR_RUN_CASE(1) QR_RUN_CASE(2) QR_RUN_CASE(3)
@@ -752,8 +769,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
     float2 *y = static_cast<float2 *>(a.y);
     const float2 *diag = static_cast<const float2 *>(a.diag);
     const uint32_t nb = a.nblocks;
-    const uint32_t tmask = threads - 1;
-    const int tb = a.tb;
+    const uint32_t t8 = t << 3;
 
     const uint64_t first = blockIdx.x;
     const uint64_t my_items =
@@ -841,7 +857,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
         for (uint32_t r = s_blk[j]; r < r1; ++r) {
             const uint32_t rn = s_run[r + 1];
             run_tab_dispatch<AMPS>(rw >> 16, A, B, smem_raw, soff, s_tab, tdesc, rw & 0xffffu,
-                                   rn & 0xffffu, t, tmask, tb);
+                                   rn & 0xffffu, t, t8);
             rw = rn;
         }
 
@@ -860,11 +876,16 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
         }
         if (last) {
             float2 *yo = y + st * a.N + (q << a.b);
+            const float2 *vo = a.v ? static_cast<const float2 *>(a.v) + st * a.N + (q << a.b)
+                                   : nullptr;
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
                 const float2 lm = mylo[m * threads];
-                yo[t + threads * (uint32_t)m] =
-                    make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
+                const uint32_t rl = t + threads * (uint32_t)m;
+                float2 o = make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
+                if (vo)  // fused y = alpha (H psi) + beta v, in FP32
+                    o = cx_axpby((float)a.ar, (float)a.ai, o, (float)a.br, (float)a.bi, vo[rl]);
+                yo[rl] = o;
             }
         }
 

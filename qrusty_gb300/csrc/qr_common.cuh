@@ -73,7 +73,7 @@ struct ApplyArgs {
     const SubDescC64 *sub;
     uint32_t nsub;
     // per-tile-table kernel: per sub-group an 8-byte thread descriptor
-    // {lo | key << 16 | tvar << 24, z0_t | beta0_t << 10 | beta1_t << 20} and
+    // {partner byte-offset XOR | tvar << 31, z0_t | beta0_t << 10 | beta1_t << 20} and
     // its TileDataC64; sub-groups of a block in runs of equal key
     const uint2 *tdesc;
     const TileDataC64 *tdata;
@@ -81,6 +81,9 @@ struct ApplyArgs {
     const uint32_t *run_g0;   // sub-groups of run r: [run_g0[r], run_g0[r+1])
     const uint32_t *run_key;  // key = zm | xm << 4
     uint32_t nruns;
+    // fused epilogue y = alpha * (H psi) + beta * v when v != nullptr
+    const void *v;
+    double ar, ai, br, bi;
 };
 
 
@@ -115,6 +118,26 @@ cudaError_t launch_batch_c64c(const BatchArgs &a, int nsm, cudaStream_t st);
 
 // Device error codes written to the error word.
 enum : int { kErrNone = 0, kErrMbarTimeout = 1, kErrCsrPos = 2 };
+
+// num-complex 0.4 arithmetic with every operation an explicit round-to-nearest
+// intrinsic (no FMA contraction): a * b = (ar br - ai bi, ar bi + ai br).
+// a*x + b*y is the axpby of qrusty/src/accel.rs:374-379.
+__device__ __forceinline__ double2 cx_axpby(double ar, double ai, double2 x, double br, double bi,
+                                            double2 y) {
+    const double ur = __dsub_rn(__dmul_rn(ar, x.x), __dmul_rn(ai, x.y));
+    const double ui = __dadd_rn(__dmul_rn(ar, x.y), __dmul_rn(ai, x.x));
+    const double vr = __dsub_rn(__dmul_rn(br, y.x), __dmul_rn(bi, y.y));
+    const double vi = __dadd_rn(__dmul_rn(br, y.y), __dmul_rn(bi, y.x));
+    return make_double2(__dadd_rn(ur, vr), __dadd_rn(ui, vi));
+}
+__device__ __forceinline__ float2 cx_axpby(float ar, float ai, float2 x, float br, float bi,
+                                           float2 y) {
+    const float ur = __fsub_rn(__fmul_rn(ar, x.x), __fmul_rn(ai, x.y));
+    const float ui = __fadd_rn(__fmul_rn(ar, x.y), __fmul_rn(ai, x.x));
+    const float vr = __fsub_rn(__fmul_rn(br, y.x), __fmul_rn(bi, y.y));
+    const float vi = __fadd_rn(__fmul_rn(br, y.y), __fmul_rn(bi, y.x));
+    return make_float2(__fadd_rn(ur, vr), __fadd_rn(ui, vi));
+}
 
 // log2 of the thread count of the compensated-complex64 kernels: the
 // single-operator kernels and the batched kernel (see qr_apply.cu).

@@ -31,13 +31,27 @@ __global__ void __launch_bounds__(256) csr_indptr_kernel(uint64_t N, uint64_t G,
         indptr[r] = r * G;
 }
 
-// Rank of column r ^ x_g in row r: g + sum of sigma_{g,b} over the bits b
-// of r in the group's position mask (sig: the group's row of the table).
-__device__ __forceinline__ int32_t csr_pos(uint64_t r, uint32_t g, uint64_t pm,
-                                           const int32_t *sig) {
-    int32_t pos = (int32_t)g;
-    for (uint64_t m = r & pm; m; m &= m - 1) pos += sig[__ffsll((long long)m) - 1];
-    return pos;
+// Row bits as a 32-bit word when n <= 32 (half the integer work), else 64.
+template <bool WIDE> struct RowT { using T = uint32_t; };
+template <> struct RowT<true> { using T = uint64_t; };
+
+template <typename W>
+__device__ __forceinline__ uint32_t parity(W v) {
+    if constexpr (sizeof(W) == 8) return (uint32_t)__popcll(v) & 1u;
+    else return (uint32_t)__popc(v) & 1u;
+}
+template <typename W>
+__device__ __forceinline__ int lowbit(W v) {
+    if constexpr (sizeof(W) == 8) return __ffsll((long long)v) - 1;
+    else return __ffs((int)v) - 1;
+}
+
+// sum of sigma_b over the set bits b of m (sig: the group's row of the table)
+template <typename W>
+__device__ __forceinline__ int32_t sigma_sum(W m, const int32_t *sig) {
+    int32_t s = 0;
+    for (; m; m &= m - 1) s += sig[lowbit(m)];
+    return s;
 }
 
 __device__ __forceinline__ void csr_store(const CsrArgs &a, uint64_t rr, int32_t pos, uint64_t col,
@@ -52,55 +66,88 @@ __device__ __forceinline__ void csr_store(const CsrArgs &a, uint64_t rr, int32_t
 }
 
 // Class of row r for group d: bit 0 = parity(r & z0), bit j+1 = parity(r & beta_j).
-__device__ __forceinline__ uint32_t csr_class(const CsrGroup &d, uint64_t r) {
-    uint32_t c = (uint32_t)__popcll(r & d.z0) & 1u;
+template <typename W>
+__device__ __forceinline__ uint32_t csr_class(const CsrGroup &d, W r) {
+    uint32_t c = parity<W>(r & (W)d.z0);
 #pragma unroll
     for (int j = 0; j < kCsrMaxRank; ++j)
-        if ((uint32_t)j < d.d) c |= ((uint32_t)__popcll(r & d.beta[j]) & 1u) << (j + 1);
+        if ((uint32_t)j < d.d) c |= parity<W>(r & (W)d.beta[j]) << (j + 1);
     return c;
 }
 
 constexpr int kCsrThreads = 256;
 constexpr uint32_t kCsrSmemSig = 12288;  // sigma entries staged in shared memory (48 KB)
+constexpr size_t kCsrLutBytes = 64u * 1024u;
 
-// Class-table groups.  G <= 256: thread t owns group g = t % G of row t / G
-// in every pass of 256 / G consecutive rows, so its descriptor and position
-// mask stay in registers and no per-entry division is needed.  G > 256: one
-// row per pass, threads stride the groups.  Fold-mode groups are left to
-// csr_fold_kernel, so no lane of a warp waits on another's long fold.
+// Low-bit width of the per-group position lookup table: G x (2^L + 1)
+// 32-bit entries (rows padded by one word so lanes on consecutive groups hit
+// distinct banks) within 64 KB.  L <= 8, so 256-row launches stay aligned.
+__host__ __device__ inline int csr_lut_bits(uint32_t G) {
+    int L = 8;
+    while (L > 1 && (size_t)G * ((1u << L) + 1) * 4u > kCsrLutBytes) --L;
+    return L;
+}
+
+// Class-table groups.  G <= 256: blocks take chunks of 2^L rows; in a chunk,
+// thread t owns group g = t % G of rows t / G, t / G + 256 / G, ..., so its
+// descriptor and position mask stay in registers; the position terms of the
+// row bits above the chunk are summed once per chunk and the low L bits come
+// from a shared-memory table built per block.  G > 256: one row per pass,
+// threads stride the groups.  Fold-mode groups are left to csr_fold_kernel,
+// so no lane of a warp waits on another's long fold.
+template <bool WIDE>
 __global__ void __launch_bounds__(kCsrThreads) csr_fill_kernel(const CsrArgs a) {
-    extern __shared__ int32_t s_sig[];
+    using W = typename RowT<WIDE>::T;
+    extern __shared__ int32_t s_dyn[];
     const uint32_t G = (uint32_t)a.G;
-    const uint64_t nsig = (uint64_t)G * (uint32_t)a.n;
-    const bool staged = nsig <= kCsrSmemSig;
-    if (staged)
-        for (uint32_t i = threadIdx.x; i < nsig; i += kCsrThreads) s_sig[i] = a.sig[i];
-    __syncthreads();
-    const int32_t *sig = staged ? s_sig : a.sig;
     if (G <= (uint32_t)kCsrThreads) {
+        const int L = csr_lut_bits(G);
+        const uint32_t lsz = (1u << L) + 1;  // padded row
+        for (uint32_t i = threadIdx.x; i < G * lsz; i += kCsrThreads) {
+            const uint32_t g = i / lsz, v = i - g * lsz;
+            const W pm = (W)a.pmask[g] & (((W)1 << L) - 1) & (W)v;
+            s_dyn[i] = v < (1u << L) ? sigma_sum<W>(pm, a.sig + (size_t)g * (uint32_t)a.n) : 0;
+        }
+        __syncthreads();
         const uint32_t rpp = kCsrThreads / G;
         const uint32_t t = threadIdx.x;
         if (t >= rpp * G) return;  // no barrier follows
         const uint32_t rs = t / G, g = t - rs * G;
         const CsrGroup d = a.grp[g];
         if (d.d == kCsrFold) return;
-        const uint64_t xg = a.gx[g], pm = a.pmask[g];
-        const int32_t *sg = sig + (size_t)g * (uint32_t)a.n;
-        const uint64_t npass = (a.nrows + rpp - 1) / rpp;
-        for (uint64_t p = blockIdx.x; p < npass; p += gridDim.x) {
-            const uint64_t rr = p * rpp + rs;
-            if (rr >= a.nrows) break;
-            const uint64_t r = a.row0 + rr;
-            csr_store(a, rr, csr_pos(r, g, pm, sg), r ^ xg, a.ctab[d.tab + csr_class(d, r)]);
+        const W xg = (W)a.gx[g], pm = (W)a.pmask[g];
+        const W lomask = ((W)1 << L) - 1;
+        const int32_t *sg = a.sig + (size_t)g * (uint32_t)a.n;
+        const int32_t *lut = s_dyn + g * lsz;
+        const double2 *tab = a.ctab + d.tab;
+        const uint64_t nchunk = (a.nrows + lomask) >> L;
+        for (uint64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+            const uint64_t rr0 = ch << L;
+            const W base = (W)(a.row0 + rr0);
+            const int32_t phi = (int32_t)g + sigma_sum<W>(base & pm & ~lomask, sg);
+            const uint64_t rend = min(rr0 + ((uint64_t)1 << L), a.nrows);
+            for (uint64_t rr = rr0 + rs; rr < rend; rr += rpp) {
+                const W r = (W)(a.row0 + rr);
+                csr_store(a, rr, phi + lut[(uint32_t)(r & lomask)], (uint64_t)(r ^ xg),
+                          tab[csr_class<W>(d, r)]);
+            }
         }
     } else {
+        const uint64_t nsig = (uint64_t)G * (uint32_t)a.n;
+        const bool staged = nsig <= kCsrSmemSig;
+        if (staged)
+            for (uint32_t i = threadIdx.x; i < nsig; i += kCsrThreads) s_dyn[i] = a.sig[i];
+        __syncthreads();
+        const int32_t *sig = staged ? s_dyn : a.sig;
         for (uint64_t rr = blockIdx.x; rr < a.nrows; rr += gridDim.x) {
-            const uint64_t r = a.row0 + rr;
+            const W r = (W)(a.row0 + rr);
             for (uint32_t g = threadIdx.x; g < G; g += kCsrThreads) {
                 const CsrGroup d = a.grp[g];
                 if (d.d == kCsrFold) continue;
-                const int32_t pos = csr_pos(r, g, a.pmask[g], sig + (size_t)g * (uint32_t)a.n);
-                csr_store(a, rr, pos, r ^ a.gx[g], a.ctab[d.tab + csr_class(d, r)]);
+                const int32_t pos = (int32_t)g + sigma_sum<W>(r & (W)a.pmask[g],
+                                                              sig + (size_t)g * (uint32_t)a.n);
+                csr_store(a, rr, pos, (uint64_t)(r ^ (W)a.gx[g]),
+                          a.ctab[d.tab + csr_class<W>(d, r)]);
             }
         }
     }
@@ -127,7 +174,8 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fold_kernel(const CsrArgs a) 
                 vr = __dadd_rn(vr, neg ? -a.tc[2 * k] : a.tc[2 * k]);
                 vi = __dadd_rn(vi, neg ? -a.tc[2 * k + 1] : a.tc[2 * k + 1]);
             }
-            csr_store(a, rr, csr_pos(r, g, pm, sg), r ^ xg, make_double2(vr, vi));
+            csr_store(a, rr, (int32_t)g + sigma_sum<uint64_t>(r & pm, sg), r ^ xg,
+                      make_double2(vr, vi));
         }
     }
 }
@@ -142,12 +190,23 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
         if (e != cudaSuccess) return e;
     }
     if (a.nrows == 0 || a.G == 0) return cudaSuccess;
-    const uint64_t rpp = a.G <= (uint64_t)kCsrThreads ? (uint64_t)kCsrThreads / a.G : 1;
-    uint64_t g = (a.nrows + rpp - 1) / rpp;
+    size_t smem;
+    uint64_t g;
+    if (a.G <= (uint64_t)kCsrThreads) {
+        const int L = csr_lut_bits((uint32_t)a.G);
+        g = (a.nrows + (1u << L) - 1) >> L;
+        smem = (size_t)a.G * ((1u << L) + 1) * sizeof(int32_t);
+    } else {
+        g = a.nrows;
+        const uint64_t nsig = a.G * (uint64_t)a.n;
+        smem = nsig <= kCsrSmemSig ? (size_t)nsig * sizeof(int32_t) : 0;
+    }
     if (g > (uint64_t)nsm * 8) g = (uint64_t)nsm * 8;
-    const uint64_t nsig = a.G * (uint64_t)a.n;
-    const size_t smem = nsig <= kCsrSmemSig ? (size_t)nsig * sizeof(int32_t) : 0;
-    csr_fill_kernel<<<(unsigned)g, kCsrThreads, smem, st>>>(a);
+    auto kern = a.n > 32 ? csr_fill_kernel<true> : csr_fill_kernel<false>;
+    cudaError_t e0 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kCsrLutBytes + 4096);
+    if (e0 != cudaSuccess) return e0;
+    kern<<<(unsigned)g, kCsrThreads, smem, st>>>(a);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || a.nfold == 0) return e;

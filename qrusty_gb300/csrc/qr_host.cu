@@ -593,9 +593,12 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
             const uint32_t zt = (uint32_t)(sg.z0 & tmask_t), bt0 = (uint32_t)(b0 & tmask_t),
                            bt1 = (uint32_t)(b1 & tmask_t);
             const uint32_t tvar = (zt | bt0 | bt1) != 0 ? 1u : 0u;
-            const uint32_t key = runkey(sg) & 31u;
-            td.push_back(make_uint2(sg.lo | (key << 16) | (tvar << 24),
-                                    zt | (bt0 << 10) | (bt1 << 20)));
+            // byte-offset XOR of the partner within the tile: thread bits of lo
+            // (x 8 bytes) and register bits of lo (x 8 x threads); needs
+            // threads == 1 << kC64ThreadBits whenever lo has register bits
+            const uint32_t lt = (uint32_t)(sg.lo & tmask_t), lm = sg.lo >> pl.tb;
+            const uint32_t dx = (lt << 3) | (lm << (pl.tb + 3));
+            td.push_back(make_uint2(dx | (tvar << 31), zt | (bt0 << 10) | (bt1 << 20)));
             TileDataC64 d;
             memset(&d, 0, sizeof(d));
             d.z0h = sg.z0 >> pl.b;
@@ -855,7 +858,8 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, i
     // host destination: build in row chunks of <= ~1 GiB on the device
     const uint64_t per_row = op->G * 24;
     uint64_t rows = (1ull << 30) / (per_row ? per_row : 1);
-    if (rows == 0) rows = 1;
+    // whole 256-row chunks, so that every launch starts on a chunk boundary
+    rows = rows < 256 ? 256 : rows & ~255ull;
     if (rows > op->N) rows = op->N;
     DevBuf d_ptr, d_idx, d_dat;
     QR_CUDA(d_ptr.alloc((op->N + 1) * sizeof(uint64_t)), "alloc indptr staging");
@@ -883,26 +887,35 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, i
     return check_kernel_error(op);
 }
 
-int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates, int32_t adjoint,
-             void *stream) {
-    if (!op || !psi || !y) return fail(QR_EINVAL, "qr_apply: null argument");
+static int apply_impl(const char *name, qr_op *op, int32_t dtype, const void *psi, void *y,
+                      int32_t nstates, int32_t adjoint, void *stream, const void *v,
+                      const double *alpha, const double *beta) {
+    if (!op || !psi || !y) return fail(QR_EINVAL, "%s: null argument", name);
     if (dtype != QR_C128 && dtype != QR_C64C)
-        return fail(QR_EINVAL, "qr_apply: dtype must be QR_C128 or QR_C64C");
-    if (nstates < 1) return fail(QR_EINVAL, "qr_apply: nstates=%d < 1", nstates);
-    if (adjoint != 0 && adjoint != 1) return fail(QR_EINVAL, "qr_apply: adjoint must be 0 or 1");
-    if (op->n > 40) return fail(QR_EINVAL, "qr_apply: n=%d too large for a state vector", op->n);
+        return fail(QR_EINVAL, "%s: dtype must be QR_C128 or QR_C64C", name);
+    if (nstates < 1) return fail(QR_EINVAL, "%s: nstates=%d < 1", name, nstates);
+    if (adjoint != 0 && adjoint != 1) return fail(QR_EINVAL, "%s: adjoint must be 0 or 1", name);
+    if (op->n > 40) return fail(QR_EINVAL, "%s: n=%d too large for a state vector", name, op->n);
     const size_t esz = dtype == QR_C128 ? 16 : 8;
     const uint64_t bytes = (uint64_t)nstates * op->N * esz;
     const char *pb = static_cast<const char *>(psi), *yb = static_cast<const char *>(y);
-    if (pb < yb + bytes && yb < pb + bytes) return fail(QR_EINVAL, "qr_apply: psi and y overlap");
+    if (pb < yb + bytes && yb < pb + bytes) return fail(QR_EINVAL, "%s: psi and y overlap", name);
     if ((reinterpret_cast<uintptr_t>(psi) | reinterpret_cast<uintptr_t>(y)) & 15)
-        return fail(QR_EINVAL, "qr_apply: psi and y must be 16-byte aligned");
+        return fail(QR_EINVAL, "%s: psi and y must be 16-byte aligned", name);
+    if (v) {
+        // v may be y itself (each element is read before it is written, by
+        // the same thread) but must not overlap psi, which other tiles read
+        const char *vb = static_cast<const char *>(v);
+        if (vb < pb + bytes && pb < vb + bytes) return fail(QR_EINVAL, "%s: psi and v overlap", name);
+        if (vb != yb && vb < yb + bytes && yb < vb + bytes)
+            return fail(QR_EINVAL, "%s: v overlaps y without being y", name);
+    }
     int rc = check_device(op);
     if (rc) return rc;
     rc = build_plan(op, dtype, adjoint);
     if (rc) return rc;
     const Plan &pl = op->plans[dtype][adjoint];
-    ApplyArgs a;
+    ApplyArgs a{};
     a.psi = psi;
     a.y = y;
     a.N = op->N;
@@ -930,7 +943,14 @@ int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates
     a.run_g0 = pl.run_g0.as<uint32_t>();
     a.run_key = pl.run_key.as<uint32_t>();
     a.nruns = pl.nruns;
-    if (pl.nblocks == 0) {
+    a.v = v;
+    if (v) {
+        a.ar = alpha[0];
+        a.ai = alpha[1];
+        a.br = beta[0];
+        a.bi = beta[1];
+    }
+    if (pl.nblocks == 0 && !v) {
         // operator without terms reachable here cannot happen (T >= 1); keep y defined
         QR_CUDA(cudaMemsetAsync(y, 0, bytes, static_cast<cudaStream_t>(stream)), "zero y");
         return QR_OK;
@@ -939,6 +959,18 @@ int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates
                          static_cast<cudaStream_t>(stream)),
             "apply launch");
     return QR_OK;
+}
+
+int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates, int32_t adjoint,
+             void *stream) {
+    return apply_impl("qr_apply", op, dtype, psi, y, nstates, adjoint, stream, nullptr, nullptr,
+                      nullptr);
+}
+
+int qr_apply_axpby(qr_op *op, int32_t dtype, const double *alpha, const void *psi,
+                   const double *beta, const void *v, void *y, int32_t nstates, void *stream) {
+    if (!alpha || !beta || !v) return fail(QR_EINVAL, "qr_apply_axpby: null argument");
+    return apply_impl("qr_apply_axpby", op, dtype, psi, y, nstates, 0, stream, v, alpha, beta);
 }
 
 int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host, int32_t nstates,
@@ -954,13 +986,26 @@ int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host, 
     if (!op->hstream) QR_CUDA(cudaStreamCreateWithFlags(&op->hstream, cudaStreamNonBlocking),
                               "create stream");
     if (op->stage_in.bytes < bytes) QR_CUDA(op->stage_in.alloc(bytes), "alloc psi staging");
-    if (op->stage_out.bytes < bytes) QR_CUDA(op->stage_out.alloc(bytes), "alloc y staging");
+    // Pinned (page-locked, mapped) y: the kernel stores each finished output
+    // tile straight into host memory, so the write-back overlaps the
+    // computation instead of following it.  Pageable y: device staging + copy.
+    void *y_dev = nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, y_host) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+        at.devicePointer != nullptr)
+        y_dev = at.devicePointer;
+    cudaGetLastError();  // a pageable pointer may leave a benign error behind
+    if (!y_dev && op->stage_out.bytes < bytes)
+        QR_CUDA(op->stage_out.alloc(bytes), "alloc y staging");
     QR_CUDA(cudaMemcpyAsync(op->stage_in.p, psi_host, bytes, cudaMemcpyHostToDevice, op->hstream),
             "copy psi to device");
-    rc = qr_apply(op, dtype, op->stage_in.p, op->stage_out.p, nstates, adjoint, op->hstream);
+    rc = qr_apply(op, dtype, op->stage_in.p, y_dev ? y_dev : op->stage_out.p, nstates, adjoint,
+                  op->hstream);
     if (rc) return rc;
-    QR_CUDA(cudaMemcpyAsync(y_host, op->stage_out.p, bytes, cudaMemcpyDeviceToHost, op->hstream),
-            "copy y to host");
+    if (!y_dev)
+        QR_CUDA(cudaMemcpyAsync(y_host, op->stage_out.p, bytes, cudaMemcpyDeviceToHost,
+                                op->hstream),
+                "copy y to host");
     QR_CUDA(cudaStreamSynchronize(op->hstream), "apply_host sync");
     return check_kernel_error(op);
 }

@@ -291,6 +291,22 @@ class PauliOperator:
                                        ns, out.data_ptr(), st))
         return out
 
+    def apply_axpby(self, psi, v, alpha=1.0, beta=0.0, out=None):
+        """alpha * (H psi) + beta * v in one kernel (CUDA tensors of one dtype;
+        v may be ``out``).  Equals ``axpby(alpha, H.apply(psi), beta, v)``
+        bit for bit."""
+        import torch
+        N = 1 << self.n
+        p, vv = psi.contiguous(), v.contiguous()
+        if p.dtype != vv.dtype or p.numel() != vv.numel():
+            raise ValueError("psi and v must have the same dtype and size")
+        y = torch.empty_like(p) if out is None else out
+        st = torch.cuda.current_stream(p.device).cuda_stream
+        check(_lib.load().qr_apply_axpby(self._h, self._dtype_of(p), _scalar2(alpha), p.data_ptr(),
+                                         _scalar2(beta), vv.data_ptr(), y.data_ptr(),
+                                         p.numel() // N, st))
+        return y
+
     def diagonal(self, dtype=None, device=None):
         """Diagonal of H (2^n entries) without building the CSR: for
         complex128 equal bit for bit to the diagonal of ``csr_device()``."""

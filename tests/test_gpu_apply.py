@@ -149,6 +149,29 @@ def test_host_entry_matches_device(cuda):
     assert np.array_equal(yh64, yd64)
 
 
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_host_entry_pinned_output(cuda, dtype):
+    """Page-locked y: the kernel writes the result straight into host memory
+    (no staging copy); same bits as the device entry, two states, both the
+    operator and its adjoint, and psi and y the same buffer."""
+    import torch
+    t = W.cfg2(n=14)
+    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
+    rng = np.random.default_rng(9)
+    psi = W.random_state(rng, 1 << t.n, nstates=2).astype(dtype).reshape(-1)
+    tdt = torch.complex128 if dtype == np.complex128 else torch.complex64
+    h_in = torch.from_numpy(psi.copy()).pin_memory()
+    h_out = torch.empty_like(h_in).pin_memory()
+    for adj in (False, True):
+        yd = op.apply(torch.from_numpy(psi).to(cuda), adjoint=adj).cpu().numpy()
+        h_out.fill_(float("nan"))
+        op.apply(h_in.numpy(), out=h_out.numpy(), adjoint=adj)
+        assert h_out.dtype == tdt and np.array_equal(h_out.numpy(), yd)
+    inplace = h_in.clone().pin_memory()
+    op.apply(inplace.numpy(), out=inplace.numpy())
+    assert np.array_equal(inplace.numpy(), op.apply(torch.from_numpy(psi).to(cuda)).cpu().numpy())
+
+
 def test_spmat_dot_densevec(cuda, oracle, golden):  # test_it.py:218-230
     m = Pauli("IX").to_matrix()
     x = np.array([1.0 + 2j, 2.0 + 3j, 3.0 + 4j, 4.0 + 5j])

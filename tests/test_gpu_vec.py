@@ -160,3 +160,27 @@ def test_argument_errors(cuda):
     av = (C.c_double * 2)(1.0, 0.0)
     rc = _lib.load().qr_ax(7, 4, av, None, None, None)
     assert rc == _lib.QR_EINVAL
+
+
+@pytest.mark.parametrize("which", ["jw14", "chain12"])
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_fused_apply_axpby(cuda, which, dtype):
+    """alpha (H psi) + beta v fused into the apply kernel equals apply then
+    axpby bit for bit; v may be the output buffer (the residual update)."""
+    import torch
+    t = W.cfg2(n=14) if which == "jw14" else W.cfg1(with_state=False, n=12)[0]
+    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
+    tdt = torch.complex128 if dtype == "c128" else torch.complex64
+    g = torch.Generator(device=cuda).manual_seed(5)
+    N = 1 << t.n
+    psi = torch.randn(2 * N, dtype=tdt, device=cuda, generator=g)
+    v = torch.randn(2 * N, dtype=tdt, device=cuda, generator=g)
+    a, b = 1.0 - 0.25j, -0.8125 + 0.5j
+    want = axpby(a, op.apply(psi), b, v)
+    got = op.apply_axpby(psi, v, a, b)
+    assert torch.equal(torch.view_as_real(got), torch.view_as_real(want))
+    inplace = v.clone()
+    op.apply_axpby(psi, inplace, a, b, out=inplace)
+    assert torch.equal(torch.view_as_real(inplace), torch.view_as_real(want))
+    with pytest.raises(_lib.QrError, match="psi and v overlap"):
+        op.apply_axpby(psi, psi, a, b)
