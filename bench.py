@@ -31,6 +31,8 @@ Secondary workloads (--workload, one JSON line each, 1 GPU):
           complex128 / complex64 elements: GB/s against the HBM peak.
   csr     device CSR build (indptr, indices, data) of the chain at n = 22:
           bytes written per second, and the oracle's CPU build beside it.
+  spmv    CSR * vector (qr_csr_spmv) on that matrix: 24 B per stored entry
+          plus the gathered vector reads.
 """
 from __future__ import annotations
 
@@ -356,6 +358,11 @@ def run_gpu_arm(args, t, desc):
                      "peak_source": peak_kind},
         "c128": {"value": whole_job_rate(ws, T * N, ms128 / 1e3), "ms_per_step": ms128,
                  "steps": s128,
+                 # 4 DFMA (8 flops) per amplitude and x group; GB300 FP64 is
+                 # 1.25 TFLOP/s nominal (no measured FP64 peak is recorded)
+                 "fp64_tflops": 8.0 * N * int(info["ngroups"]) / (ms128 / 1e3) / 1e12,
+                 "fp64_frac_of_nominal": 8.0 * N * int(info["ngroups"]) / (ms128 / 1e3)
+                                         / 1.25e15,
                  "hbm_achieved_gbs": ach128, "hbm_frac": ach128 / hbm},
         "speedup_c64c_vs_c128": ms128 / ms64,
         "rel_err": {"c64c_vs_c128_full": rel64},
@@ -492,13 +499,31 @@ def run_grad(args):
 
     ms = _events_time(step, args.steps, args.warmup, stream)
     N = 1 << t.n
+    # where a step goes: coefficient update (plans rebuilt), forward, adjoint,
+    # per-term inner products
+    cc = t.coeff.real.astype(np.complex128)
+    reps = 5
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(reps):
+        cc[0] += 1e-6
+        op = terms.operator(cc)
+        op.apply(p.detach(), out=torch.empty_like(p))  # plans are rebuilt lazily on first use
+        torch.cuda.synchronize()
+    ms_update_fwd = 1e3 * (time.perf_counter() - t0) / reps
+    pd, gd = p.detach(), wd
+    ms_fwd = _events_time(lambda: op.apply(pd), 10, 3, stream)
+    ms_adj = _events_time(lambda: op.apply(gd, adjoint=True), 10, 3, stream)
+    ms_tg = _events_time(lambda: op.term_grad(pd, gd), 10, 3, stream)
     out = _base_line(
         args, "differentiable H(c)·ψ training step term·amp/s (forward terms x amplitudes / step)",
         t.T * N / (ms / 1e3), UNIT, ms, "c64c forward / adjoint, fp64 reductions",
         {"workload": "n=%d, %d random-letter terms, real c, complex64 psi, L = Re<H(c)psi, w> "
                      "(seed %d)" % (t.n, t.T, W.SEED0 + 4),
          "step": "forward + backward (grad_c, grad_psi) + SGD update of c",
-         "l2": "state 8 MiB: L2-resident"})
+         "l2": "state 8 MiB: L2-resident"},
+        breakdown_ms={"coeff_update_and_forward_incl_plan_rebuild": ms_update_fwd,
+                      "forward_apply": ms_fwd, "adjoint_apply": ms_adj, "term_grad": ms_tg})
     print(json.dumps(out), flush=True)
 
 
@@ -594,6 +619,58 @@ def run_csr(args):
     print(json.dumps(out), flush=True)
 
 
+def run_spmv(args):
+    import torch
+    from qrusty_gb300 import PauliOperator, _lib
+    from qrusty_gb300 import workloads as W
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    n = args.n if args.n != 26 else 22
+    t, _ = W.cfg1(with_state=False, n=n)
+    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
+    ip, ij, d = op.csr_device()
+    N = 1 << n
+    g = torch.Generator(device=dev).manual_seed(3)
+    v = torch.randn(N, dtype=torch.complex128, device=dev, generator=g)
+    y = torch.empty_like(v)
+    L = _lib.load()
+    st = stream.cuda_stream
+    fn = lambda: L.qr_csr_spmv(N, N, ip.data_ptr(), ij.data_ptr(), d.data_ptr(), v.data_ptr(),
+                               y.data_ptr(), st)
+    ms = _events_time(fn, args.steps, args.warmup, stream)
+    nnz = d.numel()
+    alg = 24 * nnz + 8 * (N + 1) + 16 * N  # entries + indptr + y; v gathers hit L2 (64 MiB)
+    ref = op.apply(v)
+    err = float(torch.linalg.vector_norm(y - ref) / torch.linalg.vector_norm(ref))
+    hbm, peak_kind = peaks()
+    gbs = alg / (ms / 1e3) / 1e9
+    out = _base_line(
+        args, "CSR*vector nnz/s (qr_csr_spmv, complex128)", nnz / (ms / 1e3), "nnz/s", ms,
+        "c128",
+        {"workload": "tfim+xxz open chain n=%d, %d terms, CSR built on the device (seed %d)"
+                     % (n, t.T, W.SEED0 + 1), "nnz": int(nnz),
+         "l2": "CSR %d MiB > L2; vector 64 MiB" % ((24 * nnz) >> 20)},
+        roofline={"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                  "frac": gbs / hbm, "traffic": None, "alg_bytes_per_launch": alg,
+                  "alg_bytes_rule": "24 nnz + 8 (N+1) + 16 N", "peak_source": peak_kind},
+        rel_err={"vs_matrix_free_c128": err})
+    if not args.no_cpu:
+        from oracle import oracle as O
+        O.build()
+        rows = min(N, args.cpu_rows * 4)
+        ipc, ijc, dc = O.csr_build(n, t.x, t.z, O.make_params(t.phase, t.coeff), rows=(0, rows))
+        vh = v.cpu().numpy()
+        nth = os.cpu_count() or 1
+        O.spmv(ipc, ijc, dc, vh, nthreads=nth)
+        t0 = time.perf_counter()
+        for _ in range(3):
+            O.spmv(ipc, ijc, dc, vh, nthreads=nth)
+        dt = (time.perf_counter() - t0) / 3
+        out["cpu_baseline"] = {"value": len(dc) / dt, "unit": "nnz/s", "cores": nth, "kind": "port",
+                               "sample": "rows [0, %d) of 2^%d, chunks of 1024 rows" % (rows, n)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__,
                                  formatter_class=argparse.RawDescriptionHelpFormatter)
@@ -601,7 +678,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["jw", "chain", "batch", "grad", "vec", "csr"],
+    ap.add_argument("--workload", choices=["jw", "chain", "batch", "grad", "vec", "csr", "spmv"],
                     default="jw")
     ap.add_argument("--qubits", "--n", dest="n", type=int, default=26,
                     help="qubits of the workload (--n is accepted outside torchrun)")
@@ -615,10 +692,11 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and not args.quick:
         raise SystemExit("--warmup must be >= 3")
-    if args.workload in ("batch", "grad", "vec", "csr"):
+    if args.workload in ("batch", "grad", "vec", "csr", "spmv"):
         if args.impl == "reference":
             raise SystemExit("--impl reference measures the headline workloads (jw, chain)")
-        {"batch": run_batch, "grad": run_grad, "vec": run_vec, "csr": run_csr}[args.workload](args)
+        {"batch": run_batch, "grad": run_grad, "vec": run_vec, "csr": run_csr,
+         "spmv": run_spmv}[args.workload](args)
         return
     if args.workload == "chain" and args.n == 26:
         args.n = 22

@@ -106,7 +106,8 @@ int qr_apply(qr_op *op, int32_t dtype, const void *psi, void *y, int32_t nstates
  * combination is qrusty's axpby (qrusty/src/accel.rs:374-379) applied to
  * the value qr_apply would store, with num-complex arithmetic (complex128) or
  * its FP32 form (QR_C64C), so the result equals qr_apply followed by
- * qr_axpby bit for bit.  v may be y itself; neither may overlap psi. */
+ * qr_axpby bit for bit.  v may be psi or y itself (not a shifted view of y);
+ * y must not overlap psi. */
 int qr_apply_axpby(qr_op *op, int32_t dtype, const double *alpha, const void *psi,
                    const double *beta, const void *v, void *y, int32_t nstates, void *stream);
 
@@ -127,7 +128,7 @@ int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host,
 /* y = A v for a CSR matrix given by device arrays (replaces
  * spmat_dot_densevec, qrusty/src/accel.rs:338-370, and its binding
  * pyqrusty/src/lib.rs:476-491).  complex128; each row's products are summed
- * by one warp (lane-strided partial sums, then a butterfly), so the result
+ * by 8 lanes (lane-strided partial sums, then a butterfly), so the result
  * matches a storage-order sum to rounding, not bit for bit.  v has ncols
  * entries; a column index >= ncols is skipped.  indptr must be a valid
  * non-decreasing row-pointer array over data / indices. */

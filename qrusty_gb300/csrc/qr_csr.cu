@@ -126,10 +126,16 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_kernel(const CsrArgs a) 
             const W base = (W)(a.row0 + rr0);
             const int32_t phi = (int32_t)g + sigma_sum<W>(base & pm & ~lomask, sg);
             const uint64_t rend = min(rr0 + ((uint64_t)1 << L), a.nrows);
-            for (uint64_t rr = rr0 + rs; rr < rend; rr += rpp) {
-                const W r = (W)(a.row0 + rr);
-                csr_store(a, rr, phi + lut[(uint32_t)(r & lomask)], (uint64_t)(r ^ xg),
-                          tab[csr_class<W>(d, r)]);
+            // two rows per step: their table reads are in flight together
+            for (uint64_t rr = rr0 + rs; rr < rend; rr += 2 * (uint64_t)rpp) {
+                const uint64_t rr2 = rr + rpp;
+                const W r = (W)(a.row0 + rr), r2 = (W)(a.row0 + rr2);
+                const bool two = rr2 < rend;
+                const double2 v1 = tab[csr_class<W>(d, r)];
+                const double2 v2 = two ? tab[csr_class<W>(d, r2)] : v1;
+                csr_store(a, rr, phi + lut[(uint32_t)(r & lomask)], (uint64_t)(r ^ xg), v1);
+                if (two)
+                    csr_store(a, rr2, phi + lut[(uint32_t)(r2 & lomask)], (uint64_t)(r2 ^ xg), v2);
             }
         }
     } else {
@@ -220,34 +226,55 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-// y = A v, complex128.  One warp per row; lanes stride the row's entries and
-// the partial sums are combined with a butterfly.  Replaces
-// spmat_dot_densevec (qrusty/src/accel.rs:338-370).
+// y = A v, complex128.  S lanes per row: the lanes of a row stride its
+// entries two at a time (independent loads in flight), then combine their
+// partial sums with a butterfly over the S lanes.
+// Replaces spmat_dot_densevec (qrusty/src/accel.rs:338-370).
+template <int S>
 __global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, uint64_t ncols,
-                                                       const uint64_t *indptr,
-                                                       const uint64_t *indices,
-                                                       const double2 *data, const double2 *v,
-                                                       double2 *y) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
-    for (uint64_t r = blockIdx.x * (uint64_t)(blockDim.x / 32) + (threadIdx.x / 32); r < nrows;
-         r += warps) {
+                                                       const uint64_t *__restrict__ indptr,
+                                                       const uint64_t *__restrict__ indices,
+                                                       const double2 *__restrict__ data,
+                                                       const double2 *__restrict__ v,
+                                                       double2 *__restrict__ y) {
+    const uint32_t sl = threadIdx.x & (S - 1);
+    const uint64_t groups = (uint64_t)gridDim.x * (blockDim.x / S);
+    for (uint64_t r = blockIdx.x * (uint64_t)(blockDim.x / S) + (threadIdx.x / S); r < nrows;
+         r += groups) {
         const uint64_t j0 = indptr[r], j1 = indptr[r + 1];
-        double sr = 0.0, si = 0.0;
-        for (uint64_t j = j0 + lane; j < j1; j += 32) {
-            const uint64_t c = indices[j];
-            if (c >= ncols) continue;  // out-of-range column: skipped
-            const double2 d = data[j];
-            const double2 x = v[c];
-            sr = fma(d.x, x.x, fma(-d.y, x.y, sr));
-            si = fma(d.x, x.y, fma(d.y, x.x, si));
+        double sr = 0.0, si = 0.0, tr = 0.0, ti = 0.0;
+        uint64_t j = j0 + sl;
+        for (; j + S < j1; j += 2 * S) {
+            const uint64_t c0 = indices[j], c1 = indices[j + S];
+            const double2 d0 = data[j], d1 = data[j + S];
+            if (c0 < ncols) {
+                const double2 x0 = v[c0];
+                sr = fma(d0.x, x0.x, fma(-d0.y, x0.y, sr));
+                si = fma(d0.x, x0.y, fma(d0.y, x0.x, si));
+            }
+            if (c1 < ncols) {
+                const double2 x1 = v[c1];
+                tr = fma(d1.x, x1.x, fma(-d1.y, x1.y, tr));
+                ti = fma(d1.x, x1.y, fma(d1.y, x1.x, ti));
+            }
         }
+        if (j < j1) {
+            const uint64_t c = indices[j];  // out-of-range columns are skipped
+            if (c < ncols) {
+                const double2 d = data[j];
+                const double2 x = v[c];
+                sr = fma(d.x, x.x, fma(-d.y, x.y, sr));
+                si = fma(d.x, x.y, fma(d.y, x.x, si));
+            }
+        }
+        sr += tr;
+        si += ti;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            sr += __shfl_xor_sync(0xffffffffu, sr, o);
-            si += __shfl_xor_sync(0xffffffffu, si, o);
+        for (int o = S / 2; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o, S);
+            si += __shfl_xor_sync(0xffffffffu, si, o, S);
         }
-        if (lane == 0) y[r] = make_double2(sr, si);
+        if (sl == 0) y[r] = make_double2(sr, si);
     }
 }
 
@@ -255,12 +282,17 @@ cudaError_t launch_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indp
                             const uint64_t *indices, const double *data, const double *v,
                             double *y, int nsm, cudaStream_t st) {
     if (nrows == 0) return cudaSuccess;
-    uint64_t g = (nrows + 7) / 8;
-    if (g > (uint64_t)nsm * 32) g = (uint64_t)nsm * 32;
-    csr_spmv_kernel<<<(unsigned)g, 256, 0, st>>>(nrows, ncols, indptr, indices,
-                                                 reinterpret_cast<const double2 *>(data),
-                                                 reinterpret_cast<const double2 *>(v),
-                                                 reinterpret_cast<double2 *>(y));
+    // 8 lanes per row: rows of a Pauli-sum CSR hold G entries (tens to a few
+    // hundred), about 6 per lane at G = 44; no host read of nnz, so the call
+    // stays asynchronous
+    constexpr int S = 8;
+    const uint64_t rows_per_block = 256 / S;
+    uint64_t g = (nrows + rows_per_block - 1) / rows_per_block;
+    if (g > (uint64_t)nsm * 16) g = (uint64_t)nsm * 16;
+    csr_spmv_kernel<S><<<(unsigned)g, 256, 0, st>>>(nrows, ncols, indptr, indices,
+                                                    reinterpret_cast<const double2 *>(data),
+                                                    reinterpret_cast<const double2 *>(v),
+                                                    reinterpret_cast<double2 *>(y));
     count_launch();
     return cudaGetLastError();
 }

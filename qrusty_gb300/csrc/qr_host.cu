@@ -55,9 +55,12 @@ struct cd {
 };
 
 // Device buffer with RAII release.
+// Device buffer that keeps its allocation when refilled with no more bytes
+// than it holds (plan rebuilds after a coefficient update reuse it instead of
+// a cudaFree / cudaMalloc pair, which would synchronise the device).
 struct DevBuf {
     void *p = nullptr;
-    size_t bytes = 0;
+    size_t bytes = 0, cap = 0;
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
@@ -65,13 +68,17 @@ struct DevBuf {
     void release() {
         if (p) cudaFree(p);
         p = nullptr;
-        bytes = 0;
+        bytes = cap = 0;
     }
     cudaError_t alloc(size_t b) {
-        release();
         if (b == 0) b = 16;
+        if (p && b <= cap) {
+            bytes = b;
+            return cudaSuccess;
+        }
+        release();
         cudaError_t e = cudaMalloc(&p, b);
-        if (e == cudaSuccess) bytes = b;
+        if (e == cudaSuccess) bytes = cap = b;
         else p = nullptr;
         return e;
     }
@@ -903,12 +910,13 @@ static int apply_impl(const char *name, qr_op *op, int32_t dtype, const void *ps
     if ((reinterpret_cast<uintptr_t>(psi) | reinterpret_cast<uintptr_t>(y)) & 15)
         return fail(QR_EINVAL, "%s: psi and y must be 16-byte aligned", name);
     if (v) {
-        // v may be y itself (each element is read before it is written, by
-        // the same thread) but must not overlap psi, which other tiles read
+        // v is only read: it may be psi, or y itself (each element of y is
+        // read by the thread that then writes it), but not a shifted view of y
         const char *vb = static_cast<const char *>(v);
-        if (vb < pb + bytes && pb < vb + bytes) return fail(QR_EINVAL, "%s: psi and v overlap", name);
         if (vb != yb && vb < yb + bytes && yb < vb + bytes)
             return fail(QR_EINVAL, "%s: v overlaps y without being y", name);
+        if (reinterpret_cast<uintptr_t>(v) & 15)
+            return fail(QR_EINVAL, "%s: v must be 16-byte aligned", name);
     }
     int rc = check_device(op);
     if (rc) return rc;
@@ -1126,34 +1134,9 @@ int qr_op_set_coeffs(qr_op *op, const double *coeff) {
         }
     }
     for (int d = 0; d < 2; ++d)
-        for (int j = 0; j < 2; ++j) {
-            Plan &pl = op->plans[d][j];
-            for (Plan &bp : op->bplans) {
-                bp.built = false;
-                bp.groups.release();
-                bp.tables.release();
-                bp.fat_z.release();
-                bp.fat_c.release();
-                bp.blk_hi.release();
-                bp.blk_g0.release();
-                bp.diag.release();
-                bp.sub.release();
-            }
-            pl.built = false;
-            pl.groups.release();
-            pl.tables.release();
-            pl.fat_z.release();
-            pl.fat_c.release();
-            pl.blk_hi.release();
-            pl.blk_g0.release();
-            pl.diag.release();
-            pl.sub.release();
-            pl.tdesc.release();
-            pl.tdata.release();
-            pl.blk_r0.release();
-            pl.run_g0.release();
-            pl.run_key.release();
-        }
+        for (int j = 0; j < 2; ++j) op->plans[d][j].built = false;
+    // plans are rebuilt on next use into the buffers they already hold
+    for (Plan &bp : op->bplans) bp.built = false;
     return QR_OK;
 }
 
@@ -1212,7 +1195,9 @@ int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const uint32_t nstr = (uint32_t)op->mx.size();
-    uint64_t nchunk = ((uint64_t)op->nsm * 8 + nstr - 1) / nstr;
+    // blocks take 4 strings each: enough chunks for ~8 blocks per SM
+    const uint64_t nbatch = (nstr + 3) / 4;
+    uint64_t nchunk = ((uint64_t)op->nsm * 8 + nbatch - 1) / nbatch;
     const uint64_t maxc = op->N >= 4096 ? op->N / 4096 : 1;
     if (nchunk > maxc) nchunk = maxc;
     if (nchunk < 1) nchunk = 1;

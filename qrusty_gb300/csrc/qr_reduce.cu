@@ -6,6 +6,7 @@
 // by a second kernel in a fixed order, so results are deterministic.
 #include <cstdio>
 #include <mutex>
+#include <type_traits>
 
 #include "../../include/qrusty_gpu.h"
 #include "qr_common.cuh"
@@ -13,6 +14,9 @@
 namespace qr {
 
 constexpr int kRedThreads = 256;
+
+__device__ __forceinline__ bool parity_of(uint32_t v) { return (__popc(v) & 1) != 0; }
+__device__ __forceinline__ bool parity_of(uint64_t v) { return (__popcll(v) & 1) != 0; }
 
 // Block-wide FP64 complex sum; result valid in thread 0.
 __device__ __forceinline__ double2 block_sum(double re, double im, double2 *sh) {
@@ -107,67 +111,107 @@ cudaError_t launch_vdot(int dtype, uint64_t N, const void *a, const void *b, int
 // FP64 across threads and chunks.  partial[m * nchunk + c].
 constexpr int kGradPerThread = 32;
 
-template <bool F32>
+constexpr int kGradK = 4;  // strings per block: they share each g load
+
+template <bool F32> struct GradT;
+template <> struct GradT<true> {
+    using V = float2;
+    using A = float;
+};
+template <> struct GradT<false> {
+    using V = double2;
+    using A = double;
+};
+
+// Accumulate (-1)^popc(r & z) conj(p) g into (ar, ai).
+template <typename A, typename V>
+__device__ __forceinline__ void grad_acc(A &ar, A &ai, V p, V gg, bool neg) {
+    A pr = p.x * gg.x + p.y * gg.y;
+    A pi = p.x * gg.y - p.y * gg.x;
+    ar += neg ? -pr : pr;
+    ai += neg ? -pi : pi;
+}
+
+// partial[m * gridDim.x + blockIdx.x] = the chunk's sum over rows r and states
+// of (-1)^popc(r & z_m) conj(psi[r ^ x_m]) g[r], for the kGradK strings of
+// this block (g read once for all of them).  complex64: FP32 products and
+// per-thread FP32 sums over at most kGradPerThread rows, then FP64.
+template <bool F32, bool WIDE>
 __global__ void __launch_bounds__(kRedThreads) term_grad_partial_kernel(
     uint64_t N, int nstates, const uint64_t *sx, const uint64_t *sz, uint32_t nstr,
     const void *psi_, const void *g_, uint64_t chunk, uint32_t nchunk, double2 *partial) {
+    using W = typename std::conditional<WIDE, uint64_t, uint32_t>::type;
+    using V = typename GradT<F32>::V;
+    using A = typename GradT<F32>::A;
     __shared__ double2 sh[kRedThreads / 32];
-    for (uint32_t m = blockIdx.y; m < nstr; m += gridDim.y) {
-        const uint64_t x = sx[m], z = sz[m];
-        double re = 0.0, im = 0.0;
+    const uint32_t nbatch = (nstr + kGradK - 1) / kGradK;
+    for (uint32_t bm = blockIdx.y; bm < nbatch; bm += gridDim.y) {
+        const uint32_t m0 = bm * kGradK;
+        const uint32_t kv = nstr - m0 < (uint32_t)kGradK ? nstr - m0 : (uint32_t)kGradK;
+        W x[kGradK], z[kGradK];
+#pragma unroll
+        for (int k = 0; k < kGradK; ++k) {
+            x[k] = (uint32_t)k < kv ? (W)sx[m0 + k] : (W)0;
+            z[k] = (uint32_t)k < kv ? (W)sz[m0 + k] : (W)0;
+        }
+        double re[kGradK], im[kGradK];
+#pragma unroll
+        for (int k = 0; k < kGradK; ++k) re[k] = im[k] = 0.0;
         for (uint32_t c = blockIdx.x; c < nchunk; c += gridDim.x) {
             const uint64_t r0 = (uint64_t)c * chunk, r1 = (r0 + chunk < N) ? r0 + chunk : N;
             for (int s = 0; s < nstates; ++s) {
-                if constexpr (F32) {
-                    const float2 *psi = static_cast<const float2 *>(psi_) + (size_t)s * N;
-                    const float2 *g = static_cast<const float2 *>(g_) + (size_t)s * N;
-                    float fr = 0.f, fi = 0.f;
-                    int k = 0;
-                    for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-                        const float2 p = psi[r ^ x];
-                        const float2 gg = g[r];
-                        // conj(p) * g
-                        float pr = fmaf(p.x, gg.x, p.y * gg.y);
-                        float pi = fmaf(p.x, gg.y, -p.y * gg.x);
-                        if (__popcll(r & z) & 1) {
-                            pr = -pr;
-                            pi = -pi;
-                        }
-                        fr += pr;
-                        fi += pi;
-                        if (++k == kGradPerThread) {
-                            re += (double)fr;
-                            im += (double)fi;
-                            fr = fi = 0.f;
-                            k = 0;
+                const V *psi = static_cast<const V *>(psi_) + (size_t)s * N;
+                const V *g = static_cast<const V *>(g_) + (size_t)s * N;
+                A fr[kGradK], fi[kGradK];
+#pragma unroll
+                for (int k = 0; k < kGradK; ++k) fr[k] = fi[k] = A(0);
+                int cnt = 0;
+                W r = (W)(r0 + threadIdx.x);
+                // two rows per step (independent loads in flight)
+                for (; (uint64_t)r + kRedThreads < r1; r += 2 * kRedThreads) {
+                    const W r2 = r + kRedThreads;
+                    const V g1 = g[r], g2 = g[r2];
+#pragma unroll
+                    for (int k = 0; k < kGradK; ++k) {
+                        if ((uint32_t)k < kv) {
+                            const V p1 = psi[r ^ x[k]], p2 = psi[r2 ^ x[k]];
+                            grad_acc<A, V>(fr[k], fi[k], p1, g1, parity_of(r & z[k]));
+                            grad_acc<A, V>(fr[k], fi[k], p2, g2, parity_of(r2 & z[k]));
                         }
                     }
-                    re += (double)fr;
-                    im += (double)fi;
-                } else {
-                    const double2 *psi = static_cast<const double2 *>(psi_) + (size_t)s * N;
-                    const double2 *g = static_cast<const double2 *>(g_) + (size_t)s * N;
-                    for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-                        const double2 p = psi[r ^ x];
-                        const double2 gg = g[r];
-                        double pr = fma(p.x, gg.x, p.y * gg.y);
-                        double pi = fma(p.x, gg.y, -p.y * gg.x);
-                        if (__popcll(r & z) & 1) {
-                            pr = -pr;
-                            pi = -pi;
+                    if (F32 && ++cnt == kGradPerThread / 2) {  // 2 rows per step
+#pragma unroll
+                        for (int k = 0; k < kGradK; ++k) {
+                            re[k] += (double)fr[k];
+                            im[k] += (double)fi[k];
+                            fr[k] = fi[k] = A(0);
                         }
-                        re += pr;
-                        im += pi;
+                        cnt = 0;
                     }
+                }
+                if ((uint64_t)r < r1) {
+                    const V g1 = g[r];
+#pragma unroll
+                    for (int k = 0; k < kGradK; ++k)
+                        if ((uint32_t)k < kv)
+                            grad_acc<A, V>(fr[k], fi[k], psi[r ^ x[k]], g1, parity_of(r & z[k]));
+                }
+#pragma unroll
+                for (int k = 0; k < kGradK; ++k) {
+                    re[k] += (double)fr[k];
+                    im[k] += (double)fi[k];
                 }
             }
         }
-        const double2 t = block_sum(re, im, sh);
-        if (threadIdx.x == 0) partial[(size_t)m * gridDim.x + blockIdx.x] = t;
+#pragma unroll
+        for (int k = 0; k < kGradK; ++k) {
+            const double2 t = block_sum(re[k], im[k], sh);
+            if (threadIdx.x == 0 && (uint32_t)k < kv)
+                partial[(size_t)(m0 + k) * gridDim.x + blockIdx.x] = t;
+        }
     }
 }
 
-// out[k] = conj(unit(phase_k)) * R[map[k]], unit = (1, -i, -1, +i)[phase].
 __global__ void __launch_bounds__(kRedThreads) term_grad_scatter_kernel(uint64_t T,
                                                                         const uint32_t *map,
                                                                         const uint8_t *phase,
@@ -192,15 +236,25 @@ cudaError_t launch_term_grad(int dtype, uint64_t N, int nstates, const uint64_t 
                              double2 *partial, uint32_t nchunk, uint64_t chunk, double2 *R,
                              uint64_t T, const uint32_t *map, const uint8_t *phase, double2 *out,
                              cudaStream_t st) {
-    const unsigned gy = nstr < 65535u ? nstr : 65535u;
+    const uint32_t nbatch = (nstr + kGradK - 1) / kGradK;
+    const unsigned gy = nbatch < 65535u ? nbatch : 65535u;
     const dim3 grid(nchunk, gy);
-    if (dtype == 1)
-        term_grad_partial_kernel<true><<<grid, kRedThreads, 0, st>>>(N, nstates, sx, sz, nstr, psi,
-                                                                     g, chunk, nchunk, partial);
-    else
-        term_grad_partial_kernel<false><<<grid, kRedThreads, 0, st>>>(N, nstates, sx, sz, nstr,
-                                                                      psi, g, chunk, nchunk,
-                                                                      partial);
+    const bool wide = N >= (1ull << 32);  // 32-bit rows need r + 2 * 256 < 2^32
+    if (dtype == 1) {
+        if (wide)
+            term_grad_partial_kernel<true, true><<<grid, kRedThreads, 0, st>>>(
+                N, nstates, sx, sz, nstr, psi, g, chunk, nchunk, partial);
+        else
+            term_grad_partial_kernel<true, false><<<grid, kRedThreads, 0, st>>>(
+                N, nstates, sx, sz, nstr, psi, g, chunk, nchunk, partial);
+    } else {
+        if (wide)
+            term_grad_partial_kernel<false, true><<<grid, kRedThreads, 0, st>>>(
+                N, nstates, sx, sz, nstr, psi, g, chunk, nchunk, partial);
+        else
+            term_grad_partial_kernel<false, false><<<grid, kRedThreads, 0, st>>>(
+                N, nstates, sx, sz, nstr, psi, g, chunk, nchunk, partial);
+    }
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;

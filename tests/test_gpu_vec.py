@@ -182,5 +182,10 @@ def test_fused_apply_axpby(cuda, which, dtype):
     inplace = v.clone()
     op.apply_axpby(psi, inplace, a, b, out=inplace)
     assert torch.equal(torch.view_as_real(inplace), torch.view_as_real(want))
-    with pytest.raises(_lib.QrError, match="psi and v overlap"):
-        op.apply_axpby(psi, psi, a, b)
+    # v = psi: the eigensolver residual H psi - theta psi
+    want2 = axpby(a, op.apply(psi), b, psi)
+    got2 = op.apply_axpby(psi, psi, a, b)
+    assert torch.equal(torch.view_as_real(got2), torch.view_as_real(want2))
+    buf = torch.zeros(2 * N + 2, dtype=tdt, device=cuda)
+    with pytest.raises(_lib.QrError, match="v overlaps y"):
+        op.apply_axpby(psi, buf[2:], a, b, out=buf[:-2])
