@@ -189,24 +189,31 @@ int qr_expect(qr_op *op, int32_t dtype, const void *psi, int32_t nstates, double
 int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32_t nstates,
                  double *out, void *stream);
 
-/* Batched H psi: many operators, each with its own states, in ONE
- * persistent kernel launch over a work list of (operator, state, amplitude
- * tile) items, replayed from a CUDA graph.  Compensated complex64 only.
- * New: no reference counterpart (qrusty applies one operator at a time).
+/* Batched H psi: many operators, each with its own states, behind ONE graph
+ * launch per call.  Compensated complex64 only.  New: no reference
+ * counterpart (qrusty applies one operator at a time).
  *
  * qr_batch_create: ops[i] (all on the current device, n <= 32) with
  * nstates[i] states each.  The operators must outlive the batch, and their
  * coefficients must not change while it exists.
  * qr_batch_apply: psi[i] / y[i] are device pointers to operator i's
- * nstates[i] complex64 states (back to back).  The first call chooses the
- * amplitude-tile width by timing each candidate on the given buffers (the
- * autotuner; y is overwritten) and captures the launch into a CUDA graph;
- * every call launches that graph on `stream`.  A call whose pointers differ
- * from the previous call's synchronises `stream` before uploading them. */
+ * nstates[i] complex64 states (back to back).  The first call times, on the
+ * given buffers (y is overwritten), (a) one persistent kernel over a work list
+ * of (operator, state, amplitude tile) items at tile widths 2^12, 2^11, 2^10
+ * and (b) a graph of one apply kernel per operator on four parallel
+ * branches, keeps the fastest and captures it into a CUDA graph; every call
+ * launches that graph on `stream`.  A call whose pointers differ from the
+ * previous call's synchronises `stream` first (and, for (b), captures the
+ * graph again). */
 typedef struct qr_batch qr_batch;
 int qr_batch_create(int32_t nops, qr_op *const *ops, const int32_t *nstates, qr_batch **out);
 int qr_batch_destroy(qr_batch *b);
 int qr_batch_apply(qr_batch *b, const void *const *psi, void *const *y, void *stream);
+/* Mode the first apply chose: 0 persistent work-list kernel, 1 graph of
+ * per-operator kernels; -1 before the first apply.  qr_batch_set_mode fixes
+ * it instead (-1 restores the choice by timing); only before the first apply. */
+int qr_batch_mode(const qr_batch *b);
+int qr_batch_set_mode(qr_batch *b, int32_t mode);
 /* Tile width the autotuner chose (log2 amplitudes; 0 before the first apply). */
 int qr_batch_tile_bits(const qr_batch *b);
 

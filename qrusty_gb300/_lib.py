@@ -28,7 +28,7 @@ EXPORTS = (
     "qr_op_create", "qr_op_destroy", "qr_op_get_info", "qr_csr_size", "qr_csr_build",
     "qr_apply", "qr_check", "qr_apply_host", "qr_csr_spmv", "qr_op_set_coeffs", "qr_vdot",
     "qr_expect", "qr_term_grad", "qr_vdot_noalloc", "qr_batch_create", "qr_batch_destroy",
-    "qr_batch_apply", "qr_batch_tile_bits", "qr_axpby", "qr_axpy", "qr_ax", "qr_precond2",
+    "qr_batch_apply", "qr_batch_tile_bits", "qr_batch_mode", "qr_batch_set_mode", "qr_axpby", "qr_axpy", "qr_ax", "qr_precond2",
     "qr_csr_diagonal", "qr_op_diagonal", "qr_apply_axpby", "qr_rawio_info", "qr_rawio_read", "qr_rawio_write",
     "qr_mm_write", "qr_mm_open", "qr_mm_fetch", "qr_mm_close", "qr_last_error", "qr_launch_count",
 )
@@ -90,6 +90,8 @@ def load(build_if_missing: bool = True):
     L.qr_batch_destroy.argtypes = [vp]
     L.qr_batch_apply.argtypes = [vp, vp, vp, vp]
     L.qr_batch_tile_bits.argtypes = [vp]
+    L.qr_batch_mode.argtypes = [vp]
+    L.qr_batch_set_mode.argtypes = [vp, i32]
     L.qr_term_grad.argtypes = [vp, i32, vp, vp, i32, vp, vp]
     L.qr_axpby.argtypes = [i32, u64, vp, vp, vp, vp, vp, vp]
     L.qr_axpy.argtypes = [i32, u64, vp, vp, vp, vp, vp]

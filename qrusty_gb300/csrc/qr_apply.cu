@@ -327,30 +327,30 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
     }
 }
 
-// ---------------------------------------------------------------- c64c kernel
-// Compensated complex64 path.  256 threads x AMPS = 16 amplitudes per 4096-
-// amplitude tile; thread t owns r_lo = t + 256 m.  The host splits every
-// x-group into sub-groups whose z masks agree on the register bits
-// [kTb, kTb + log2 AMPS), so for a thread the sub-group's factor is
+// ---------------------------------------------------------------- c64c kernels
+// Compensated complex64 path.  A 4096-amplitude tile is held by T threads x
+// AMPS amplitudes (single-operator kernel: 512 x 8, batched kernel: 256 x 16);
+// thread t owns r_lo = t + T m.  The host splits every x-group into
+// sub-groups whose z masks agree on the register bits [kTb, kTb + log2 AMPS)
+// and whose z differences span rank <= 2, so for a thread the sub-group's
+// factor is
 //     D_m = (-1)^popc(m & zm) * Dt,   Dt = (-1)^popc(r0 & z0) * tab[u],
-// r0 = (tile << b) | t, u_i = popc(r0 & beta_i) & 1 (rank <= 2, table
-// inline in the 64-byte descriptor, read one sub-group ahead).  The sign
-// pattern over m selects a compile-time instantiation, so the inner step per
-// amplitude is one shared-memory load and two packed FMAs:
+// r0 = (tile << b) | t, u_i = popc(r0 & beta_i) & 1.  The sign pattern over
+// m selects a compile-time instantiation, so the inner step per amplitude is
+// one shared-memory load and two packed FMAs:
 //     A_m += (+-Dt.re) * p,  B_m += (+-Dt.im) * p      (fma.rn.f32x2)
 // and y = A + iB is folded into the running (hi, lo) two-sum pair every
 // kFlush partner tiles; hi stays in registers, the error term lo (touched
 // only at a fold) lives in shared memory.
 //
-// Pipeline: a kC64Stages-deep ring of partner tiles filled by 1-D TMA bulk
-// copies.  Warps run decoupled: each waits on the stage's full mbarrier,
-// consumes it, and counts itself out on a shared counter; the last warp out
-// refills the stage with the tile kC64Stages steps ahead.  No CTA-wide
-// barrier sits on the steady-state path.
-// Single-operator kernels run 512 threads x 8 amplitudes per 4096-amplitude
-// tile (16 warps per SM hide more latency than 8 warps x 16 amplitudes,
-// and fewer register bits leave fewer sign patterns to split on); the
-// batched kernel keeps 256 x 16, its register budget at 512 threads spills.
+// Pipeline: a ring of partner tiles filled by 1-D TMA bulk copies.  Warps run
+// decoupled: each waits on the stage's full mbarrier, consumes it, and counts
+// itself out on a shared counter; the last warp out refills the stage with
+// the tile a ring length ahead.  No CTA-wide barrier sits on the
+// steady-state path.  The single-operator kernel runs 16 warps per SM
+// (512 x 8 hides more latency than 256 x 16, and fewer register bits leave
+// fewer sign patterns to split on); the batched kernel keeps 256 x 16, its
+// register budget at 512 threads spills.
 constexpr int kTb = kC64ThreadBits;       // log2(threads) whenever AMPS >= 2
 constexpr int kMsh = kTb + 3;             // byte shift of the register index m
 constexpr int kFlush = 8;                 // partner tiles per compensated fold
@@ -364,86 +364,6 @@ template <bool WIDE>
 __device__ __forceinline__ uint32_t parity(uint64_t r, uint64_t m) {
     if constexpr (WIDE) return (uint32_t)__popcll(r & m) & 1u;
     else return (uint32_t)__popc((uint32_t)r & (uint32_t)m) & 1u;
-}
-
-// Thread-dependent state of one sub-group, computed one group ahead.
-struct GroupState {
-    float2 D;       // Dt: table entry with the thread's sign folded in
-    uint32_t off;   // byte offset of the thread's partner for m = 0 (without stage)
-    uint32_t kind;  // descriptor kind (zm | d << 4 | big << 8)
-};
-
-template <bool WIDE>
-__device__ __forceinline__ GroupState group_setup(const SubDescC64 &sd, uint64_t r0, uint32_t t,
-                                                  uint32_t tmask, int tb) {
-    GroupState gs;
-    gs.kind = sd.kind;
-    gs.off = ((t ^ (sd.lo & tmask)) << 3) | ((sd.lo >> tb) << kMsh);
-    const uint32_t u = parity<WIDE>(r0, sd.beta0) | (parity<WIDE>(r0, sd.beta1) << 1);
-    float dx = (u & 2u) ? ((u & 1u) ? sd.tab[6] : sd.tab[4]) : ((u & 1u) ? sd.tab[2] : sd.tab[0]);
-    float dy = (u & 2u) ? ((u & 1u) ? sd.tab[7] : sd.tab[5]) : ((u & 1u) ? sd.tab[3] : sd.tab[1]);
-    if (parity<WIDE>(r0, sd.z0)) {
-        dx = -dx;
-        dy = -dy;
-    }
-    gs.D = make_float2(dx, dy);
-    return gs;
-}
-
-// One sub-group's m-loop (compile-time sign pattern ZM), with the next
-// sub-group's setup in the same basic block so its dependency chain overlaps
-// the 2*AMPS independent FMAs.
-template <int AMPS, int ZM, bool XM, bool WIDE>
-__device__ __forceinline__ void mloop_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                          const unsigned char *sm, uint32_t off, float2 D,
-                                          const SubDescC64 *ndp, uint64_t r0n, uint32_t t,
-                                          uint32_t tmask, int tb, GroupState &next) {
-    // Phase 1: all partner loads (independent, so their latency overlaps).
-    // XM: the sub-group's x has register bits, so partners are permuted by
-    // XOR; otherwise the offsets are compile-time immediates.
-    float2 p[AMPS];
-#pragma unroll
-    for (int m = 0; m < AMPS; ++m) {
-        const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
-        p[m] = *reinterpret_cast<const float2 *>(sm + o);
-    }
-    // Phase 2: the next sub-group's setup (its own load/parity chain).
-    const SubDescC64 nd = *ndp;
-    next = group_setup<WIDE>(nd, r0n, t, tmask, tb);
-    // Phase 3: packed FMAs with the compile-time sign pattern.
-    const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
-    const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
-#pragma unroll
-    for (int m = 0; m < AMPS; ++m) {
-        const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
-        A[m] = __ffma2_rn(neg ? an : ap, p[m], A[m]);
-        B[m] = __ffma2_rn(neg ? bn : bp, p[m], B[m]);
-    }
-}
-
-template <int AMPS, bool WIDE>
-__device__ __forceinline__ void mloop_dispatch(uint32_t zm, float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                               const unsigned char *sm, uint32_t off, float2 D,
-                                               const SubDescC64 *nd, uint64_t r0n, uint32_t t,
-                                               uint32_t tmask, int tb, GroupState &next) {
-#define QR_ZM_CASE(k)                                                                        \
-    case k:                                                                                  \
-        if constexpr ((k & 15) < AMPS)                                                       \
-            mloop_c64<AMPS, (k & 15), (k >> 4) != 0, WIDE>(A, B, sm, off, D, nd, r0n, t, tmask, \
-                                                           tb, next);                        \
-        break;
-    switch (zm) {
-        QR_ZM_CASE(0) QR_ZM_CASE(1) QR_ZM_CASE(2) QR_ZM_CASE(3)
-        QR_ZM_CASE(4) QR_ZM_CASE(5) QR_ZM_CASE(6) QR_ZM_CASE(7)
-        QR_ZM_CASE(8) QR_ZM_CASE(9) QR_ZM_CASE(10) QR_ZM_CASE(11)
-        QR_ZM_CASE(12) QR_ZM_CASE(13) QR_ZM_CASE(14) QR_ZM_CASE(15)
-        QR_ZM_CASE(16) QR_ZM_CASE(17) QR_ZM_CASE(18) QR_ZM_CASE(19)
-        QR_ZM_CASE(20) QR_ZM_CASE(21) QR_ZM_CASE(22) QR_ZM_CASE(23)
-        QR_ZM_CASE(24) QR_ZM_CASE(25) QR_ZM_CASE(26) QR_ZM_CASE(27)
-        QR_ZM_CASE(28) QR_ZM_CASE(29) QR_ZM_CASE(30) QR_ZM_CASE(31)
-        default: break;
-    }
-#undef QR_ZM_CASE
 }
 
 // Rank 3-4 (table) or term-by-term ("fat") sub-group through GroupDesc.
@@ -478,181 +398,9 @@ __device__ __forceinline__ void big_group_c64(float2 (&A)[AMPS], float2 (&B)[AMP
     }
 }
 
-template <int AMPS, bool WIDE>
-__global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    const uint32_t threads = blockDim.x;
-    const uint32_t nwarps = threads >> 5;
-    const uint32_t t = threadIdx.x;
-    const uint32_t lane = t & 31;
-    const uint32_t tile_bytes = (1u << a.b) * 8u;
-    float2 *s_lo = reinterpret_cast<float2 *>(smem_raw + (size_t)kC64Stages * tile_bytes);
-    uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * blockDim.x);
-    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kC64Stages);
-
-    const float2 *psi = static_cast<const float2 *>(a.psi);
-    float2 *y = static_cast<float2 *>(a.y);
-    const float2 *tables = static_cast<const float2 *>(a.tables);
-    const float2 *fat_c = static_cast<const float2 *>(a.fat_c);
-    const float2 *diag = static_cast<const float2 *>(a.diag);
-    const uint32_t nb = a.nblocks;
-    const uint32_t tmask = threads - 1;
-
-    const uint64_t first = blockIdx.x;
-    const uint64_t my_items =
-        a.nitems > first ? (a.nitems - first + gridDim.x - 1) / gridDim.x : 0;
-    const uint64_t total = my_items * nb;
-    if (total == 0) return;
-
-    auto issue = [&](uint64_t L) {
-        const uint64_t k = L / nb;
-        const uint32_t j = (uint32_t)(L - k * nb);
-        const uint64_t item = first + k * gridDim.x;
-        const uint64_t st = item / a.ntiles;
-        const uint64_t q = item - st * a.ntiles;
-        const float2 *src = psi + st * a.N + ((q ^ a.blk_hi[j]) << a.b);
-        const int s = (int)(L % (uint64_t)kC64Stages);
-        mbar_expect_tx(&full[s], tile_bytes);
-        bulk_g2s(smem_raw + (size_t)s * tile_bytes, src, tile_bytes, &full[s]);
-    };
-    if (t == 0) {
-        for (int s = 0; s < kC64Stages; ++s) {
-            mbar_init(&full[s], 1);
-            cnt[s] = 0;
-        }
-        mbar_fence_init();
-        const uint64_t pro = total < (uint64_t)kC64Stages ? total : (uint64_t)kC64Stages;
-        for (uint64_t L = 0; L < pro; ++L) issue(L);
-    }
-    __syncthreads();
-
-    float2 A[AMPS], B[AMPS], hi[AMPS];
-    float2 *mylo = s_lo + t;  // lo[m] at mylo[m * threads]
-    const SubDescC64 *subs = a.sub;
-    const uint32_t nsub = a.nsub;
-    // loop state advanced incrementally (no division on the steady path)
-    uint32_t j = 0, s = 0, par = 0;
-    uint64_t item = first;
-    uint64_t st = item / a.ntiles;
-    uint64_t q = item - st * a.ntiles;
-    // current sub-group's thread state, computed one group ahead in the
-    // tile-by-tile linear order of sub-groups
-    GroupState cur;
-    if (nsub > 0) cur = group_setup<WIDE>(subs[0], (q << a.b) | t, t, tmask, a.tb);
-
-    for (uint64_t L = 0; L < total; ++L) {
-        const uint64_t r0 = (q << a.b) | t;
-        if (j == 0) {
-#pragma unroll
-            for (int m = 0; m < AMPS; ++m) {
-                A[m] = B[m] = hi[m] = make_float2(0.f, 0.f);
-                mylo[m * threads] = make_float2(0.f, 0.f);
-            }
-        }
-        if (!mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
-            if (lane == 0) atomicExch(a.err, kErrMbarTimeout);
-            return;
-        }
-        const uint32_t soff = s * tile_bytes;
-
-        if ((int)j == a.diag_block && diag != nullptr) {
-            const float2 *dg = diag + (q << a.b);
-#pragma unroll
-            for (int m = 0; m < AMPS; ++m) {
-                const uint32_t rl = t + threads * (uint32_t)m;
-                const float2 d = dg[rl];
-                const float2 p = *reinterpret_cast<const float2 *>(smem_raw + soff + rl * 8u);
-                A[m] = __ffma2_rn(make_float2(d.x, d.x), p, A[m]);
-                B[m] = __ffma2_rn(make_float2(d.y, d.y), p, B[m]);
-            }
-        }
-
-        const uint32_t g1 = a.blk_g0[j + 1];
-        for (uint32_t g = a.blk_g0[j]; g < g1; ++g) {
-            // next sub-group in linear order: g + 1 of this tile, or 0 of the next
-            uint64_t r0n = r0;
-            uint32_t gn = g + 1;
-            if (gn == nsub) {
-                gn = 0;
-                uint64_t qn = q + gridDim.x;
-                while (qn >= a.ntiles) qn -= a.ntiles;
-                r0n = (qn << a.b) | t;
-            }
-            const uint32_t off = soff | cur.off;
-            GroupState nxt;
-            if ((cur.kind >> 8) == 0) {
-                mloop_dispatch<AMPS, WIDE>(cur.kind & 31u, A, B, smem_raw, off, cur.D, subs + gn,
-                                           r0n, t, tmask, a.tb, nxt);
-            } else {
-                big_group_c64<AMPS>(A, B, smem_raw, off, a.groups[g], r0, a.tb, tables, a.fat_z,
-                                    fat_c);
-                nxt = group_setup<WIDE>(subs[gn], r0n, t, tmask, a.tb);
-            }
-            cur = nxt;
-        }
-
-        const bool last = (j == nb - 1);
-        if (last || (j % kFlush) == kFlush - 1) {
-#pragma unroll
-            for (int m = 0; m < AMPS; ++m) {
-                const float yr = __fsub_rn(A[m].x, B[m].y);
-                const float yi = __fadd_rn(A[m].y, B[m].x);
-                float2 lm = mylo[m * threads];
-                two_sum_into(hi[m].x, lm.x, yr);
-                two_sum_into(hi[m].y, lm.y, yi);
-                mylo[m * threads] = lm;
-                A[m] = B[m] = make_float2(0.f, 0.f);
-            }
-        }
-        if (last) {
-            float2 *yo = y + st * a.N + (q << a.b);
-            const float2 *vo = a.v ? static_cast<const float2 *>(a.v) + st * a.N + (q << a.b)
-                                   : nullptr;
-#pragma unroll
-            for (int m = 0; m < AMPS; ++m) {
-                const float2 lm = mylo[m * threads];
-                const uint32_t rl = t + threads * (uint32_t)m;
-                float2 o = make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
-                if (vo)  // fused y = alpha (H psi) + beta v, in FP32
-                    o = cx_axpby((float)a.ar, (float)a.ai, o, (float)a.br, (float)a.bi, vo[rl]);
-                yo[rl] = o;
-            }
-        }
-
-        // this warp is done with stage s; the last warp out refills it
-        __syncwarp();
-        if (lane == 0) {
-            __threadfence_block();
-            const uint32_t old = atomicAdd(&cnt[s], 1u);
-            if (old == nwarps - 1) {
-                cnt[s] = 0;
-                if (L + (uint64_t)kC64Stages < total) {
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    issue(L + (uint64_t)kC64Stages);
-                }
-            }
-        }
-        // advance (stage ring, partner tile, item)
-        if (++s == kC64Stages) {
-            s = 0;
-            par ^= 1u;
-        }
-        if (++j == nb) {
-            j = 0;
-            item += gridDim.x;
-            q += gridDim.x;
-            while (q >= a.ntiles) {
-                q -= a.ntiles;
-                ++st;
-            }
-        }
-    }
-}
-
 // ---------------------------------------------------------------- c64c, tile table
-// The production compensated-c64 kernel.  Same tiles, thread layout, partner
-// ring and two-sum folding as apply_c64c, with the per-sub-group work split
-// by who can do it once:
+// The single-operator compensated-c64 kernel.  The per-sub-group work is
+// split by who can do it once:
 //   * per output tile (cooperatively, into shared memory): for every
 //     sub-group the tile-index parity of z0 / beta0,1 applied to its table,
 //     stored pre-duplicated as (re, re, im, im) for the packed FMAs;
@@ -667,7 +415,6 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c(const ApplyArgs a) 
 constexpr int kTabStages = QR_TAB_STAGES;  // partner-tile ring depth (4 timed best of 3, 4, 5)
 constexpr size_t kMaxSmemPerBlock = 227u * 1024u;  // sm_100-family opt-in limit
 constexpr int kTabEnt = 4;  // per-tile table entries (float4) per sub-group
-constexpr uint32_t kTabMaxSub = 512;
 // full barriers, stage counters and the abort flag, rounded to 8 bytes
 constexpr size_t kTabBarBytes = ((size_t)kTabStages * 12u + 4u + 7u) & ~(size_t)7u;
 
@@ -747,22 +494,25 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
     const uint32_t t = threadIdx.x;
     const uint32_t lane = t & 31;
     const uint32_t tile_bytes = (1u << a.b) * 8u;
+    const uint32_t tabn = a.nsub < kTabCap ? a.nsub : kTabCap;
     float4 *s_tab = reinterpret_cast<float4 *>(smem_raw + (size_t)kTabStages * tile_bytes);
-    float2 *s_lo = reinterpret_cast<float2 *>(s_tab + kTabEnt * (size_t)a.nsub);
+    float2 *s_lo = reinterpret_cast<float2 *>(s_tab + kTabEnt * (size_t)tabn);
     uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
     uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kTabStages);
     volatile uint32_t *s_abort = cnt + kTabStages;
-    // sub-group descriptors, runs (g0 | key << 16) and per-block run ranges,
-    // staged once per CTA
-    uint2 *s_td = reinterpret_cast<uint2 *>(smem_raw + (size_t)kTabStages * tile_bytes +
-                                            (size_t)kTabEnt * 16u * a.nsub +
+    // sub-group descriptors, runs (g0 | key << 16) and per-block run ranges of
+    // the current chunk, indices relative to the chunk; with one chunk they
+    // are staged once per CTA
+    uint2 *s_td = reinterpret_cast<uint2 *>(reinterpret_cast<unsigned char *>(s_lo) +
                                             (size_t)AMPS * threads * 8u + kTabBarBytes);
-    uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + a.nsub);
-    uint32_t *s_blk = s_run + a.nruns + 1;
-    for (uint32_t i = t; i < a.nsub; i += threads) s_td[i] = a.tdesc[i];
-    for (uint32_t i = t; i <= a.nruns; i += threads)
-        s_run[i] = a.run_g0[i] | (i < a.nruns ? a.run_key[i] << 16 : 0u);
-    for (uint32_t i = t; i <= a.nblocks; i += threads) s_blk[i] = a.blk_r0[i];
+    uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + kTabCap);
+    uint32_t *s_blk = s_run + kTabCap + 1;
+    if (a.nchunks == 1) {
+        for (uint32_t i = t; i < a.nsub; i += threads) s_td[i] = a.tdesc[i];
+        for (uint32_t i = t; i <= a.nruns; i += threads)
+            s_run[i] = a.run_g0[i] | (i < a.nruns ? a.run_key[i] << 16 : 0u);
+        for (uint32_t i = t; i <= a.nblocks; i += threads) s_blk[i] = a.blk_r0[i];
+    }
     const uint2 *tdesc = s_td;
 
     const float2 *psi = static_cast<const float2 *>(a.psi);
@@ -803,6 +553,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
     float2 A[AMPS], B[AMPS], hi[AMPS];
     float2 *mylo = s_lo + t;
     uint32_t j = 0, s = 0, par = 0;
+    uint32_t cidx = 0, cj0 = 0, next_j = 0;  // current chunk, its first block, the next's
     uint64_t st = first / a.ntiles;
     uint64_t q = first - st * a.ntiles;
 
@@ -813,16 +564,35 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
                 A[m] = B[m] = hi[m] = make_float2(0.f, 0.f);
                 mylo[m * threads] = make_float2(0.f, 0.f);
             }
-            // per-tile table: every warp has finished the previous tile
+            cidx = 0;
+        }
+        if (j == 0 || j == next_j) {
+            // table (and, with several chunks, run lists) of the chunk that
+            // starts at block j: every warp has finished the previous one
+            if (j != 0) ++cidx;
             __syncthreads();
-            for (uint32_t g = t; g < a.nsub; g += threads) {
-                const TileDataC64 &d = a.tdata[g];
+            const uint4 c0 = a.nchunks > 1 ? a.chunks[cidx] : make_uint4(0u, 0u, 0u, 0u);
+            const uint4 c1 = a.nchunks > 1 ? a.chunks[cidx + 1]
+                                           : make_uint4(a.nsub, a.nruns, a.nblocks, 0u);
+            cj0 = c0.z;
+            next_j = c1.z;
+            if (a.nchunks > 1) {
+                for (uint32_t i = t; i < c1.x - c0.x; i += threads) s_td[i] = a.tdesc[c0.x + i];
+                for (uint32_t i = t; i <= c1.y - c0.y; i += threads) {
+                    const uint32_t r = c0.y + i;
+                    s_run[i] = (a.run_g0[r] - c0.x) | (r < a.nruns ? a.run_key[r] << 16 : 0u);
+                }
+                for (uint32_t i = t; i <= c1.z - c0.z; i += threads)
+                    s_blk[i] = a.blk_r0[c0.z + i] - c0.y;
+            }
+            for (uint32_t gi = t; gi < c1.x - c0.x; gi += threads) {
+                const TileDataC64 &d = a.tdata[c0.x + gi];
                 const uint32_t uq = parity<WIDE>(q, d.b0h) | (parity<WIDE>(q, d.b1h) << 1);
                 const float sq = parity<WIDE>(q, d.z0h) ? -1.f : 1.f;
 #pragma unroll
                 for (uint32_t u = 0; u < 4; ++u) {
                     const float2 v = d.T[u ^ uq];
-                    s_tab[g * 4 + u] = make_float4(sq * v.x, sq * v.x, sq * v.y, sq * v.y);
+                    s_tab[gi * 4 + u] = make_float4(sq * v.x, sq * v.x, sq * v.y, sq * v.y);
                 }
             }
             __syncthreads();
@@ -852,9 +622,10 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
             }
         }
 
-        const uint32_t r1 = skip ? 0u : s_blk[j + 1];
-        uint32_t rw = s_run[s_blk[j]];
-        for (uint32_t r = s_blk[j]; r < r1; ++r) {
+        const uint32_t jl = j - cj0;
+        const uint32_t r1 = skip ? 0u : s_blk[jl + 1];
+        uint32_t rw = s_run[s_blk[jl]];
+        for (uint32_t r = s_blk[jl]; r < r1; ++r) {
             const uint32_t rn = s_run[r + 1];
             run_tab_dispatch<AMPS>(rw >> 16, A, B, smem_raw, soff, s_tab, tdesc, rw & 0xffffu,
                                    rn & 0xffffu, t, t8);
@@ -920,29 +691,13 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
     }
 }
 
-template <int AMPS, bool WIDE>
-static cudaError_t launch_c64c_w(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
-    const uint32_t tile_bytes = (1u << a.b) * 8u;
-    const size_t smem = (size_t)kC64Stages * tile_bytes + (size_t)AMPS * threads * 8u +
-                        kC64Stages * (sizeof(uint64_t) + 4);
-    auto kern = apply_c64c<AMPS, WIDE>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    uint64_t grid = a.nitems < (uint64_t)nsm ? a.nitems : (uint64_t)nsm;
-    if (grid == 0) return cudaSuccess;
-    kern<<<(unsigned)grid, threads, smem, st>>>(a);
-    count_launch();
-    return cudaGetLastError();
-}
-
 template <int AMPS>
 static size_t tab_smem_bytes(const ApplyArgs &a, int threads) {
     const uint32_t tile_bytes = (1u << a.b) * 8u;
-    size_t smem = (size_t)kTabStages * tile_bytes + (size_t)a.nsub * 16u * kTabEnt +
-                  (size_t)AMPS * threads * 8u + kTabBarBytes;
-    smem += (size_t)a.nsub * 8u + ((size_t)a.nruns + 1 + a.nblocks + 1) * 4u;
-    return smem;
+    const uint32_t tabn = a.nsub < kTabCap ? a.nsub : kTabCap;
+    return (size_t)kTabStages * tile_bytes + (size_t)tabn * 16u * kTabEnt +
+           (size_t)AMPS * threads * 8u + kTabBarBytes +
+           (size_t)kTabCap * 8u + (2u * (size_t)kTabCap + 3u) * 4u;
 }
 
 template <int AMPS, bool WIDE>
@@ -961,19 +716,16 @@ static cudaError_t launch_c64c_tab(const ApplyArgs &a, int threads, int nsm, cud
 
 template <int AMPS>
 static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
-    // the per-tile-table kernel needs its tables and run lists in shared memory
-    if (a.nsub <= kTabMaxSub && tab_smem_bytes<AMPS>(a, threads) <= kMaxSmemPerBlock) {
-        if (a.n > 32) return launch_c64c_tab<AMPS, true>(a, threads, nsm, st);
-        return launch_c64c_tab<AMPS, false>(a, threads, nsm, st);
-    }
-    if (a.n > 32) return launch_c64c_w<AMPS, true>(a, threads, nsm, st);
-    return launch_c64c_w<AMPS, false>(a, threads, nsm, st);
+    // shared memory: partner ring, one table chunk, low parts, run lists
+    if (tab_smem_bytes<AMPS>(a, threads) > kMaxSmemPerBlock) return cudaErrorInvalidValue;
+    if (a.n > 32) return launch_c64c_tab<AMPS, true>(a, threads, nsm, st);
+    return launch_c64c_tab<AMPS, false>(a, threads, nsm, st);
 }
 
 // ---------------------------------------------------------------- batched c64c
 // Many operators (different n, term counts and state counts) in ONE
 // persistent launch over a host-built work list of (operator, state, tile)
-// items.  Same partner-tile ring and inner step as apply_c64c; the operator's
+// items.  Same partner-tile ring and inner step as apply_c64c_tab; the operator's
 // parameters come from a device array per item, tiles of operators with
 // n < 12 use the first 2^n amplitudes of a stage, and the warp that refills a
 // stage walks the work list six steps ahead to find the tile to load.

@@ -81,6 +81,10 @@ struct ApplyArgs {
     const uint32_t *run_g0;   // sub-groups of run r: [run_g0[r], run_g0[r+1])
     const uint32_t *run_key;  // key = zm | xm << 4
     uint32_t nruns;
+    // chunks of consecutive blocks with at most kTabCap sub-groups:
+    // {first sub-group, first run, first block, 0}, nchunks + 1 entries
+    const uint4 *chunks;
+    uint32_t nchunks;
     // fused epilogue y = alpha * (H psi) + beta * v when v != nullptr
     const void *v;
     double ar, ai, br, bi;
@@ -138,6 +142,9 @@ __device__ __forceinline__ float2 cx_axpby(float ar, float ai, float2 x, float b
     const float vi = __fadd_rn(__fmul_rn(br, y.y), __fmul_rn(bi, y.x));
     return make_float2(__fadd_rn(ur, vr), __fadd_rn(ui, vi));
 }
+
+// sub-groups of one per-tile factor table of the compensated-complex64 kernel
+constexpr uint32_t kTabCap = 512;
 
 // log2 of the thread count of the compensated-complex64 kernels: the
 // single-operator kernels and the batched kernel (see qr_apply.cu).

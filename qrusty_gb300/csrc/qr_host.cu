@@ -102,9 +102,9 @@ struct Plan {
     bool has_diag = false;
     DevBuf groups, tables, fat_z, fat_c, blk_hi, blk_g0, diag;
     // compensated-c64 kernel tables
-    uint32_t nsub = 0, nruns = 0;
+    uint32_t nsub = 0, nruns = 0, nchunks = 0;
     DevBuf sub;
-    DevBuf tdesc, tdata, blk_r0, run_g0, run_key;
+    DevBuf tdesc, tdata, blk_r0, run_g0, run_key, chunks;
 };
 
 }  // namespace qr
@@ -527,11 +527,28 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         }
     }
     bg0.push_back((uint32_t)ord.size());
+    if (f32) {
+        // the per-tile table holds at most kTabCap sub-groups: a partner tile
+        // with more is visited as several consecutive blocks (same partner)
+        std::vector<uint64_t> vh;
+        std::vector<uint32_t> vg;
+        for (size_t j = 0; j + 1 < bg0.size(); ++j) {
+            uint32_t g = bg0[j];
+            do {
+                vh.push_back(bhi[j]);
+                vg.push_back(g);
+                g += std::min<uint32_t>(kTabCap, bg0[j + 1] - g);
+            } while (g < bg0[j + 1]);
+        }
+        vg.push_back((uint32_t)ord.size());
+        bhi.swap(vh);
+        bg0.swap(vg);
+    }
     pl.nblocks = (uint32_t)bhi.size();
     pl.ngroups = ord.size();
     pl.diag_block = -1;
     for (size_t j = 0; j < bhi.size(); ++j)
-        if (bhi[j] == 0) pl.diag_block = (int)j;
+        if (bhi[j] == 0 && pl.diag_block < 0) pl.diag_block = (int)j;
 
     std::vector<unsigned char> tab, fc;
     std::vector<uint64_t> fz;
@@ -627,6 +644,17 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         }
         r0v.push_back((uint32_t)rkey.size());
         rg0.push_back((uint32_t)ord.size());
+        // chunks: consecutive blocks holding at most kTabCap sub-groups; the
+        // kernel rebuilds its table (and staged run lists) at each chunk start
+        std::vector<uint4> ch;
+        for (uint32_t j = 0; j < pl.nblocks; ++j) {
+            if (ch.empty() || bg0[j + 1] - ch.back().x > kTabCap)
+                ch.push_back(make_uint4(bg0[j], r0v[j], j, 0));
+        }
+        if (ch.empty()) ch.push_back(make_uint4(0, 0, 0, 0));
+        pl.nchunks = (uint32_t)ch.size();
+        ch.push_back(make_uint4((uint32_t)ord.size(), (uint32_t)rkey.size(), pl.nblocks, 0));
+        QR_CUDA(pl.chunks.upload(ch), "upload chunks");
         if (td.empty()) {
             td.push_back(make_uint2(0, 0));
             TileDataC64 z;
@@ -951,6 +979,8 @@ static int apply_impl(const char *name, qr_op *op, int32_t dtype, const void *ps
     a.run_g0 = pl.run_g0.as<uint32_t>();
     a.run_key = pl.run_key.as<uint32_t>();
     a.nruns = pl.nruns;
+    a.chunks = pl.chunks.as<uint4>();
+    a.nchunks = pl.nchunks;
     a.v = v;
     if (v) {
         a.ar = alpha[0];
@@ -1220,17 +1250,23 @@ int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32
 }  // extern "C"
 
 struct qr_batch {
+    static constexpr int kForks = 4;  // parallel branches of the per-operator graph
     int device = 0, nsm = 0;
     std::vector<qr_op *> ops;
     std::vector<int32_t> nstates;
     int tile_bits = 0;
+    int mode = 0;         // 0: one persistent work-list kernel, 1: graph of per-operator kernels
+    int force_mode = -1;  // -1: the autotuner chooses
     DevBuf d_ops, d_items, d_ptrs, d_err;
     uint32_t nitems = 0;
     std::vector<const void *> cur_psi;
     std::vector<void *> cur_y;
+    bool ptrs_changed = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t cap = nullptr;
+    cudaStream_t fork[kForks] = {};
+    cudaEvent_t fork_ev[kForks + 1] = {};
 };
 
 namespace {
@@ -1317,6 +1353,47 @@ int batch_upload_ptrs(qr_batch *bt, const void *const *psi, void *const *y, cuda
             "upload batch pointers");
     bt->cur_psi.assign(psi, psi + n);
     bt->cur_y.assign(y, y + n);
+    bt->ptrs_changed = true;
+    return QR_OK;
+}
+
+// Graph of one compensated-c64 apply per operator on the current pointers,
+// spread over kForks parallel branches so small operators overlap.  Plans
+// must already be built (an uncaptured apply per operator does that).
+int capture_per_op(qr_batch *bt, cudaGraph_t *graph) {
+    cudaStream_t cap = bt->cap;
+    QR_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed), "begin capture");
+    cudaError_t e = cudaEventRecord(bt->fork_ev[qr_batch::kForks], cap);
+    for (int k = 0; k < qr_batch::kForks && e == cudaSuccess; ++k)
+        e = cudaStreamWaitEvent(bt->fork[k], bt->fork_ev[qr_batch::kForks], 0);
+    int rc = QR_OK;
+    for (size_t i = 0; i < bt->ops.size() && e == cudaSuccess && !rc; ++i)
+        rc = apply_impl("qr_batch_apply", bt->ops[i], QR_C64C, bt->cur_psi[i], bt->cur_y[i],
+                        bt->nstates[i], 0, bt->fork[i % qr_batch::kForks], nullptr, nullptr,
+                        nullptr);
+    for (int k = 0; k < qr_batch::kForks && e == cudaSuccess; ++k) {
+        e = cudaEventRecord(bt->fork_ev[k], bt->fork[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(cap, bt->fork_ev[k], 0);
+    }
+    cudaError_t e2 = cudaStreamEndCapture(cap, graph);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "per-operator graph capture");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
+    return QR_OK;
+}
+
+void drop_graph(qr_batch *bt) {
+    if (bt->exec) cudaGraphExecDestroy(bt->exec);
+    if (bt->graph) cudaGraphDestroy(bt->graph);
+    bt->exec = nullptr;
+    bt->graph = nullptr;
+}
+
+int instantiate_per_op(qr_batch *bt) {
+    drop_graph(bt);
+    int rc = capture_per_op(bt, &bt->graph);
+    if (rc) return rc;
+    QR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0), "graph instantiate");
     return QR_OK;
 }
 
@@ -1346,6 +1423,10 @@ int qr_batch_create(int32_t nops, qr_op *const *ops, const int32_t *nstates, qr_
     if (e == cudaSuccess) e = bt->d_err.alloc(sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(bt->d_err.p, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bt->cap, cudaStreamNonBlocking);
+    for (int k = 0; k < qr_batch::kForks && e == cudaSuccess; ++k)
+        e = cudaStreamCreateWithFlags(&bt->fork[k], cudaStreamNonBlocking);
+    for (int k = 0; k <= qr_batch::kForks && e == cudaSuccess; ++k)
+        e = cudaEventCreateWithFlags(&bt->fork_ev[k], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete bt;
         return cuda_fail(e, "qr_batch_create");
@@ -1356,14 +1437,27 @@ int qr_batch_create(int32_t nops, qr_op *const *ops, const int32_t *nstates, qr_
 
 int qr_batch_destroy(qr_batch *bt) {
     if (!bt) return QR_OK;
-    if (bt->exec) cudaGraphExecDestroy(bt->exec);
-    if (bt->graph) cudaGraphDestroy(bt->graph);
+    if (bt->cap) cudaStreamSynchronize(bt->cap);
+    drop_graph(bt);
+    for (auto &f : bt->fork)
+        if (f) cudaStreamDestroy(f);
+    for (auto &ev : bt->fork_ev)
+        if (ev) cudaEventDestroy(ev);
     if (bt->cap) cudaStreamDestroy(bt->cap);
     delete bt;
     return QR_OK;
 }
 
 int qr_batch_tile_bits(const qr_batch *bt) { return bt ? bt->tile_bits : 0; }
+
+int qr_batch_mode(const qr_batch *bt) { return bt && bt->exec ? bt->mode : -1; }
+
+int qr_batch_set_mode(qr_batch *bt, int32_t mode) {
+    if (!bt || mode < -1 || mode > 1) return fail(QR_EINVAL, "qr_batch_set_mode: bad arguments");
+    if (bt->exec) return fail(QR_ESTATE, "qr_batch_set_mode: the first apply has already chosen");
+    bt->force_mode = mode;
+    return QR_OK;
+}
 
 int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *stream) {
     if (!bt || !psi || !y) return fail(QR_EINVAL, "qr_batch_apply: null argument");
@@ -1373,52 +1467,93 @@ int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *s
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int rc = batch_upload_ptrs(bt, psi, y, st);
     if (rc) return rc;
+    if (bt->exec && bt->mode == 1 && bt->ptrs_changed) {
+        // per-operator graph nodes carry the state pointers: capture again
+        rc = instantiate_per_op(bt);
+        if (rc) return rc;
+    }
+    bt->ptrs_changed = false;
     if (!bt->exec) {
-        // autotuner: time each candidate tile width on these buffers
+        // autotuner: time each candidate on these buffers -- the persistent
+        // work-list kernel at tile widths 2^12, 2^11, 2^10, and a graph of
+        // one per-operator kernel each
         int best = -1;
         float best_ms = 0.f;
         cudaEvent_t e0, e1;
         QR_CUDA(cudaEventCreate(&e0), "event");
         QR_CUDA(cudaEventCreate(&e1), "event");
-        for (int tb : {12, 11, 10}) {
-            rc = batch_build(bt, tb);
-            if (rc) break;
-            BatchArgs a = batch_args(bt);
-            cudaError_t e = launch_batch_c64c(a, bt->nsm, bt->cap);
+        auto timed = [&](auto &&launch, float *ms) -> cudaError_t {
+            cudaError_t e = launch();
             if (e == cudaSuccess) e = cudaEventRecord(e0, bt->cap);
-            for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = launch_batch_c64c(a, bt->nsm, bt->cap);
+            for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = launch();
             if (e == cudaSuccess) e = cudaEventRecord(e1, bt->cap);
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-            float ms = 0.f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-            if (e != cudaSuccess) {
-                rc = cuda_fail(e, "qr_batch autotune");
-                break;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+            return e;
+        };
+        if (bt->force_mode != 1) {
+            for (int tb : {12, 11, 10}) {
+                rc = batch_build(bt, tb);
+                if (rc) break;
+                BatchArgs a = batch_args(bt);
+                float ms = 0.f;
+                cudaError_t e = timed([&] { return launch_batch_c64c(a, bt->nsm, bt->cap); }, &ms);
+                if (e != cudaSuccess) {
+                    rc = cuda_fail(e, "qr_batch autotune");
+                    break;
+                }
+                if (best < 0 || ms < best_ms) {
+                    best = tb;
+                    best_ms = ms;
+                }
             }
-            if (best < 0 || ms < best_ms) {
-                best = tb;
+        }
+        if (!rc && bt->force_mode != 0) {
+            for (size_t i = 0; i < bt->ops.size() && !rc; ++i)  // builds the plans
+                rc = apply_impl("qr_batch_apply", bt->ops[i], QR_C64C, bt->cur_psi[i],
+                                bt->cur_y[i], bt->nstates[i], 0, bt->cap, nullptr, nullptr,
+                                nullptr);
+            if (!rc) rc = instantiate_per_op(bt);
+            float ms = 0.f;
+            if (!rc) {
+                cudaError_t e = timed([&] { return cudaGraphLaunch(bt->exec, bt->cap); }, &ms);
+                if (e != cudaSuccess) rc = cuda_fail(e, "qr_batch autotune");
+            }
+            if (!rc && (best < 0 || ms < best_ms)) {
+                best = 0;  // per-operator graph
                 best_ms = ms;
             }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (rc) return rc;
-        rc = batch_build(bt, best);
-        if (rc) return rc;
-        BatchArgs a = batch_args(bt);
-        QR_CUDA(cudaStreamBeginCapture(bt->cap, cudaStreamCaptureModeRelaxed), "begin capture");
-        cudaError_t e = launch_batch_c64c(a, bt->nsm, bt->cap);
-        cudaError_t e2 = cudaStreamEndCapture(bt->cap, &bt->graph);
-        if (e != cudaSuccess) return cuda_fail(e, "batch launch under capture");
-        if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
-        QR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0), "graph instantiate");
+        if (best == 0) {
+            bt->mode = 1;
+            bt->tile_bits = 12;
+        } else {
+            drop_graph(bt);
+            bt->mode = 0;
+            rc = batch_build(bt, best);
+            if (rc) return rc;
+            BatchArgs a = batch_args(bt);
+            QR_CUDA(cudaStreamBeginCapture(bt->cap, cudaStreamCaptureModeRelaxed), "begin capture");
+            cudaError_t e = launch_batch_c64c(a, bt->nsm, bt->cap);
+            cudaError_t e2 = cudaStreamEndCapture(bt->cap, &bt->graph);
+            if (e != cudaSuccess) return cuda_fail(e, "batch launch under capture");
+            if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
+            QR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0), "graph instantiate");
+        }
         QR_CUDA(cudaStreamSynchronize(bt->cap), "autotune sync");
         int h = 0;
         QR_CUDA(cudaMemcpy(&h, bt->d_err.p, sizeof(int), cudaMemcpyDeviceToHost), "error word");
         if (h) return fail(QR_EKERNEL, "batched kernel reported error %d", h);
+        for (qr_op *op : bt->ops) {
+            rc = check_kernel_error(op);
+            if (rc) return rc;
+        }
     }
     QR_CUDA(cudaGraphLaunch(bt->exec, st), "graph launch");
-    count_launch();
+    count_launch(bt->mode == 1 ? bt->ops.size() : 1);  // kernels the graph runs
     return QR_OK;
 }
 

@@ -723,6 +723,16 @@ class Batch:
             pass
 
     @property
+    def mode(self) -> int:
+        """0: one persistent work-list kernel, 1: graph of per-operator
+        kernels (chosen by timing on the first apply); -1 before it."""
+        return int(_lib.load().qr_batch_mode(self._h))
+
+    def set_mode(self, mode: int) -> None:
+        """Fix the mode instead of timing (before the first apply)."""
+        check(_lib.load().qr_batch_set_mode(self._h, int(mode)))
+
+    @property
     def tile_bits(self) -> int:
         return int(_lib.load().qr_batch_tile_bits(self._h))
 

@@ -89,6 +89,19 @@ def test_fat_groups(cuda, oracle):
     assert op.info()["nfat"] >= 1
 
 
+@pytest.mark.parametrize("n,T", [(12, 2000), (14, 3000), (17, 1500)])
+def test_many_sub_groups(cuda, oracle, n, T):
+    """Random-letter operators with thousands of x groups: the compensated
+    kernel's factor table is rebuilt per chunk of <= 512 sub-groups; at n = 12
+    every group shares one partner tile, which is visited as several blocks."""
+    rng = np.random.default_rng(n * 1000 + T)
+    t = W.random_letters_op(rng, n, T)
+    c = t.coeff * (1 - 0.4j)
+    psi = W.random_state(rng, 1 << n)
+    op, _, _ = check(cuda, oracle, t.n, t.x, t.z, t.phase, c, psi)
+    assert op.info()["nsub"] > 512
+
+
 def test_small_diag_group_in_table(cuda, oracle):
     # x = 0 group of rank <= 4 stays a regular table group (no diagonal vector)
     n = 13

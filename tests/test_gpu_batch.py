@@ -39,7 +39,10 @@ def check_against_c128(ops, psis, ys):
     return worst
 
 
-def test_batch_uneven_small(cuda):
+@pytest.mark.parametrize("mode", [-1, 0, 1])
+def test_batch_uneven_small(cuda, mode):
+    """Both launch forms (persistent work-list kernel, graph of per-operator
+    kernels) and the timed choice between them."""
     rng = np.random.default_rng(42)
     terms, nstates = [], []
     for k in range(24):
@@ -54,8 +57,11 @@ def test_batch_uneven_small(cuda):
     nstates.append(2)
     ops, psis, ys = make_batch(terms, nstates, cuda, 1)
     b = Batch(ops, nstates)
+    assert b.mode == -1
+    b.set_mode(mode)
     b.apply(psis, ys)
     assert b.tile_bits in (10, 11, 12)
+    assert b.mode in ((0, 1) if mode == -1 else (mode,))
     assert check_against_c128(ops, psis, ys) <= 1e-6
     # graph replay with the same buffers, then with new output buffers
     import torch
@@ -68,6 +74,8 @@ def test_batch_uneven_small(cuda):
     torch.cuda.synchronize()
     for a_, b_ in zip(first, ys2):
         assert torch.equal(a_, b_)
+    with pytest.raises(Exception, match="already chosen"):
+        b.set_mode(0)
 
 
 def test_batch_matches_single_operator_kernel(cuda):
