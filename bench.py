@@ -362,7 +362,7 @@ def run_gpu_arm(args, t, desc):
                  # 1.25 TFLOP/s nominal (no measured FP64 peak is recorded)
                  "fp64_tflops": 8.0 * N * int(info["ngroups"]) / (ms128 / 1e3) / 1e12,
                  "fp64_frac_of_nominal": 8.0 * N * int(info["ngroups"]) / (ms128 / 1e3)
-                                         / 1.25e15,
+                                         / 1.25e12,
                  "hbm_achieved_gbs": ach128, "hbm_frac": ach128 / hbm},
         "speedup_c64c_vs_c128": ms128 / ms64,
         "rel_err": {"c64c_vs_c128_full": rel64},

@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from . import build as _build
+import importlib
 
 QR_OK = 0
 QR_EINVAL = -1
@@ -58,7 +58,7 @@ _lib = None
 
 
 def lib_path() -> str:
-    return _build.LIB
+    return importlib.import_module(__package__ + ".build").LIB
 
 
 def load(build_if_missing: bool = True):
@@ -66,6 +66,7 @@ def load(build_if_missing: bool = True):
     global _lib
     if _lib is not None:
         return _lib
+    _build = importlib.import_module(__package__ + ".build")  # loaded on first use only
     path = _build.LIB
     if not os.path.exists(path):
         if not build_if_missing:

@@ -409,10 +409,7 @@ __device__ __forceinline__ void big_group_c64(float2 (&A)[AMPS], float2 (&B)[AMP
 //     table read, the partner offset;
 //   * per run of sub-groups with equal register-bit sign pattern: one
 //     dispatch to a compile-time instantiation.
-#ifndef QR_TAB_STAGES
-#define QR_TAB_STAGES 4
-#endif
-constexpr int kTabStages = QR_TAB_STAGES;  // partner-tile ring depth (4 timed best of 3, 4, 5)
+constexpr int kTabStages = 4;  // partner-tile ring depth (timed best of 3, 4, 5)
 constexpr size_t kMaxSmemPerBlock = 227u * 1024u;  // sm_100-family opt-in limit
 constexpr int kTabEnt = 4;  // per-tile table entries (float4) per sub-group
 // full barriers, stage counters and the abort flag, rounded to 8 bytes
@@ -486,7 +483,7 @@ __device__ __forceinline__ void run_tab_dispatch(uint32_t key, float2 (&A)[AMPS]
 #undef QR_RUN_CASE
 }
 
-template <int AMPS, bool WIDE>
+template <int AMPS, bool WIDE, bool MULTI>
 __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t threads = blockDim.x;
@@ -507,7 +504,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
                                             (size_t)AMPS * threads * 8u + kTabBarBytes);
     uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + kTabCap);
     uint32_t *s_blk = s_run + kTabCap + 1;
-    if (a.nchunks == 1) {
+    if constexpr (!MULTI) {
         for (uint32_t i = t; i < a.nsub; i += threads) s_td[i] = a.tdesc[i];
         for (uint32_t i = t; i <= a.nruns; i += threads)
             s_run[i] = a.run_g0[i] | (i < a.nruns ? a.run_key[i] << 16 : 0u);
@@ -566,17 +563,17 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
             }
             cidx = 0;
         }
-        if (j == 0 || j == next_j) {
+        if (j == 0 || (MULTI && j == next_j)) {
             // table (and, with several chunks, run lists) of the chunk that
             // starts at block j: every warp has finished the previous one
             if (j != 0) ++cidx;
             __syncthreads();
-            const uint4 c0 = a.nchunks > 1 ? a.chunks[cidx] : make_uint4(0u, 0u, 0u, 0u);
-            const uint4 c1 = a.nchunks > 1 ? a.chunks[cidx + 1]
-                                           : make_uint4(a.nsub, a.nruns, a.nblocks, 0u);
-            cj0 = c0.z;
-            next_j = c1.z;
-            if (a.nchunks > 1) {
+            uint4 c0 = make_uint4(0u, 0u, 0u, 0u), c1 = make_uint4(a.nsub, a.nruns, a.nblocks, 0u);
+            if constexpr (MULTI) {
+                c0 = a.chunks[cidx];
+                c1 = a.chunks[cidx + 1];
+                cj0 = c0.z;
+                next_j = c1.z;
                 for (uint32_t i = t; i < c1.x - c0.x; i += threads) s_td[i] = a.tdesc[c0.x + i];
                 for (uint32_t i = t; i <= c1.y - c0.y; i += threads) {
                     const uint32_t r = c0.y + i;
@@ -622,7 +619,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
             }
         }
 
-        const uint32_t jl = j - cj0;
+        const uint32_t jl = MULTI ? j - cj0 : j;
         const uint32_t r1 = skip ? 0u : s_blk[jl + 1];
         uint32_t rw = s_run[s_blk[jl]];
         for (uint32_t r = s_blk[jl]; r < r1; ++r) {
@@ -703,7 +700,8 @@ static size_t tab_smem_bytes(const ApplyArgs &a, int threads) {
 template <int AMPS, bool WIDE>
 static cudaError_t launch_c64c_tab(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
     const size_t smem = tab_smem_bytes<AMPS>(a, threads);
-    auto kern = apply_c64c_tab<AMPS, WIDE>;
+    // one chunk (operators of up to 512 sub-groups): no chunk bookkeeping
+    auto kern = a.nchunks > 1 ? apply_c64c_tab<AMPS, WIDE, true> : apply_c64c_tab<AMPS, WIDE, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
