@@ -411,6 +411,23 @@ class SparsePauliOp:
         conv = "kron" if name in _KRON_MODES else "rowwise"
         return SpMat._from_op(self.operator(conv))
 
+    # pyqrusty/src/lib.rs:382-404 (qrusty/src/lib.rs:401-524): the same
+    # matrix through the named builders, all built on the GPU
+    def to_matrix_binary(self) -> "SpMat":
+        return self.to_matrix_mode("Binary")
+
+    def to_matrix_accel(self) -> "SpMat":
+        return self.to_matrix_mode("Accel")
+
+    def to_matrix_reduce(self) -> "SpMat":
+        return self.to_matrix_mode("Reduce")
+
+    def to_matrix_rayon(self) -> "SpMat":
+        return self.to_matrix_mode("Rayon")
+
+    def to_matrix_rayon_chunked(self, step: int) -> "SpMat":
+        return self.to_matrix_mode("RayonChunked/%d" % int(step))
+
     def apply(self, psi, out=None, adjoint: bool = False):
         """Matrix-free y = H psi on the GPU (rowwise convention); see
         PauliOperator.apply."""

@@ -131,6 +131,10 @@ def test_i_plus_2x_all_modes(cuda):  # qrusty/src/lib.rs:775-813
     for mode in ["", "Binary", "Accel", "Rowwise", "RowwiseUnsafe", "RowwiseUnsafeChunked/500",
                  "Reduce", "Rayon", "RayonChunked/1"]:
         assert np.array_equal(csr_matrix(spop.to_matrix_mode(mode)).todense(), want)
+    # the named builders of pyqrusty's SparsePauliOp (pyqrusty/src/lib.rs:382-404)
+    for m in (spop.to_matrix(), spop.to_matrix_binary(), spop.to_matrix_accel(),
+              spop.to_matrix_reduce(), spop.to_matrix_rayon(), spop.to_matrix_rayon_chunked(1)):
+        assert np.array_equal(csr_matrix(m).todense(), want)
 
 
 def test_export_moves(cuda):  # pyqrusty/src/lib.rs:190-214
