@@ -665,7 +665,21 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
                 cnt[s] = 0;
                 if (L + (uint64_t)kTabStages < total && *s_abort == 0) {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    issue(L + (uint64_t)kTabStages);
+                    // step kTabStages partner blocks ahead of (st, q, j) with
+                    // adds only (no 64-bit division on the steady-state path)
+                    uint32_t j2 = j + (uint32_t)kTabStages;
+                    uint64_t q2 = q, st2 = st;
+                    while (j2 >= nb) {
+                        j2 -= nb;
+                        q2 += gridDim.x;
+                        while (q2 >= a.ntiles) {
+                            q2 -= a.ntiles;
+                            ++st2;
+                        }
+                    }
+                    const float2 *src = psi + st2 * a.N + ((q2 ^ a.blk_hi[j2]) << a.b);
+                    mbar_expect_tx(&full[s], tile_bytes);
+                    bulk_g2s(smem_raw + (size_t)s * tile_bytes, src, tile_bytes, &full[s]);
                 }
             }
         }

@@ -191,6 +191,7 @@ struct CsrArgs {
     const uint32_t *fold;     // groups in fold mode
     uint32_t nfold;
     const double2 *ctab;      // class tables
+    uint32_t nctab;           // class-table entries
     const uint64_t *tz;       // terms in group-stable order (fold mode)
     const double *tc;         // 2 doubles per term
     uint64_t *indptr, *indices;

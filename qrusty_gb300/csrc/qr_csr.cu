@@ -78,6 +78,7 @@ __device__ __forceinline__ uint32_t csr_class(const CsrGroup &d, W r) {
 constexpr int kCsrThreads = 256;
 constexpr uint32_t kCsrSmemSig = 12288;  // sigma entries staged in shared memory (48 KB)
 constexpr size_t kCsrLutBytes = 64u * 1024u;
+constexpr uint32_t kCsrSmemCtab = 2048;  // class-table entries staged in shared memory (32 KB)
 
 // Low-bit width of the per-group position lookup table: G x (2^L + 1)
 // 32-bit entries (rows padded by one word so lanes on consecutive groups hit
@@ -108,6 +109,11 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_kernel(const CsrArgs a) 
             const W pm = (W)a.pmask[g] & (((W)1 << L) - 1) & (W)v;
             s_dyn[i] = v < (1u << L) ? sigma_sum<W>(pm, a.sig + (size_t)g * (uint32_t)a.n) : 0;
         }
+        // class tables next to the position table when they fit
+        double2 *s_ctab = reinterpret_cast<double2 *>(s_dyn + ((G * lsz + 3u) & ~3u));
+        const bool ctab_smem = a.nctab <= kCsrSmemCtab;
+        if (ctab_smem)
+            for (uint32_t i = threadIdx.x; i < a.nctab; i += kCsrThreads) s_ctab[i] = a.ctab[i];
         __syncthreads();
         const uint32_t rpp = kCsrThreads / G;
         const uint32_t t = threadIdx.x;
@@ -119,7 +125,7 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_kernel(const CsrArgs a) 
         const W lomask = ((W)1 << L) - 1;
         const int32_t *sg = a.sig + (size_t)g * (uint32_t)a.n;
         const int32_t *lut = s_dyn + g * lsz;
-        const double2 *tab = a.ctab + d.tab;
+        const double2 *tab = (ctab_smem ? s_ctab : a.ctab) + d.tab;
         const uint64_t nchunk = (a.nrows + lomask) >> L;
         for (uint64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
             const uint64_t rr0 = ch << L;
@@ -201,7 +207,8 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
     if (a.G <= (uint64_t)kCsrThreads) {
         const int L = csr_lut_bits((uint32_t)a.G);
         g = (a.nrows + (1u << L) - 1) >> L;
-        smem = (size_t)a.G * ((1u << L) + 1) * sizeof(int32_t);
+        smem = (((size_t)a.G * ((1u << L) + 1) + 3u) & ~(size_t)3u) * sizeof(int32_t);
+        if (a.nctab <= kCsrSmemCtab) smem += (size_t)a.nctab * sizeof(double2);
     } else {
         g = a.nrows;
         const uint64_t nsig = a.G * (uint64_t)a.n;
@@ -210,7 +217,7 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
     if (g > (uint64_t)nsm * 8) g = (uint64_t)nsm * 8;
     auto kern = a.n > 32 ? csr_fill_kernel<true> : csr_fill_kernel<false>;
     cudaError_t e0 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)kCsrLutBytes + 4096);
+                                          (int)(kCsrLutBytes + kCsrSmemCtab * sizeof(double2)) + 64);
     if (e0 != cudaSuccess) return e0;
     kern<<<(unsigned)g, kCsrThreads, smem, st>>>(a);
     count_launch();
@@ -227,7 +234,7 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
 }
 
 // y = A v, complex128.  S lanes per row: the lanes of a row stride its
-// entries two at a time (independent loads in flight), then combine their
+// entries four at a time (independent loads in flight), then combine their
 // partial sums with a butterfly over the S lanes.
 // Replaces spmat_dot_densevec (qrusty/src/accel.rs:338-370).
 template <int S>
@@ -244,21 +251,27 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, uint64_t 
         const uint64_t j0 = indptr[r], j1 = indptr[r + 1];
         double sr = 0.0, si = 0.0, tr = 0.0, ti = 0.0;
         uint64_t j = j0 + sl;
-        for (; j + S < j1; j += 2 * S) {
-            const uint64_t c0 = indices[j], c1 = indices[j + S];
-            const double2 d0 = data[j], d1 = data[j + S];
-            if (c0 < ncols) {
-                const double2 x0 = v[c0];
-                sr = fma(d0.x, x0.x, fma(-d0.y, x0.y, sr));
-                si = fma(d0.x, x0.y, fma(d0.y, x0.x, si));
+        // four entries per lane per step: their loads are in flight together
+        for (; j + 3 * S < j1; j += 4 * S) {
+            uint64_t c[4];
+            double2 d[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                c[u] = indices[j + u * S];
+                d[u] = data[j + u * S];
             }
-            if (c1 < ncols) {
-                const double2 x1 = v[c1];
-                tr = fma(d1.x, x1.x, fma(-d1.y, x1.y, tr));
-                ti = fma(d1.x, x1.y, fma(d1.y, x1.x, ti));
+            double2 x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) x[u] = c[u] < ncols ? v[c[u]] : make_double2(0.0, 0.0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (c[u] >= ncols) continue;  // out-of-range columns are skipped
+                double &ar = (u & 1) ? tr : sr, &ai = (u & 1) ? ti : si;
+                ar = fma(d[u].x, x[u].x, fma(-d[u].y, x[u].y, ar));
+                ai = fma(d[u].x, x[u].y, fma(d[u].y, x[u].x, ai));
             }
         }
-        if (j < j1) {
+        for (; j < j1; j += S) {
             const uint64_t c = indices[j];  // out-of-range columns are skipped
             if (c < ncols) {
                 const double2 d = data[j];

@@ -128,7 +128,7 @@ struct qr_op {
     std::vector<uint64_t> pmask;        // per group: bits with a nonzero sigma
     std::vector<int32_t> sig;           // G x n: sigma_{g,b}
     bool csr_uploaded = false;
-    uint32_t nfold = 0;
+    uint32_t nfold = 0, nctab = 0;
     DevBuf d_gx, d_goff, d_tz, d_tc, d_pmask, d_sig, d_grp, d_ctab, d_fold;
     // merged terms (FP64 simplification) for qr_apply; mmap[k] = merged index
     std::vector<uint64_t> mx, mz;
@@ -268,6 +268,7 @@ int upload_csr_tables(qr_op *op) {
     QR_CUDA(op->d_sig.upload(op->sig), "upload position table");
     QR_CUDA(op->d_grp.upload(grp), "upload group descriptors");
     QR_CUDA(op->d_ctab.upload(ctab), "upload class tables");
+    op->nctab = (uint32_t)ctab.size();
     QR_CUDA(op->d_fold.upload(fold), "upload fold groups");
     op->nfold = (uint32_t)fold.size();
     op->csr_uploaded = true;
@@ -878,6 +879,7 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, i
     a.fold = op->d_fold.as<uint32_t>();
     a.nfold = op->nfold;
     a.ctab = op->d_ctab.as<double2>();
+    a.nctab = op->nctab;
     a.tz = op->d_tz.as<uint64_t>();
     a.tc = op->d_tc.as<double>();
     a.err = op->d_err.as<int>();

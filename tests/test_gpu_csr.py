@@ -158,3 +158,32 @@ def test_device_build_matches_host(cuda):
     assert np.array_equal(di.cpu().numpy().view(np.uint64), hi)
     assert np.array_equal(dj.cpu().numpy().view(np.uint64), hj)
     assert np.array_equal(_bits(dd.cpu().numpy()), _bits(hd))
+
+
+def test_spmv_skips_out_of_range_columns(cuda):
+    """qr_csr_spmv skips entries whose column is >= ncols (even when their
+    value is not finite), for rows shorter and longer than the unrolled step."""
+    import scipy.sparse as sps
+    import torch
+    from qrusty_gb300 import _lib
+    rng = np.random.default_rng(2)
+    nrows, ncols = 37, 50
+    lens = rng.integers(0, 90, nrows)
+    indptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    nnz = int(indptr[-1])
+    indices = rng.integers(0, ncols + 20, nnz).astype(np.int64)
+    data = rng.standard_normal(nnz) + 1j * rng.standard_normal(nnz)
+    data[indices >= ncols] = np.inf
+    v = rng.standard_normal(ncols) + 1j * rng.standard_normal(ncols)
+    keep = indices < ncols
+    A = sps.csr_matrix((np.where(keep, data, 0), np.where(keep, indices, 0), indptr),
+                       shape=(nrows, ncols))
+    want = A @ v
+    d = lambda a: torch.from_numpy(a).to(cuda)
+    ip, ij, dd, vd = d(indptr), d(indices), d(data), d(v)
+    y = torch.empty(nrows, dtype=torch.complex128, device=cuda)
+    _lib.check(_lib.load().qr_csr_spmv(nrows, ncols, ip.data_ptr(), ij.data_ptr(), dd.data_ptr(),
+                                       vd.data_ptr(), y.data_ptr(), None))
+    got = y.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-12)
