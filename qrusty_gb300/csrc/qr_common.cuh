@@ -176,7 +176,8 @@ struct CsrGroup {
     uint64_t beta[kCsrMaxRank];
     uint32_t d;       // rank of the z differences, or kCsrFold
     uint32_t tab;     // first class-table entry (2^(d+1) entries)
-    uint32_t pad0, pad1;
+    uint32_t zparts;  // fold mode: bit 0 every c'_k.re is +-0, bit 1 every c'_k.im is +-0
+    uint32_t pad1;
     uint32_t k0, k1;  // terms [k0, k1) in group-stable order (fold mode)
 };
 static_assert(sizeof(CsrGroup) == 64, "CsrGroup layout");

@@ -77,12 +77,12 @@ __device__ __forceinline__ uint32_t csr_class(const CsrGroup &d, W r) {
 
 constexpr int kCsrThreads = 256;
 constexpr uint32_t kCsrSmemSig = 12288;  // sigma entries staged in shared memory (48 KB)
-constexpr size_t kCsrLutBytes = 64u * 1024u;
+constexpr size_t kCsrLutBytes = 32u * 1024u;
 constexpr uint32_t kCsrSmemCtab = 2048;  // class-table entries staged in shared memory (32 KB)
 
 // Low-bit width of the per-group position lookup table: G x (2^L + 1)
 // 32-bit entries (rows padded by one word so lanes on consecutive groups hit
-// distinct banks) within 64 KB.  L <= 8, so 256-row launches stay aligned.
+// distinct banks) within 32 KB, so that six 256-thread blocks fit an SM.  L <= 8, so 256-row launches stay aligned.
 __host__ __device__ inline int csr_lut_bits(uint32_t G) {
     int L = 8;
     while (L > 1 && (size_t)G * ((1u << L) + 1) * 4u > kCsrLutBytes) --L;
@@ -125,25 +125,31 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_kernel(const CsrArgs a) 
         const W lomask = ((W)1 << L) - 1;
         const int32_t *sg = a.sig + (size_t)g * (uint32_t)a.n;
         const int32_t *lut = s_dyn + g * lsz;
-        const double2 *tab = (ctab_smem ? s_ctab : a.ctab) + d.tab;
         const uint64_t nchunk = (a.nrows + lomask) >> L;
-        for (uint64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
-            const uint64_t rr0 = ch << L;
-            const W base = (W)(a.row0 + rr0);
-            const int32_t phi = (int32_t)g + sigma_sum<W>(base & pm & ~lomask, sg);
-            const uint64_t rend = min(rr0 + ((uint64_t)1 << L), a.nrows);
-            // two rows per step: their table reads are in flight together
-            for (uint64_t rr = rr0 + rs; rr < rend; rr += 2 * (uint64_t)rpp) {
-                const uint64_t rr2 = rr + rpp;
-                const W r = (W)(a.row0 + rr), r2 = (W)(a.row0 + rr2);
-                const bool two = rr2 < rend;
-                const double2 v1 = tab[csr_class<W>(d, r)];
-                const double2 v2 = two ? tab[csr_class<W>(d, r2)] : v1;
-                csr_store(a, rr, phi + lut[(uint32_t)(r & lomask)], (uint64_t)(r ^ xg), v1);
-                if (two)
-                    csr_store(a, rr2, phi + lut[(uint32_t)(r2 & lomask)], (uint64_t)(r2 ^ xg), v2);
+        // the class table is read through a pointer of known state space
+        // (shared or global), so the loads are LDS / LDG, not generic
+        auto rows = [&](const double2 *tab) {
+            for (uint64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+                const uint64_t rr0 = ch << L;
+                const W base = (W)(a.row0 + rr0);
+                const int32_t phi = (int32_t)g + sigma_sum<W>(base & pm & ~lomask, sg);
+                const uint64_t rend = min(rr0 + ((uint64_t)1 << L), a.nrows);
+                // two rows per step: their table reads are in flight together
+                for (uint64_t rr = rr0 + rs; rr < rend; rr += 2 * (uint64_t)rpp) {
+                    const uint64_t rr2 = rr + rpp;
+                    const W r = (W)(a.row0 + rr), r2 = (W)(a.row0 + rr2);
+                    const bool two = rr2 < rend;
+                    const double2 v1 = tab[csr_class<W>(d, r)];
+                    const double2 v2 = two ? tab[csr_class<W>(d, r2)] : v1;
+                    csr_store(a, rr, phi + lut[(uint32_t)(r & lomask)], (uint64_t)(r ^ xg), v1);
+                    if (two)
+                        csr_store(a, rr2, phi + lut[(uint32_t)(r2 & lomask)], (uint64_t)(r2 ^ xg),
+                                  v2);
+                }
             }
-        }
+        };
+        if (ctab_smem) rows(s_ctab + d.tab);
+        else rows(a.ctab + d.tab);
     } else {
         const uint64_t nsig = (uint64_t)G * (uint32_t)a.n;
         const bool staged = nsig <= kCsrSmemSig;
@@ -168,6 +174,36 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_kernel(const CsrArgs a) 
 // Fold-mode groups (z span wider than kCsrMaxRank): one thread per row, all
 // lanes of a warp on the same group, the group's +-c'_k folded in input-term
 // order from the first term (make_row's fold), terms read warp-uniformly.
+// A part (re or im) whose every coefficient is +-0 takes no FP64 additions:
+// under round-to-nearest a sum of signed zeros is -0 exactly when every
+// addend is -0, so the fold's result is -0 iff each +-c'_k part is -0.
+template <bool RZ, bool IZ>
+__device__ __forceinline__ double2 csr_fold_row(const CsrArgs &a, uint64_t r, uint32_t k0,
+                                                uint32_t k1) {
+    const uint64_t *tz = a.tz;
+    const double *tc = a.tc;
+    double vr = 0.0, vi = 0.0;
+    uint32_t nr = 1u, ni = 1u;  // every addend so far -0 (zero parts)
+    for (uint32_t k = k0; k < k1; ++k) {
+        const uint32_t neg = (uint32_t)__popcll(r & tz[k]) & 1u;
+        if constexpr (RZ) {
+            nr &= neg ^ (uint32_t)signbit(tc[2 * k]);
+        } else {
+            const double cr = neg ? -tc[2 * k] : tc[2 * k];
+            vr = k == k0 ? cr : __dadd_rn(vr, cr);
+        }
+        if constexpr (IZ) {
+            ni &= neg ^ (uint32_t)signbit(tc[2 * k + 1]);
+        } else {
+            const double ci = neg ? -tc[2 * k + 1] : tc[2 * k + 1];
+            vi = k == k0 ? ci : __dadd_rn(vi, ci);
+        }
+    }
+    if constexpr (RZ) vr = nr ? -0.0 : 0.0;
+    if constexpr (IZ) vi = ni ? -0.0 : 0.0;
+    return make_double2(vr, vi);
+}
+
 __global__ void __launch_bounds__(kCsrThreads) csr_fold_kernel(const CsrArgs a) {
     for (uint32_t f = blockIdx.y; f < a.nfold; f += gridDim.y) {
         const uint32_t g = a.fold[f];
@@ -177,17 +213,14 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fold_kernel(const CsrArgs a) 
         for (uint64_t rr = blockIdx.x * (uint64_t)kCsrThreads + threadIdx.x; rr < a.nrows;
              rr += (uint64_t)gridDim.x * kCsrThreads) {
             const uint64_t r = a.row0 + rr;
-            const uint32_t k0 = d.k0, k1 = d.k1;
-            const bool neg0 = (__popcll(r & a.tz[k0]) & 1) != 0;
-            double vr = neg0 ? -a.tc[2 * k0] : a.tc[2 * k0];
-            double vi = neg0 ? -a.tc[2 * k0 + 1] : a.tc[2 * k0 + 1];
-            for (uint32_t k = k0 + 1; k < k1; ++k) {
-                const bool neg = (__popcll(r & a.tz[k]) & 1) != 0;
-                vr = __dadd_rn(vr, neg ? -a.tc[2 * k] : a.tc[2 * k]);
-                vi = __dadd_rn(vi, neg ? -a.tc[2 * k + 1] : a.tc[2 * k + 1]);
+            double2 v;
+            switch (d.zparts & 3u) {  // warp-uniform
+                case 1: v = csr_fold_row<true, false>(a, r, d.k0, d.k1); break;
+                case 2: v = csr_fold_row<false, true>(a, r, d.k0, d.k1); break;
+                case 3: v = csr_fold_row<true, true>(a, r, d.k0, d.k1); break;
+                default: v = csr_fold_row<false, false>(a, r, d.k0, d.k1); break;
             }
-            csr_store(a, rr, (int32_t)g + sigma_sum<uint64_t>(r & pm, sg), r ^ xg,
-                      make_double2(vr, vi));
+            csr_store(a, rr, (int32_t)g + sigma_sum<uint64_t>(r & pm, sg), r ^ xg, v);
         }
     }
 }
@@ -214,11 +247,16 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
         const uint64_t nsig = a.G * (uint64_t)a.n;
         smem = nsig <= kCsrSmemSig ? (size_t)nsig * sizeof(int32_t) : 0;
     }
-    if (g > (uint64_t)nsm * 8) g = (uint64_t)nsm * 8;
     auto kern = a.n > 32 ? csr_fill_kernel<true> : csr_fill_kernel<false>;
     cudaError_t e0 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)(kCsrLutBytes + kCsrSmemCtab * sizeof(double2)) + 64);
     if (e0 != cudaSuccess) return e0;
+    // one wave of resident blocks striding the row chunks (no partial second wave)
+    int per_sm = 0;
+    e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCsrThreads, smem);
+    if (e0 != cudaSuccess) return e0;
+    if (per_sm < 1) per_sm = 1;
+    if (g > (uint64_t)nsm * per_sm) g = (uint64_t)nsm * per_sm;
     kern<<<(unsigned)g, kCsrThreads, smem, st>>>(a);
     count_launch();
     cudaError_t e = cudaGetLastError();
@@ -256,13 +294,13 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, uint64_t 
             uint64_t c[4];
             double2 d[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                c[u] = indices[j + u * S];
-                d[u] = data[j + u * S];
+            for (int u = 0; u < 4; ++u) {  // the matrix streams once: evict-first loads
+                c[u] = __ldcs(indices + j + u * S);
+                d[u] = __ldcs(data + j + u * S);
             }
             double2 x[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) x[u] = c[u] < ncols ? v[c[u]] : make_double2(0.0, 0.0);
+            for (int u = 0; u < 4; ++u) x[u] = c[u] < ncols ? __ldg(v + c[u]) : make_double2(0.0, 0.0);
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 if (c[u] >= ncols) continue;  // out-of-range columns are skipped

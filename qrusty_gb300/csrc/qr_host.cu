@@ -232,6 +232,14 @@ void build_csr_groups(const qr_op *op, std::vector<CsrGroup> &grp, std::vector<c
         if (sp.overflow) {
             d.d = kCsrFold;
             d.tab = 0;
+            // a part whose every coefficient is +-0 folds to a zero whose sign
+            // the kernel derives without FP64 additions
+            bool rz = true, iz = true;
+            for (uint32_t k = k0; k < k1; ++k) {
+                rz = rz && op->tc[k].re == 0.0;
+                iz = iz && op->tc[k].im == 0.0;
+            }
+            d.zparts = (rz ? 1u : 0u) | (iz ? 2u : 0u);
             fold.push_back((uint32_t)g);
             continue;
         }

@@ -94,6 +94,30 @@ def test_cancellation_zero_kept(cuda, oracle):
     assert np.count_nonzero(d == 0) == 4
 
 
+@pytest.mark.parametrize("kind", ["real", "imag", "neg_zero", "mixed"])
+def test_fold_group_signed_zero_parts(cuda, oracle, kind):
+    """A group whose z span exceeds the class-table rank is folded per row;
+    a part whose coefficients are all +-0 is formed without FP64 additions
+    and must carry the same zero sign as the term-order fold."""
+    rng = np.random.default_rng(7)
+    n, T = 9, 24
+    x = np.zeros(T, np.uint64)
+    z = rng.integers(1, 1 << n, T).astype(np.uint64)
+    z[3:9] = 1 << np.arange(6, dtype=np.uint64)  # GF(2) rank >= 6: fold mode
+    ph = rng.choice(np.array([0, 2], np.uint8), T)  # phase 2 flips the zero's sign
+    v = rng.uniform(-1, 1, T)
+    if kind == "real":
+        c = v + 0j
+    elif kind == "imag":
+        c = 1j * v
+    elif kind == "neg_zero":
+        c = np.array([complex(a, -0.0) for a in v])
+        ph[:] = 0
+    else:
+        c = np.array([complex(a, -0.0 if i % 3 else 0.0) for i, a in enumerate(v)])
+    check_csr(oracle, n, x, z, ph, c)
+
+
 @pytest.mark.parametrize("name", ["H2", "H4"])
 def test_reference_test_H(cuda, golden, name):
     """pyqrusty/tests/test_H.py:32-48 on the GPU build: kron path
