@@ -204,6 +204,121 @@ __device__ __forceinline__ double2 csr_fold_row(const CsrArgs &a, uint64_t r, ui
     return make_double2(vr, vi);
 }
 
+// ------------------------------------------------------------ staged fill
+// Rows are assembled in shared memory and leave the SM as contiguous TMA
+// bulk stores (cp.async.bulk shared -> global): a warp's entries of one row
+// land at permuted positions, which as direct global stores become many
+// partial-line L2 writes.  Two staging buffers of R rows (R a power of two
+// dividing the 2^L-row chunk) alternate, so the bulk store of one overlaps
+// the assembly of the next.  Entries of fold-mode groups are left unset in
+// the stage and written afterwards by csr_fold_kernel (same stream): a
+// per-row FP64 fold inside the staged pass holds every warp of the block at
+// the sub-chunk barrier for the length of its serial chain.
+constexpr size_t kCsrStageBytes = 24u * 1024u;  // one buffer: R rows x G x (8 + 16) bytes
+
+__host__ __device__ inline int csr_stage_rows(uint32_t G, int L) {
+    int R = 1 << L;
+    while (R > 2 && (size_t)R * G * 24u > kCsrStageBytes) R >>= 1;
+    return R;
+}
+
+__device__ __forceinline__ uint32_t csr_saddr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void csr_bulk_s2g(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+                 "r"(csr_saddr(src)), "r"(bytes)
+                 : "memory");
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kCsrThreads) csr_fill_staged_kernel(const CsrArgs a) {
+    using W = typename RowT<WIDE>::T;
+    extern __shared__ __align__(128) int32_t s_dyn[];
+    const uint32_t G = (uint32_t)a.G;
+    const int L = csr_lut_bits(G);
+    const uint32_t lsz = (1u << L) + 1;
+    const uint32_t t = threadIdx.x;
+    for (uint32_t i = t; i < G * lsz; i += kCsrThreads) {
+        const uint32_t g = i / lsz, v = i - g * lsz;
+        const W pm = (W)a.pmask[g] & (((W)1 << L) - 1) & (W)v;
+        s_dyn[i] = v < (1u << L) ? sigma_sum<W>(pm, a.sig + (size_t)g * (uint32_t)a.n) : 0;
+    }
+    double2 *s_ctab = reinterpret_cast<double2 *>(s_dyn + ((G * lsz + 3u) & ~3u));
+    const bool ctab_smem = a.nctab <= kCsrSmemCtab;
+    if (ctab_smem)
+        for (uint32_t i = t; i < a.nctab; i += kCsrThreads) s_ctab[i] = a.ctab[i];
+    // staging buffers, 128-byte aligned: per buffer R*G indices then R*G values
+    const uint32_t R = (uint32_t)csr_stage_rows(G, L);
+    const uint32_t ent = R * G;
+    const size_t head = ((size_t)((G * lsz + 3u) & ~3u) * 4u +
+                         (ctab_smem ? (size_t)a.nctab * sizeof(double2) : 0u) + 127u) &
+                        ~(size_t)127u;
+    unsigned char *stage = reinterpret_cast<unsigned char *>(s_dyn) + head;
+    const size_t buf_bytes = ((size_t)ent * 24u + 127u) & ~(size_t)127u;
+    __syncthreads();
+
+    const uint32_t rpp = kCsrThreads / G;
+    const uint32_t rs = t / G, g = t - rs * G;
+    const bool lane_on = t < rpp * G;  // idle threads still take every barrier
+    CsrGroup d{};
+    W xg = 0, pm = 0;
+    const int32_t *sg = a.sig;
+    bool active = false;
+    if (lane_on) {
+        d = a.grp[g];
+        active = d.d != kCsrFold;
+        xg = (W)a.gx[g];
+        pm = (W)a.pmask[g];
+        sg = a.sig + (size_t)g * (uint32_t)a.n;
+    }
+    const W lomask = ((W)1 << L) - 1;
+    const int32_t *lut = s_dyn + (lane_on ? g : 0u) * lsz;
+    const double2 *tab = (ctab_smem ? s_ctab : a.ctab) + d.tab;
+    const uint64_t nchunk = (a.nrows + lomask) >> L;
+    uint32_t k = 0;  // sub-chunks issued by this block: buffer k & 1
+    for (uint64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+        const uint64_t rr0 = ch << L;
+        const uint64_t rend = min(rr0 + ((uint64_t)1 << L), a.nrows);
+        const int32_t phi =
+            active ? (int32_t)g + sigma_sum<W>((W)(a.row0 + rr0) & pm & ~lomask, sg) : 0;
+        for (uint64_t sc = rr0; sc < rend; sc += R, ++k) {
+            const uint32_t rows = (uint32_t)min((uint64_t)R, rend - sc);
+            unsigned char *buf = stage + (size_t)(k & 1u) * buf_bytes;
+            uint64_t *s_idx = reinterpret_cast<uint64_t *>(buf);
+            double2 *s_val = reinterpret_cast<double2 *>(buf + (size_t)ent * 8u);
+            // the bulk store that last read this buffer (two sub-chunks ago)
+            // has finished reading it
+            if (t == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+            __syncthreads();
+            if (active) {
+#pragma unroll 2
+                for (uint32_t rl = rs; rl < rows; rl += rpp) {
+                    const W r = (W)(a.row0 + sc + rl);
+                    const double2 v = ctab_smem ? s_ctab[d.tab + csr_class<W>(d, r)]
+                                                : tab[csr_class<W>(d, r)];
+                    const int32_t pos = phi + lut[(uint32_t)(r & lomask)];
+                    if (pos < 0 || (uint32_t)pos >= G) {  // cannot happen for a valid trie table
+                        atomicExch(a.err, kErrCsrPos);
+                        continue;
+                    }
+                    s_idx[rl * G + (uint32_t)pos] = (uint64_t)(r ^ xg);
+                    s_val[rl * G + (uint32_t)pos] = v;
+                }
+            }
+            // shared writes visible to the bulk-copy (async) proxy
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (t == 0) {
+                csr_bulk_s2g(a.indices + sc * G, s_idx, rows * G * 8u);
+                csr_bulk_s2g(a.data + 2 * sc * G, s_val, rows * G * 16u);
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            }
+        }
+    }
+    if (t == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
 __global__ void __launch_bounds__(kCsrThreads) csr_fold_kernel(const CsrArgs a) {
     for (uint32_t f = blockIdx.y; f < a.nfold; f += gridDim.y) {
         const uint32_t g = a.fold[f];
@@ -225,6 +340,19 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fold_kernel(const CsrArgs a) 
     }
 }
 
+// fold-mode groups, after the fill kernel on the same stream
+static cudaError_t launch_csr_fold(const CsrArgs &a, int nsm, cudaStream_t st) {
+    if (a.nfold == 0) return cudaSuccess;
+    uint64_t gx = (a.nrows + kCsrThreads - 1) / kCsrThreads;
+    const uint32_t gy = a.nfold < 65535u ? a.nfold : 65535u;
+    uint64_t cap = ((uint64_t)nsm * 8 + gy - 1) / gy;
+    if (cap < 1) cap = 1;
+    if (gx > cap) gx = cap;
+    csr_fold_kernel<<<dim3((unsigned)gx, gy), kCsrThreads, 0, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
     if (a.row0 == 0 && a.indptr != nullptr) {
         uint64_t g = (a.N + 1 + 255) / 256;
@@ -237,11 +365,33 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
     if (a.nrows == 0 || a.G == 0) return cudaSuccess;
     size_t smem;
     uint64_t g;
+    const bool aligned = ((uintptr_t)a.indices % 16u) == 0 && ((uintptr_t)a.data % 16u) == 0;
     if (a.G <= (uint64_t)kCsrThreads) {
         const int L = csr_lut_bits((uint32_t)a.G);
         g = (a.nrows + (1u << L) - 1) >> L;
         smem = (((size_t)a.G * ((1u << L) + 1) + 3u) & ~(size_t)3u) * sizeof(int32_t);
         if (a.nctab <= kCsrSmemCtab) smem += (size_t)a.nctab * sizeof(double2);
+        // staged path: every bulk store a whole number of 16-byte units
+        // (even row counts) from 16-byte aligned outputs
+        if (aligned && L >= 1 && a.nrows % 2 == 0) {
+            const uint32_t R = (uint32_t)csr_stage_rows((uint32_t)a.G, L);
+            const size_t buf = ((size_t)R * a.G * 24u + 127u) & ~(size_t)127u;
+            const size_t sm = ((smem + 127u) & ~(size_t)127u) + 2 * buf;
+            auto kern = a.n > 32 ? csr_fill_staged_kernel<true> : csr_fill_staged_kernel<false>;
+            cudaError_t e0 =
+                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e0 != cudaSuccess) return e0;
+            int per_sm = 0;
+            e0 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCsrThreads, sm);
+            if (e0 != cudaSuccess) return e0;
+            if (per_sm < 1) per_sm = 1;
+            if (g > (uint64_t)nsm * per_sm) g = (uint64_t)nsm * per_sm;
+            kern<<<(unsigned)g, kCsrThreads, sm, st>>>(a);
+            count_launch();
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+            return launch_csr_fold(a, nsm, st);
+        }
     } else {
         g = a.nrows;
         const uint64_t nsig = a.G * (uint64_t)a.n;
@@ -260,15 +410,8 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
     kern<<<(unsigned)g, kCsrThreads, smem, st>>>(a);
     count_launch();
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess || a.nfold == 0) return e;
-    uint64_t gx = (a.nrows + kCsrThreads - 1) / kCsrThreads;
-    const uint32_t gy = a.nfold < 65535u ? a.nfold : 65535u;
-    uint64_t cap = ((uint64_t)nsm * 8 + gy - 1) / gy;
-    if (cap < 1) cap = 1;
-    if (gx > cap) gx = cap;
-    csr_fold_kernel<<<dim3((unsigned)gx, gy), kCsrThreads, 0, st>>>(a);
-    count_launch();
-    return cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_csr_fold(a, nsm, st);
 }
 
 // y = A v, complex128.  S lanes per row: the lanes of a row stride its
