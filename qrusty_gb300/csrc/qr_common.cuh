@@ -171,13 +171,17 @@ cudaError_t launch_diag(int dtype, int n, int db, uint64_t ntiles, const uint64_
 // span has rank > kCsrMaxRank, the term range to fold per row.
 constexpr int kCsrMaxRank = 4;
 constexpr uint32_t kCsrFold = 0xffffffffu;
+// Fold-mode groups: the longest leading run of terms whose z differences
+// span rank <= kCsrPrefixRank is folded per class on the host (table of
+// 2^(rank+1) entries); rows add only the terms after it.
+constexpr int kCsrPrefixRank = 10;
 struct CsrGroup {
     uint64_t z0;
     uint64_t beta[kCsrMaxRank];
     uint32_t d;       // rank of the z differences, or kCsrFold
     uint32_t tab;     // first class-table entry (2^(d+1) entries)
     uint32_t zparts;  // fold mode: bit 0 every c'_k.re is +-0, bit 1 every c'_k.im is +-0
-    uint32_t pad1;
+    uint32_t pre;     // fold mode: prefix terms (bits 0-23) folded per class, prefix rank << 24
     uint32_t k0, k1;  // terms [k0, k1) in group-stable order (fold mode)
 };
 static_assert(sizeof(CsrGroup) == 64, "CsrGroup layout");
@@ -195,6 +199,9 @@ struct CsrArgs {
     uint32_t nctab;           // class-table entries
     const uint64_t *tz;       // terms in group-stable order (fold mode)
     const double *tc;         // 2 doubles per term
+    const uint64_t *pbeta;    // nfold x kCsrPrefixRank: prefix span bases (fold mode)
+    const double2 *ptab;      // prefix class tables (fold mode)
+    double2 *fvals;           // nfold x nrows fold-mode values, or null (written in place)
     uint64_t *indptr, *indices;
     double *data;
     uint64_t row0, nrows;     // rows to fill

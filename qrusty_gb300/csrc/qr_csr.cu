@@ -77,12 +77,13 @@ __device__ __forceinline__ uint32_t csr_class(const CsrGroup &d, W r) {
 
 constexpr int kCsrThreads = 256;
 constexpr uint32_t kCsrSmemSig = 12288;  // sigma entries staged in shared memory (48 KB)
-constexpr size_t kCsrLutBytes = 32u * 1024u;
+constexpr size_t kCsrLutBytes = 16u * 1024u;
 constexpr uint32_t kCsrSmemCtab = 2048;  // class-table entries staged in shared memory (32 KB)
 
 // Low-bit width of the per-group position lookup table: G x (2^L + 1)
 // 32-bit entries (rows padded by one word so lanes on consecutive groups hit
-// distinct banks) within 32 KB, so that six 256-thread blocks fit an SM.  L <= 8, so 256-row launches stay aligned.
+// distinct banks) within 16 KB, so that with the staging buffers four
+// 256-thread blocks fit an SM's 228 KB.  L <= 8, so 256-row launches stay aligned.
 __host__ __device__ inline int csr_lut_bits(uint32_t G) {
     int L = 8;
     while (L > 1 && (size_t)G * ((1u << L) + 1) * 4u > kCsrLutBytes) --L;
@@ -174,29 +175,48 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_kernel(const CsrArgs a) 
 // Fold-mode groups (z span wider than kCsrMaxRank): one thread per row, all
 // lanes of a warp on the same group, the group's +-c'_k folded in input-term
 // order from the first term (make_row's fold), terms read warp-uniformly.
-// A part (re or im) whose every coefficient is +-0 takes no FP64 additions:
-// under round-to-nearest a sum of signed zeros is -0 exactly when every
-// addend is -0, so the fold's result is -0 iff each +-c'_k part is -0.
+// The leading terms up to z-span rank kCsrPrefixRank come from the host's
+// per-class fold of them (same additions, same order); the rest are added
+// per row.  A part (re or im) whose every coefficient is +-0 takes no FP64
+// additions: under round-to-nearest a sum of signed zeros is -0 exactly when
+// every addend is -0, so the fold's result is -0 iff each +-c'_k part is -0.
 template <bool RZ, bool IZ>
-__device__ __forceinline__ double2 csr_fold_row(const CsrArgs &a, uint64_t r, uint32_t k0,
-                                                uint32_t k1) {
+__device__ __forceinline__ double2 csr_fold_row(const CsrArgs &a, uint64_t r, const CsrGroup &d,
+                                                uint32_t f) {
     const uint64_t *tz = a.tz;
     const double *tc = a.tc;
     double vr = 0.0, vi = 0.0;
     uint32_t nr = 1u, ni = 1u;  // every addend so far -0 (zero parts)
-    for (uint32_t k = k0; k < k1; ++k) {
-        const uint32_t neg = (uint32_t)__popcll(r & tz[k]) & 1u;
+    uint32_t k = d.k0;
+    const uint32_t m = d.pre & 0xffffffu;
+    if (m != 0) {
+        // the fold of the leading m terms, looked up by the row's sign class
+        const uint32_t dp = d.pre >> 24;
+        const uint64_t *pb = a.pbeta + (size_t)f * kCsrPrefixRank;
+        uint32_t c = (uint32_t)__popcll(r & d.z0) & 1u;
+        for (uint32_t j = 0; j < dp; ++j) c |= ((uint32_t)__popcll(r & pb[j]) & 1u) << (j + 1);
+        const double2 v = a.ptab[d.tab + c];
+        vr = v.x;
+        vi = v.y;
+        nr = (uint32_t)signbit(v.x);
+        ni = (uint32_t)signbit(v.y);
+        k += m;
+    }
+    for (; k < d.k1; ++k) {
+        // sign applied to the bit pattern: no floating-point negation
+        const uint64_t sb = (uint64_t)(__popcll(r & tz[k]) & 1) << 63;
         if constexpr (RZ) {
-            nr &= neg ^ (uint32_t)signbit(tc[2 * k]);
+            nr &= (uint32_t)(sb >> 63) ^ (uint32_t)signbit(tc[2 * k]);
         } else {
-            const double cr = neg ? -tc[2 * k] : tc[2 * k];
-            vr = k == k0 ? cr : __dadd_rn(vr, cr);
+            const double cr = __longlong_as_double(__double_as_longlong(tc[2 * k]) ^ (long long)sb);
+            vr = k == d.k0 ? cr : __dadd_rn(vr, cr);
         }
         if constexpr (IZ) {
-            ni &= neg ^ (uint32_t)signbit(tc[2 * k + 1]);
+            ni &= (uint32_t)(sb >> 63) ^ (uint32_t)signbit(tc[2 * k + 1]);
         } else {
-            const double ci = neg ? -tc[2 * k + 1] : tc[2 * k + 1];
-            vi = k == k0 ? ci : __dadd_rn(vi, ci);
+            const double ci =
+                __longlong_as_double(__double_as_longlong(tc[2 * k + 1]) ^ (long long)sb);
+            vi = k == d.k0 ? ci : __dadd_rn(vi, ci);
         }
     }
     if constexpr (RZ) vr = nr ? -0.0 : 0.0;
@@ -210,10 +230,13 @@ __device__ __forceinline__ double2 csr_fold_row(const CsrArgs &a, uint64_t r, ui
 // land at permuted positions, which as direct global stores become many
 // partial-line L2 writes.  Two staging buffers of R rows (R a power of two
 // dividing the 2^L-row chunk) alternate, so the bulk store of one overlaps
-// the assembly of the next.  Entries of fold-mode groups are left unset in
-// the stage and written afterwards by csr_fold_kernel (same stream): a
-// per-row FP64 fold inside the staged pass holds every warp of the block at
-// the sub-chunk barrier for the length of its serial chain.
+// the assembly of the next.  Fold-mode groups (per-row FP64 folds) are
+// computed first by csr_fold_kernel<true> into a row-major value buffer and
+// copied into the stage here: folded inside the staged pass, their serial
+// chains would hold every warp of the block at the sub-chunk barrier, and
+// stored in place after it, each entry becomes a DRAM read-modify-write of
+// a line the bulk store has already evicted.  Without a value buffer the
+// fold entries are left unset and stored afterwards by csr_fold_kernel<false>.
 constexpr size_t kCsrStageBytes = 24u * 1024u;  // one buffer: R rows x G x (8 + 16) bytes
 
 __host__ __device__ inline int csr_stage_rows(uint32_t G, int L) {
@@ -256,6 +279,10 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_staged_kernel(const CsrA
                         ~(size_t)127u;
     unsigned char *stage = reinterpret_cast<unsigned char *>(s_dyn) + head;
     const size_t buf_bytes = ((size_t)ent * 24u + 127u) & ~(size_t)127u;
+    // with precomputed fold values: high-bit position term of each fold-mode
+    // group for the current chunk
+    int32_t *s_phi = reinterpret_cast<int32_t *>(stage + 2 * buf_bytes);
+    const uint32_t nfv = a.fvals ? a.nfold : 0u;
     __syncthreads();
 
     const uint32_t rpp = kCsrThreads / G;
@@ -276,49 +303,133 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_staged_kernel(const CsrA
     const int32_t *lut = s_dyn + (lane_on ? g : 0u) * lsz;
     const double2 *tab = (ctab_smem ? s_ctab : a.ctab) + d.tab;
     const uint64_t nchunk = (a.nrows + lomask) >> L;
-    uint32_t k = 0;  // sub-chunks issued by this block: buffer k & 1
-    for (uint64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
-        const uint64_t rr0 = ch << L;
-        const uint64_t rend = min(rr0 + ((uint64_t)1 << L), a.nrows);
-        const int32_t phi =
-            active ? (int32_t)g + sigma_sum<W>((W)(a.row0 + rr0) & pm & ~lomask, sg) : 0;
-        for (uint64_t sc = rr0; sc < rend; sc += R, ++k) {
-            const uint32_t rows = (uint32_t)min((uint64_t)R, rend - sc);
-            unsigned char *buf = stage + (size_t)(k & 1u) * buf_bytes;
-            uint64_t *s_idx = reinterpret_cast<uint64_t *>(buf);
-            double2 *s_val = reinterpret_cast<double2 *>(buf + (size_t)ent * 8u);
-            // the bulk store that last read this buffer (two sub-chunks ago)
-            // has finished reading it
-            if (t == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-            __syncthreads();
-            if (active) {
-#pragma unroll 2
-                for (uint32_t rl = rs; rl < rows; rl += rpp) {
-                    const W r = (W)(a.row0 + sc + rl);
-                    const double2 v = ctab_smem ? s_ctab[d.tab + csr_class<W>(d, r)]
-                                                : tab[csr_class<W>(d, r)];
-                    const int32_t pos = phi + lut[(uint32_t)(r & lomask)];
-                    if (pos < 0 || (uint32_t)pos >= G) {  // cannot happen for a valid trie table
-                        atomicExch(a.err, kErrCsrPos);
-                        continue;
-                    }
-                    s_idx[rl * G + (uint32_t)pos] = (uint64_t)(r ^ xg);
-                    s_val[rl * G + (uint32_t)pos] = v;
-                }
-            }
-            // shared writes visible to the bulk-copy (async) proxy
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncthreads();
-            if (t == 0) {
-                csr_bulk_s2g(a.indices + sc * G, s_idx, rows * G * 8u);
-                csr_bulk_s2g(a.data + 2 * sc * G, s_val, rows * G * 16u);
-                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    // fold-mode entries: with nfold * R <= threads, thread t owns item
+    // (f = t / R, rl = t % R) of every sub-chunk and copies its value into a
+    // 3-slot shared ring two sub-chunks ahead (cp.async: no register waits
+    // on the load; the values come from DRAM, the fill's write stream
+    // having evicted them from L2)
+    const bool ring = nfv > 0 && nfv * R <= (uint32_t)kCsrThreads;
+    const uint32_t f_it = t / R, rl_it = t - (t / R) * R;
+    const bool own = ring && f_it < nfv;
+    const uint32_t g_it = own ? a.fold[f_it] : 0u;
+    const uint64_t x_it = own ? a.gx[g_it] : 0ull;
+    double2 *s_fv = reinterpret_cast<double2 *>(s_phi + ((nfv + 3u) & ~3u));  // 3 x nfv*R
+    auto next_sub = [&](uint64_t &c, uint64_t &s0) {
+        const uint64_t e = min((c << L) + ((uint64_t)1 << L), a.nrows);
+        s0 += R;
+        if (s0 >= e) {
+            c += gridDim.x;
+            s0 = c << L;
+        }
+    };
+    auto prefetch = [&](uint64_t c, uint64_t s0, uint32_t slot) {
+        if (own && c < nchunk) {
+            const uint32_t rows = (uint32_t)min((uint64_t)R, min((c << L) + ((uint64_t)1 << L),
+                                                                   a.nrows) - s0);
+            if (rl_it < rows) {
+                const double2 *src = a.fvals + (size_t)f_it * a.nrows + s0 + rl_it;
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                                 csr_saddr(s_fv + (size_t)slot * nfv * R + t)),
+                             "l"(src)
+                             : "memory");
             }
         }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    uint32_t k = 0;  // sub-chunks issued by this block: buffer k & 1, ring slot k % 3
+    uint64_t ch = blockIdx.x, sc = ch << L;
+    uint64_t chA = ch, scA = sc, chB, scB;  // sub-chunks k + 1 and k + 2
+    next_sub(chA, scA);
+    chB = chA;
+    scB = scA;
+    next_sub(chB, scB);
+    if (ring) {
+        prefetch(ch, sc, 0);
+        prefetch(chA, scA, 1);
     }
+    int32_t phi = 0;
+    while (ch < nchunk) {
+        const uint64_t rr0 = ch << L;
+        const uint64_t rend = min(rr0 + ((uint64_t)1 << L), a.nrows);
+        const uint32_t rows = (uint32_t)min((uint64_t)R, rend - sc);
+        unsigned char *buf = stage + (size_t)(k & 1u) * buf_bytes;
+        uint64_t *s_idx = reinterpret_cast<uint64_t *>(buf);
+        double2 *s_val = reinterpret_cast<double2 *>(buf + (size_t)ent * 8u);
+        // the bulk store that last read this buffer (two sub-chunks ago) has
+        // finished reading it
+        if (t == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+        if (sc == rr0) {  // chunk start: high-bit position terms
+            phi = active ? (int32_t)g + sigma_sum<W>((W)(a.row0 + rr0) & pm & ~lomask, sg) : 0;
+            // (the previous sub-chunk's barrier has retired every reader of s_phi)
+            for (uint32_t f = t; f < nfv; f += kCsrThreads) {
+                const uint32_t gf = a.fold[f];
+                s_phi[f] = (int32_t)gf + sigma_sum<W>((W)(a.row0 + rr0) & (W)a.pmask[gf] & ~lomask,
+                                                      a.sig + (size_t)gf * (uint32_t)a.n);
+            }
+        }
+        __syncthreads();
+        if (ring) prefetch(chB, scB, (k + 2) % 3u);
+        if (active) {
+#pragma unroll 2
+            for (uint32_t rl = rs; rl < rows; rl += rpp) {
+                const W r = (W)(a.row0 + sc + rl);
+                const double2 v =
+                    ctab_smem ? s_ctab[d.tab + csr_class<W>(d, r)] : tab[csr_class<W>(d, r)];
+                const int32_t pos = phi + lut[(uint32_t)(r & lomask)];
+                if (pos < 0 || (uint32_t)pos >= G) {  // cannot happen for a valid trie table
+                    atomicExch(a.err, kErrCsrPos);
+                    continue;
+                }
+                s_idx[rl * G + (uint32_t)pos] = (uint64_t)(r ^ xg);
+                s_val[rl * G + (uint32_t)pos] = v;
+            }
+        }
+        // fold-mode entries from the values the fold pass wrote
+        auto place = [&](uint32_t f, uint32_t rl, uint32_t gf, uint64_t xf, double2 v) {
+            const W r = (W)(a.row0 + sc + rl);
+            const int32_t pos = s_phi[f] + s_dyn[gf * lsz + (uint32_t)(r & lomask)];
+            if (pos < 0 || (uint32_t)pos >= G) {
+                atomicExch(a.err, kErrCsrPos);
+                return;
+            }
+            s_idx[rl * G + (uint32_t)pos] = (uint64_t)r ^ xf;
+            s_val[rl * G + (uint32_t)pos] = v;
+        };
+        const uint32_t nitem = nfv * rows;
+        if (ring) {
+            // this thread's copy for sub-chunk k has landed (two newer pending)
+            asm volatile("cp.async.wait_group 2;" ::: "memory");
+            if (own && rl_it < rows)
+                place(f_it, rl_it, g_it, x_it, s_fv[(size_t)(k % 3u) * nfv * R + t]);
+        } else {
+            for (uint32_t i = t; i < nitem; i += kCsrThreads) {
+                const uint32_t f = i / rows, rl = i - f * rows;
+                const uint32_t gf = a.fold[f];
+                place(f, rl, gf, a.gx[gf], a.fvals[(size_t)f * a.nrows + sc + rl]);
+            }
+        }
+        // shared writes visible to the bulk-copy (async) proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (t == 0) {
+            csr_bulk_s2g(a.indices + sc * G, s_idx, rows * G * 8u);
+            csr_bulk_s2g(a.data + 2 * sc * G, s_val, rows * G * 16u);
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        }
+        ch = chA;
+        sc = scA;
+        chA = chB;
+        scA = scB;
+        next_sub(chB, scB);
+        ++k;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     if (t == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
+// VALS: write the values row-major per fold group into a.fvals (coalesced),
+// for the staged fill to place; otherwise store the entries in place.
+template <bool VALS>
 __global__ void __launch_bounds__(kCsrThreads) csr_fold_kernel(const CsrArgs a) {
     for (uint32_t f = blockIdx.y; f < a.nfold; f += gridDim.y) {
         const uint32_t g = a.fold[f];
@@ -330,12 +441,15 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fold_kernel(const CsrArgs a) 
             const uint64_t r = a.row0 + rr;
             double2 v;
             switch (d.zparts & 3u) {  // warp-uniform
-                case 1: v = csr_fold_row<true, false>(a, r, d.k0, d.k1); break;
-                case 2: v = csr_fold_row<false, true>(a, r, d.k0, d.k1); break;
-                case 3: v = csr_fold_row<true, true>(a, r, d.k0, d.k1); break;
-                default: v = csr_fold_row<false, false>(a, r, d.k0, d.k1); break;
+                case 1: v = csr_fold_row<true, false>(a, r, d, f); break;
+                case 2: v = csr_fold_row<false, true>(a, r, d, f); break;
+                case 3: v = csr_fold_row<true, true>(a, r, d, f); break;
+                default: v = csr_fold_row<false, false>(a, r, d, f); break;
             }
-            csr_store(a, rr, (int32_t)g + sigma_sum<uint64_t>(r & pm, sg), r ^ xg, v);
+            if constexpr (VALS)
+                a.fvals[(size_t)f * a.nrows + rr] = v;
+            else
+                csr_store(a, rr, (int32_t)g + sigma_sum<uint64_t>(r & pm, sg), r ^ xg, v);
         }
     }
 }
@@ -348,7 +462,10 @@ static cudaError_t launch_csr_fold(const CsrArgs &a, int nsm, cudaStream_t st) {
     uint64_t cap = ((uint64_t)nsm * 8 + gy - 1) / gy;
     if (cap < 1) cap = 1;
     if (gx > cap) gx = cap;
-    csr_fold_kernel<<<dim3((unsigned)gx, gy), kCsrThreads, 0, st>>>(a);
+    if (a.fvals)
+        csr_fold_kernel<true><<<dim3((unsigned)gx, gy), kCsrThreads, 0, st>>>(a);
+    else
+        csr_fold_kernel<false><<<dim3((unsigned)gx, gy), kCsrThreads, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }
@@ -376,7 +493,11 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
         if (aligned && L >= 1 && a.nrows % 2 == 0) {
             const uint32_t R = (uint32_t)csr_stage_rows((uint32_t)a.G, L);
             const size_t buf = ((size_t)R * a.G * 24u + 127u) & ~(size_t)127u;
-            const size_t sm = ((smem + 127u) & ~(size_t)127u) + 2 * buf;
+            size_t sm = ((smem + 127u) & ~(size_t)127u) + 2 * buf;
+            if (a.fvals && a.nfold > 0) {  // chunk positions, then the value ring
+                sm += (((size_t)a.nfold + 3u) & ~(size_t)3u) * 4u;
+                if ((size_t)a.nfold * R <= (size_t)kCsrThreads) sm += 3u * a.nfold * R * 16u;
+            }
             auto kern = a.n > 32 ? csr_fill_staged_kernel<true> : csr_fill_staged_kernel<false>;
             cudaError_t e0 =
                 cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -386,10 +507,14 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
             if (e0 != cudaSuccess) return e0;
             if (per_sm < 1) per_sm = 1;
             if (g > (uint64_t)nsm * per_sm) g = (uint64_t)nsm * per_sm;
+            if (a.fvals) {  // fold values first; the staged pass places them
+                cudaError_t e = launch_csr_fold(a, nsm, st);
+                if (e != cudaSuccess) return e;
+            }
             kern<<<(unsigned)g, kCsrThreads, sm, st>>>(a);
             count_launch();
             cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) return e;
+            if (e != cudaSuccess || a.fvals) return e;
             return launch_csr_fold(a, nsm, st);
         }
     } else {
@@ -411,7 +536,9 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    return launch_csr_fold(a, nsm, st);
+    CsrArgs b = a;
+    b.fvals = nullptr;  // direct path: fold entries stored in place
+    return launch_csr_fold(b, nsm, st);
 }
 
 // y = A v, complex128.  S lanes per row: the lanes of a row stride its

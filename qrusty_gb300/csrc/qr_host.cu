@@ -129,7 +129,7 @@ struct qr_op {
     std::vector<int32_t> sig;           // G x n: sigma_{g,b}
     bool csr_uploaded = false;
     uint32_t nfold = 0, nctab = 0;
-    DevBuf d_gx, d_goff, d_tz, d_tc, d_pmask, d_sig, d_grp, d_ctab, d_fold;
+    DevBuf d_gx, d_goff, d_tz, d_tc, d_pmask, d_sig, d_grp, d_ctab, d_fold, d_pbeta, d_ptab, d_fv;
     // merged terms (FP64 simplification) for qr_apply; mmap[k] = merged index
     std::vector<uint64_t> mx, mz;
     std::vector<cd> mc;
@@ -210,17 +210,39 @@ struct Span {
     std::vector<uint64_t> basis;
     std::vector<uint64_t> coord;  // per term
     bool overflow = false;
+    size_t used = 0;  // leading terms whose coordinates are set (all, without overflow)
 };
 Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax);
 
 // Per group: position-formula range and either the class table (the
 // term-order fold of +-c'_k for every sign class; same additions in the same
 // order as make_row, so the same bits) or the term range for a per-row fold.
+// Term-order fold of terms [k0, k0 + m) for every sign class of a span
+// (class bit 0: parity against z0, bit j+1: against basis j): the additions
+// of make_row, in its order, once per class.
+void fold_classes(const qr_op *op, uint32_t k0, size_t m, const Span &sp, std::vector<cd> &out) {
+    const uint32_t ncls = 2u << sp.basis.size();
+    for (uint32_t c = 0; c < ncls; ++c) {
+        cd v{0.0, 0.0};
+        for (uint32_t k = k0; k < k0 + m; ++k) {
+            const uint64_t sel = 1ull | (sp.coord[k - k0] << 1);
+            const bool neg = (__builtin_popcountll(c & sel) & 1) != 0;
+            const cd t = neg ? cd{-op->tc[k].re, -op->tc[k].im} : op->tc[k];
+            if (k == k0) v = t;
+            else v = cd{v.re + t.re, v.im + t.im};
+        }
+        out.push_back(v);
+    }
+}
+
 void build_csr_groups(const qr_op *op, std::vector<CsrGroup> &grp, std::vector<cd> &ctab,
-                      std::vector<uint32_t> &fold) {
+                      std::vector<uint32_t> &fold, std::vector<uint64_t> &pbeta,
+                      std::vector<cd> &ptab) {
     grp.assign(op->G, CsrGroup{});
     ctab.clear();
     fold.clear();
+    pbeta.clear();
+    ptab.clear();
     for (uint64_t g = 0; g < op->G; ++g) {
         CsrGroup &d = grp[g];
         const uint32_t k0 = op->goff[g], k1 = op->goff[g + 1];
@@ -240,24 +262,24 @@ void build_csr_groups(const qr_op *op, std::vector<CsrGroup> &grp, std::vector<c
                 iz = iz && op->tc[k].im == 0.0;
             }
             d.zparts = (rz ? 1u : 0u) | (iz ? 2u : 0u);
+            // leading terms of rank <= kCsrPrefixRank: one table read per row
+            const Span pp = gf2_span(zs, kCsrPrefixRank);
+            const size_t m = pp.used;
+            d.pre = 0;
+            if (m >= 2) {
+                d.tab = (uint32_t)ptab.size();
+                d.pre = (uint32_t)m | ((uint32_t)pp.basis.size() << 24);
+                fold_classes(op, k0, m, pp, ptab);
+            }
+            for (int j = 0; j < kCsrPrefixRank; ++j)
+                pbeta.push_back(j < (int)pp.basis.size() ? pp.basis[j] : 0ull);
             fold.push_back((uint32_t)g);
             continue;
         }
         d.d = (uint32_t)sp.basis.size();
         for (uint32_t j = 0; j < d.d; ++j) d.beta[j] = sp.basis[j];
         d.tab = (uint32_t)ctab.size();
-        const uint32_t ncls = 2u << d.d;
-        for (uint32_t c = 0; c < ncls; ++c) {
-            cd v{0.0, 0.0};
-            for (uint32_t k = k0; k < k1; ++k) {
-                const uint64_t sel = 1ull | (sp.coord[k - k0] << 1);
-                const bool neg = (__builtin_popcountll(c & sel) & 1) != 0;
-                const cd t = neg ? cd{-op->tc[k].re, -op->tc[k].im} : op->tc[k];
-                if (k == k0) v = t;
-                else v = cd{v.re + t.re, v.im + t.im};
-            }
-            ctab.push_back(v);
-        }
+        fold_classes(op, k0, k1 - k0, sp, ctab);
     }
 }
 
@@ -266,7 +288,9 @@ int upload_csr_tables(qr_op *op) {
     std::vector<CsrGroup> grp;
     std::vector<cd> ctab;
     std::vector<uint32_t> fold;
-    build_csr_groups(op, grp, ctab, fold);
+    std::vector<uint64_t> pbeta;
+    std::vector<cd> ptab;
+    build_csr_groups(op, grp, ctab, fold, pbeta, ptab);
     if (ctab.size() > 0xffffffffull) return fail(QR_EINVAL, "qr_csr_build: class tables too large");
     QR_CUDA(op->d_gx.upload(op->gx), "upload gx");
     QR_CUDA(op->d_goff.upload(op->goff), "upload goff");
@@ -278,6 +302,10 @@ int upload_csr_tables(qr_op *op) {
     QR_CUDA(op->d_ctab.upload(ctab), "upload class tables");
     op->nctab = (uint32_t)ctab.size();
     QR_CUDA(op->d_fold.upload(fold), "upload fold groups");
+    if (pbeta.empty()) pbeta.push_back(0);
+    if (ptab.empty()) ptab.push_back(cd{0.0, 0.0});
+    QR_CUDA(op->d_pbeta.upload(pbeta), "upload prefix bases");
+    QR_CUDA(op->d_ptab.upload(ptab), "upload prefix tables");
     op->nfold = (uint32_t)fold.size();
     op->csr_uploaded = true;
     return QR_OK;
@@ -339,6 +367,7 @@ Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
         if (v != 0) {
             if (sp.basis.size() >= dmax) {
                 sp.overflow = true;
+                sp.used = k;
                 return sp;
             }
             c |= 1ull << sp.basis.size();
@@ -346,6 +375,7 @@ Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax) {
         }
         sp.coord[k] = c;
     }
+    sp.used = zs.size();
     return sp;
 }
 
@@ -887,11 +917,25 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, i
     a.fold = op->d_fold.as<uint32_t>();
     a.nfold = op->nfold;
     a.ctab = op->d_ctab.as<double2>();
+    a.pbeta = op->d_pbeta.as<uint64_t>();
+    a.ptab = op->d_ptab.as<double2>();
     a.nctab = op->nctab;
     a.tz = op->d_tz.as<uint64_t>();
     a.tc = op->d_tc.as<double>();
     a.err = op->d_err.as<int>();
+    a.fvals = nullptr;
+    // fold-mode values buffer (nfold x rows) for the staged fill; without
+    // it the fold entries are stored in place after the fill
+    auto fold_buffer = [&](uint64_t rows) {
+        a.fvals = nullptr;
+        if (op->nfold == 0 || op->G > 256) return;
+        if (op->d_fv.alloc((size_t)op->nfold * rows * sizeof(double2)) == cudaSuccess)
+            a.fvals = op->d_fv.as<double2>();
+        else
+            (void)cudaGetLastError();  // allocation failure is not sticky: clear it
+    };
     if (mem == QR_MEM_DEVICE) {
+        fold_buffer(op->N);
         a.indptr = indptr;
         a.indices = indices;
         a.data = data;
@@ -910,6 +954,7 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, i
     QR_CUDA(d_ptr.alloc((op->N + 1) * sizeof(uint64_t)), "alloc indptr staging");
     QR_CUDA(d_idx.alloc(rows * op->G * sizeof(uint64_t)), "alloc indices staging");
     QR_CUDA(d_dat.alloc(rows * op->G * 2 * sizeof(double)), "alloc data staging");
+    fold_buffer(rows);
     for (uint64_t r0 = 0; r0 < op->N; r0 += rows) {
         const uint64_t nr = std::min(rows, op->N - r0);
         a.indptr = (r0 == 0) ? d_ptr.as<uint64_t>() : nullptr;

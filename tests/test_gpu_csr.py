@@ -118,6 +118,26 @@ def test_fold_group_signed_zero_parts(cuda, oracle, kind):
     check_csr(oracle, n, x, z, ph, c)
 
 
+@pytest.mark.parametrize("kind", ["complex", "real", "imag"])
+def test_fold_group_prefix_and_tail(cuda, oracle, kind):
+    """A fold group of z-span rank 14: its first terms (rank <= 10) come from
+    a per-class prefix table, the later ones are added per row; both parts
+    must reproduce the term-order fold bit for bit."""
+    rng = np.random.default_rng(11)
+    n, T = 14, 48
+    x = np.zeros(T, np.uint64)
+    z = rng.integers(1, 1 << n, T).astype(np.uint64)
+    ph = rng.integers(0, 4, T).astype(np.uint8)
+    v = rng.normal(size=T)
+    c = {"complex": v + 1j * rng.normal(size=T), "real": v + 0j, "imag": 1j * v}[kind]
+    # a second group (x = 1) keeps the fill kernel's class-table path in play
+    x = np.concatenate([x, np.ones(4, np.uint64)])
+    z = np.concatenate([z, np.array([0, 1, 2, 3], np.uint64)])
+    ph = np.concatenate([ph, np.zeros(4, np.uint8)])
+    c = np.concatenate([c, np.ones(4)])
+    check_csr(oracle, n, x, z, ph, c)
+
+
 @pytest.mark.parametrize("name", ["H2", "H4"])
 def test_reference_test_H(cuda, golden, name):
     """pyqrusty/tests/test_H.py:32-48 on the GPU build: kron path
