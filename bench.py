@@ -653,7 +653,13 @@ def run_spmv(args):
         roofline={"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
                   "frac": gbs / hbm, "traffic": None, "alg_bytes_per_launch": alg,
                   "alg_bytes_rule": "24 nnz + 8 (N+1) + 16 N", "peak_source": peak_kind},
-        rel_err={"vs_matrix_free_c128": err})
+        rel_err={"vs_matrix_free_c128": err},
+        # complex128 multiply-add = 4 FP64 FMAs (8 flops) per entry; GB300's
+        # nominal FP64 rate (1.25 TFLOP/s) bounds this kernel before HBM does
+        fp64={"tflops": 8.0 * nnz / (ms / 1e3) / 1e12,
+              "frac_of_nominal": 8.0 * nnz / (ms / 1e3) / 1.25e12,
+              "hbm_floor_ms": alg / (hbm * 1e9) * 1e3,
+              "fp64_floor_ms": 8.0 * nnz / 1.25e12 * 1e3})
     if not args.no_cpu:
         from oracle import oracle as O
         O.build()

@@ -86,9 +86,14 @@ int qr_csr_size(const qr_op *op, uint64_t *nrows, uint64_t *nnz);
  * (qrusty/src/accel.rs:267-336) / to_matrix_rowwise_unsafe_chunked
  * (qrusty/src/lib.rs:558-571): per row, columns r ^ x ascending, values
  * summed over equal columns in input-term order, explicit zeros kept.
- * mem = QR_MEM_DEVICE: device pointers, asynchronous on `stream`.
+ * mem = QR_MEM_DEVICE: device pointers, asynchronous on `stream`
+ * (16-byte aligned indices/data take the staged bulk-store path).
  * mem = QR_MEM_HOST: host pointers; built on the device and copied back,
- * synchronous. */
+ * synchronous.
+ * Groups whose z masks span rank > 4 are folded per row into a value
+ * buffer of (such groups) x rows x 16 bytes kept with the operator: the
+ * first call that needs it (or a larger one) allocates it, so that call
+ * synchronises the device; qr_op_destroy frees it. */
 int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data,
                  int32_t mem, void *stream);
 

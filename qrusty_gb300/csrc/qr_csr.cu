@@ -238,6 +238,7 @@ __device__ __forceinline__ double2 csr_fold_row(const CsrArgs &a, uint64_t r, co
 // a line the bulk store has already evicted.  Without a value buffer the
 // fold entries are left unset and stored afterwards by csr_fold_kernel<false>.
 constexpr size_t kCsrStageBytes = 24u * 1024u;  // one buffer: R rows x G x (8 + 16) bytes
+constexpr uint32_t kCsrFvSlots = 4;              // fold-value ring depth (sub-chunks)
 
 __host__ __device__ inline int csr_stage_rows(uint32_t G, int L) {
     int R = 1 << L;
@@ -303,17 +304,20 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_staged_kernel(const CsrA
     const int32_t *lut = s_dyn + (lane_on ? g : 0u) * lsz;
     const double2 *tab = (ctab_smem ? s_ctab : a.ctab) + d.tab;
     const uint64_t nchunk = (a.nrows + lomask) >> L;
-    // fold-mode entries: with nfold * R <= threads, thread t owns item
-    // (f = t / R, rl = t % R) of every sub-chunk and copies its value into a
-    // 3-slot shared ring two sub-chunks ahead (cp.async: no register waits
-    // on the load; the values come from DRAM, the fill's write stream
-    // having evicted them from L2)
+    // fold-mode entries: with nfold * R <= threads, the highest nfold * R
+    // threads (idle in the class-table pass whenever rpp * G < threads) own
+    // one item (f, rl) of every sub-chunk each and copy its value into a
+    // kCsrFvSlots-deep shared ring, kCsrFvSlots - 1 sub-chunks ahead
+    // (cp.async: no register waits on the load; the values come from DRAM,
+    // the fill's write stream having evicted them from L2)
     const bool ring = nfv > 0 && nfv * R <= (uint32_t)kCsrThreads;
-    const uint32_t f_it = t / R, rl_it = t - (t / R) * R;
-    const bool own = ring && f_it < nfv;
+    const uint32_t base_it = ring ? (uint32_t)kCsrThreads - nfv * R : (uint32_t)kCsrThreads;
+    const bool own = ring && t >= base_it;
+    const uint32_t i_it = own ? t - base_it : 0u;
+    const uint32_t f_it = i_it / R, rl_it = i_it - (i_it / R) * R;
     const uint32_t g_it = own ? a.fold[f_it] : 0u;
     const uint64_t x_it = own ? a.gx[g_it] : 0ull;
-    double2 *s_fv = reinterpret_cast<double2 *>(s_phi + ((nfv + 3u) & ~3u));  // 3 x nfv*R
+    double2 *s_fv = reinterpret_cast<double2 *>(s_phi + ((nfv + 3u) & ~3u));  // slots x nfold*R
     auto next_sub = [&](uint64_t &c, uint64_t &s0) {
         const uint64_t e = min((c << L) + ((uint64_t)1 << L), a.nrows);
         s0 += R;
@@ -329,24 +333,21 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_staged_kernel(const CsrA
             if (rl_it < rows) {
                 const double2 *src = a.fvals + (size_t)f_it * a.nrows + s0 + rl_it;
                 asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                                 csr_saddr(s_fv + (size_t)slot * nfv * R + t)),
+                                 csr_saddr(s_fv + (size_t)slot * nfv * R + i_it)),
                              "l"(src)
                              : "memory");
             }
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    uint32_t k = 0;  // sub-chunks issued by this block: buffer k & 1, ring slot k % 3
+    uint32_t k = 0;  // sub-chunks issued by this block: buffer k & 1, ring slot k % kCsrFvSlots
     uint64_t ch = blockIdx.x, sc = ch << L;
-    uint64_t chA = ch, scA = sc, chB, scB;  // sub-chunks k + 1 and k + 2
-    next_sub(chA, scA);
-    chB = chA;
-    scB = scA;
-    next_sub(chB, scB);
-    if (ring) {
-        prefetch(ch, sc, 0);
-        prefetch(chA, scA, 1);
-    }
+    uint64_t chP = ch, scP = sc;  // prefetch cursor: sub-chunk k + kCsrFvSlots - 1
+    if (ring)
+        for (uint32_t q = 0; q + 1 < kCsrFvSlots; ++q) {
+            prefetch(chP, scP, q);
+            next_sub(chP, scP);
+        }
     int32_t phi = 0;
     while (ch < nchunk) {
         const uint64_t rr0 = ch << L;
@@ -368,7 +369,10 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_staged_kernel(const CsrA
             }
         }
         __syncthreads();
-        if (ring) prefetch(chB, scB, (k + 2) % 3u);
+        if (ring) {
+            prefetch(chP, scP, (k + kCsrFvSlots - 1) % kCsrFvSlots);
+            next_sub(chP, scP);
+        }
         if (active) {
 #pragma unroll 2
             for (uint32_t rl = rs; rl < rows; rl += rpp) {
@@ -397,10 +401,11 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_staged_kernel(const CsrA
         };
         const uint32_t nitem = nfv * rows;
         if (ring) {
-            // this thread's copy for sub-chunk k has landed (two newer pending)
-            asm volatile("cp.async.wait_group 2;" ::: "memory");
+            // this thread's copy for sub-chunk k has landed (newer ones pending)
+            asm volatile("cp.async.wait_group %0;" ::"n"(kCsrFvSlots - 1) : "memory");
             if (own && rl_it < rows)
-                place(f_it, rl_it, g_it, x_it, s_fv[(size_t)(k % 3u) * nfv * R + t]);
+                place(f_it, rl_it, g_it, x_it,
+                      s_fv[(size_t)(k % kCsrFvSlots) * nfv * R + i_it]);
         } else {
             for (uint32_t i = t; i < nitem; i += kCsrThreads) {
                 const uint32_t f = i / rows, rl = i - f * rows;
@@ -416,11 +421,7 @@ __global__ void __launch_bounds__(kCsrThreads) csr_fill_staged_kernel(const CsrA
             csr_bulk_s2g(a.data + 2 * sc * G, s_val, rows * G * 16u);
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
         }
-        ch = chA;
-        sc = scA;
-        chA = chB;
-        scA = scB;
-        next_sub(chB, scB);
+        next_sub(ch, sc);
         ++k;
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
@@ -496,7 +497,8 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
             size_t sm = ((smem + 127u) & ~(size_t)127u) + 2 * buf;
             if (a.fvals && a.nfold > 0) {  // chunk positions, then the value ring
                 sm += (((size_t)a.nfold + 3u) & ~(size_t)3u) * 4u;
-                if ((size_t)a.nfold * R <= (size_t)kCsrThreads) sm += 3u * a.nfold * R * 16u;
+                if ((size_t)a.nfold * R <= (size_t)kCsrThreads)
+                    sm += (size_t)kCsrFvSlots * a.nfold * R * 16u;
             }
             auto kern = a.n > 32 ? csr_fill_staged_kernel<true> : csr_fill_staged_kernel<false>;
             cudaError_t e0 =
