@@ -138,6 +138,37 @@ def test_fold_group_prefix_and_tail(cuda, oracle, kind):
     check_csr(oracle, n, x, z, ph, c)
 
 
+def test_more_than_256_groups(cuda, oracle):
+    """G > 256: the direct-store fill and the in-place fold of the x = 0
+    group (z span of rank 11, so a prefix table and a per-row tail)."""
+    rng = np.random.default_rng(21)
+    n = 11
+    x = rng.integers(1, 1 << n, 700).astype(np.uint64)
+    z = rng.integers(0, 1 << n, 700).astype(np.uint64)
+    x = np.concatenate([x, np.zeros(30, np.uint64)])
+    z = np.concatenate([z, rng.integers(1, 1 << n, 30).astype(np.uint64)])
+    T = len(x)
+    ph = rng.integers(0, 4, T).astype(np.uint8)
+    c = rng.normal(size=T) + 1j * rng.normal(size=T)
+    assert len(np.unique(x)) > 256
+    check_csr(oracle, n, x, z, ph, c)
+
+
+def test_many_fold_groups(cuda, oracle):
+    """Forty fold-mode groups (16 terms each, z span up to rank 14): more
+    fold entries per stage than threads, so they are placed by the strided
+    loop; each group has a prefix table and a per-row tail."""
+    rng = np.random.default_rng(22)
+    n, ng, per = 14, 40, 16
+    xs = rng.choice(np.arange(1, 1 << n), ng, replace=False).astype(np.uint64)
+    x = np.repeat(xs, per)
+    z = rng.integers(1, 1 << n, ng * per).astype(np.uint64)
+    T = len(x)
+    ph = rng.integers(0, 4, T).astype(np.uint8)
+    c = rng.normal(size=T) + 0j  # real: the zero-imaginary rule too
+    check_csr(oracle, n, x, z, ph, c)
+
+
 @pytest.mark.parametrize("name", ["H2", "H4"])
 def test_reference_test_H(cuda, golden, name):
     """pyqrusty/tests/test_H.py:32-48 on the GPU build: kron path
@@ -202,6 +233,25 @@ def test_device_build_matches_host(cuda):
     assert np.array_equal(di.cpu().numpy().view(np.uint64), hi)
     assert np.array_equal(dj.cpu().numpy().view(np.uint64), hj)
     assert np.array_equal(_bits(dd.cpu().numpy()), _bits(hd))
+
+
+def test_host_build_in_chunks_matches_device(cuda):
+    """Chain n = 21 (2.1 GB of CSR): the host-memory build runs in two
+    ~1 GiB row chunks (each with its own fold-value buffer and row offset)
+    and must equal the one-shot device build bit for bit."""
+    import torch
+    t, _ = W.cfg1(with_state=False, n=21)
+    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
+    nr, nz = op.csr_size()
+    assert nz * 24 > 2 ** 30  # more than one chunk
+    hi, hj, hd = op.csr_host()
+    di, dj, dd = op.csr_device()
+    torch.cuda.synchronize()
+    assert np.array_equal(di.cpu().numpy().view(np.uint64), hi)
+    step = 1 << 24
+    for lo in range(0, nz, step):
+        assert np.array_equal(dj[lo:lo + step].cpu().numpy().view(np.uint64), hj[lo:lo + step])
+        assert np.array_equal(_bits(dd[lo:lo + step].cpu().numpy()), _bits(hd[lo:lo + step]))
 
 
 def test_spmv_skips_out_of_range_columns(cuda):
