@@ -437,7 +437,7 @@ __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
         const float2 bp = __fmul2_rn(make_float2(T.z, T.w), make_float2(sv, sv));
         // partner byte offset: the XOR part (thread and register bits of lo) is
         // precomputed per sub-group; the stage offset occupies higher bits
-        const uint32_t off = soff | (t8 ^ (d.x & 0x7fffu));
+        const uint32_t off = soff | (t8 ^ (d.x & 0xffffu));  // bit 15: pair half
         float2 p[AMPS];
 #pragma unroll
         for (int m = 0; m < AMPS; ++m) {
@@ -702,6 +702,216 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
     }
 }
 
+// Single-chunk kernel with partner blocks visited in pairs: blocks 2p and
+// 2p+1 are loaded into the two stages of one ring slot behind one barrier,
+// and the pair's sub-groups (merged, sorted by run key, bit 15 of the
+// descriptor's offset selecting the stage) run as one list.  Most partner
+// blocks of pair-structured operators hold a single sub-group, for which the
+// per-block ring wait, run lookup, dispatch and stage release cost more than
+// the sub-group itself.
+template <int AMPS, bool WIDE>
+__global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const uint32_t threads = blockDim.x;
+    const uint32_t nwarps = threads >> 5;
+    const uint32_t t = threadIdx.x;
+    const uint32_t lane = t & 31;
+    const uint32_t tile_bytes = (1u << a.b) * 8u;
+    const uint32_t tabn = a.nsub < kTabCap ? a.nsub : kTabCap;
+    float4 *s_tab = reinterpret_cast<float4 *>(smem_raw + (size_t)kTabStages * tile_bytes);
+    float2 *s_lo = reinterpret_cast<float2 *>(s_tab + kTabEnt * (size_t)tabn);
+    uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kTabStages);
+    volatile uint32_t *s_abort = cnt + kTabStages;
+    uint2 *s_td = reinterpret_cast<uint2 *>(reinterpret_cast<unsigned char *>(s_lo) +
+                                            (size_t)AMPS * threads * 8u + kTabBarBytes);
+    uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + kTabCap);
+    uint32_t *s_blk = s_run + kTabCap + 1;
+    const uint32_t np = a.npairs, nb = a.nblocks;
+    for (uint32_t i = t; i < a.nsub; i += threads) s_td[i] = a.tdesc[i];
+    for (uint32_t i = t; i <= a.nruns; i += threads)
+        s_run[i] = a.run_g0[i] | (i < a.nruns ? a.run_key[i] << 16 : 0u);
+    for (uint32_t i = t; i <= np; i += threads) s_blk[i] = a.blk_r0[i];
+    const uint2 *tdesc = s_td;
+
+    const float2 *psi = static_cast<const float2 *>(a.psi);
+    float2 *y = static_cast<float2 *>(a.y);
+    const float2 *diag = static_cast<const float2 *>(a.diag);
+    const uint32_t t8 = t << 3;
+    const uint32_t slot_bytes = 2u * tile_bytes;
+    const int diag_pair = a.diag_block >= 0 ? (a.diag_block >> 1) : -1;
+    const uint32_t diag_half = a.diag_block >= 0 ? ((uint32_t)a.diag_block & 1u) : 0u;
+
+    const uint64_t first = blockIdx.x;
+    const uint64_t my_items =
+        a.nitems > first ? (a.nitems - first + gridDim.x - 1) / gridDim.x : 0;
+    const uint64_t total = my_items * np;
+    if (total == 0) return;
+
+    // load pair p of tile (st, q) into slot s: one or two partner tiles
+    auto issue_pair = [&](uint32_t s, uint32_t p, uint64_t st, uint64_t q) {
+        const uint32_t j0 = 2u * p;
+        const uint32_t ntl = j0 + 1 < nb ? 2u : 1u;
+        mbar_expect_tx(&full[s], ntl * tile_bytes);
+        for (uint32_t h = 0; h < ntl; ++h) {
+            const float2 *src = psi + st * a.N + ((q ^ a.blk_hi[j0 + h]) << a.b);
+            bulk_g2s(smem_raw + (size_t)s * slot_bytes + (size_t)h * tile_bytes, src, tile_bytes,
+                     &full[s]);
+        }
+    };
+    uint64_t st = first / a.ntiles;
+    uint64_t q = first - st * a.ntiles;
+    if (t == 0) {
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(&full[s], 1);
+            cnt[s] = 0;
+        }
+        *s_abort = 0;
+        mbar_fence_init();
+        // prologue: steps 0 and 1
+        uint32_t p1 = 0;
+        uint64_t q1 = q, st1 = st;
+        for (uint64_t L = 0; L < total && L < 2; ++L) {
+            issue_pair((uint32_t)L, p1, st1, q1);
+            if (++p1 == np) {
+                p1 = 0;
+                q1 += gridDim.x;
+                while (q1 >= a.ntiles) {
+                    q1 -= a.ntiles;
+                    ++st1;
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    float2 A[AMPS], B[AMPS], hi[AMPS];
+    float2 *mylo = s_lo + t;
+    uint32_t p = 0, s = 0, par = 0;
+    constexpr uint32_t kFlushPairs = kFlush / 2;
+
+    for (uint64_t L = 0; L < total; ++L) {
+        if (p == 0) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                A[m] = B[m] = hi[m] = make_float2(0.f, 0.f);
+                mylo[m * threads] = make_float2(0.f, 0.f);
+            }
+            // table of the new output tile: every warp has finished the last one
+            __syncthreads();
+            for (uint32_t gi = t; gi < a.nsub; gi += threads) {
+                const TileDataC64 &d = a.tdata[gi];
+                const uint32_t uq = parity<WIDE>(q, d.b0h) | (parity<WIDE>(q, d.b1h) << 1);
+                const float sq = parity<WIDE>(q, d.z0h) ? -1.f : 1.f;
+#pragma unroll
+                for (uint32_t u = 0; u < 4; ++u) {
+                    const float2 v = d.T[u ^ uq];
+                    s_tab[gi * 4 + u] = make_float4(sq * v.x, sq * v.x, sq * v.y, sq * v.y);
+                }
+            }
+            __syncthreads();
+        }
+        bool skip = *s_abort != 0;
+        if (!skip && !mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
+            if (lane == 0) {
+                atomicExch(a.err, kErrMbarTimeout);
+                *s_abort = 1;
+            }
+            skip = true;
+        }
+        skip = __any_sync(0xffffffffu, skip);
+        const uint32_t soff = s * slot_bytes;
+
+        if (!skip && (int)p == diag_pair && diag != nullptr) {
+            const float2 *dg = diag + (q << a.b);
+            const uint32_t doff = soff + diag_half * tile_bytes;
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const uint32_t rl = t + threads * (uint32_t)m;
+                const float2 d = dg[rl];
+                const float2 pv = *reinterpret_cast<const float2 *>(smem_raw + doff + rl * 8u);
+                A[m] = __ffma2_rn(make_float2(d.x, d.x), pv, A[m]);
+                B[m] = __ffma2_rn(make_float2(d.y, d.y), pv, B[m]);
+            }
+        }
+
+        const uint32_t r1 = skip ? 0u : s_blk[p + 1];
+        uint32_t rw = s_run[s_blk[p]];
+        for (uint32_t r = s_blk[p]; r < r1; ++r) {
+            const uint32_t rn = s_run[r + 1];
+            run_tab_dispatch<AMPS>(rw >> 16, A, B, smem_raw, soff, s_tab, tdesc, rw & 0xffffu,
+                                   rn & 0xffffu, t, t8);
+            rw = rn;
+        }
+
+        const bool last = (p == np - 1);
+        if (last || (p % kFlushPairs) == kFlushPairs - 1) {
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const float yr = __fsub_rn(A[m].x, B[m].y);
+                const float yi = __fadd_rn(A[m].y, B[m].x);
+                float2 lm = mylo[m * threads];
+                two_sum_into(hi[m].x, lm.x, yr);
+                two_sum_into(hi[m].y, lm.y, yi);
+                mylo[m * threads] = lm;
+                A[m] = B[m] = make_float2(0.f, 0.f);
+            }
+        }
+        if (last) {
+            float2 *yo = y + st * a.N + (q << a.b);
+            const float2 *vo = a.v ? static_cast<const float2 *>(a.v) + st * a.N + (q << a.b)
+                                   : nullptr;
+#pragma unroll
+            for (int m = 0; m < AMPS; ++m) {
+                const float2 lm = mylo[m * threads];
+                const uint32_t rl = t + threads * (uint32_t)m;
+                float2 o = make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
+                if (vo)  // fused y = alpha (H psi) + beta v, in FP32
+                    o = cx_axpby((float)a.ar, (float)a.ai, o, (float)a.br, (float)a.bi, vo[rl]);
+                yo[rl] = o;
+            }
+        }
+
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            const uint32_t old = atomicAdd(&cnt[s], 1u);
+            if (old == nwarps - 1) {
+                cnt[s] = 0;
+                if (L + 2 < total && *s_abort == 0) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    // two pairs ahead of (st, q, p), stepped with adds
+                    uint32_t p2 = p + 2;
+                    uint64_t q2 = q, st2 = st;
+                    while (p2 >= np) {
+                        p2 -= np;
+                        q2 += gridDim.x;
+                        while (q2 >= a.ntiles) {
+                            q2 -= a.ntiles;
+                            ++st2;
+                        }
+                    }
+                    issue_pair(s, p2, st2, q2);
+                }
+            }
+        }
+        s ^= 1u;
+        if (s == 0) par ^= 1u;
+        if (++p == np) {
+            p = 0;
+            q += gridDim.x;
+            while (q >= a.ntiles) {
+                q -= a.ntiles;
+                ++st;
+            }
+        }
+    }
+    if (*s_abort && t == 0) {
+        // bounded drain of copies that may still target this CTA's stages
+        for (int k = 0; k < 2; ++k) mbar_wait_bounded(&full[k], 0, kWaitLimitNs / 8);
+    }
+}
+
 template <int AMPS>
 static size_t tab_smem_bytes(const ApplyArgs &a, int threads) {
     const uint32_t tile_bytes = (1u << a.b) * 8u;
@@ -714,8 +924,11 @@ static size_t tab_smem_bytes(const ApplyArgs &a, int threads) {
 template <int AMPS, bool WIDE>
 static cudaError_t launch_c64c_tab(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
     const size_t smem = tab_smem_bytes<AMPS>(a, threads);
-    // one chunk (operators of up to 512 sub-groups): no chunk bookkeeping
+    // one chunk (operators of up to 512 sub-groups): no chunk bookkeeping;
+    // with a pair plan, partner blocks two at a time
     auto kern = a.nchunks > 1 ? apply_c64c_tab<AMPS, WIDE, true> : apply_c64c_tab<AMPS, WIDE, false>;
+    if constexpr (AMPS == 8)
+        if (a.npairs > 0 && a.nchunks <= 1) kern = apply_c64c_pair<AMPS, WIDE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;

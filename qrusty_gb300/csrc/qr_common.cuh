@@ -73,11 +73,12 @@ struct ApplyArgs {
     const SubDescC64 *sub;
     uint32_t nsub;
     // per-tile-table kernel: per sub-group an 8-byte thread descriptor
-    // {partner byte-offset XOR | tvar << 31, z0_t | beta0_t << 10 | beta1_t << 20} and
-    // its TileDataC64; sub-groups of a block in runs of equal key
+    // {partner byte-offset XOR | pair half << 15 | tvar << 31,
+    //  z0_t | beta0_t << 10 | beta1_t << 20} and its TileDataC64; sub-groups
+    // of a block (or pair of blocks) in runs of equal key
     const uint2 *tdesc;
     const TileDataC64 *tdata;
-    const uint32_t *blk_r0;   // runs of block j: [blk_r0[j], blk_r0[j+1])
+    const uint32_t *blk_r0;   // runs of block (pair) j: [blk_r0[j], blk_r0[j+1])
     const uint32_t *run_g0;   // sub-groups of run r: [run_g0[r], run_g0[r+1])
     const uint32_t *run_key;  // key = zm | xm << 4
     uint32_t nruns;
@@ -85,6 +86,9 @@ struct ApplyArgs {
     // {first sub-group, first run, first block, 0}, nchunks + 1 entries
     const uint4 *chunks;
     uint32_t nchunks;
+    // > 0: partner blocks visited in pairs (blocks 2p, 2p+1 in one ring slot
+    // of two stages); blk_r0 then indexes pairs and tdesc bit 15 is the half
+    uint32_t npairs;
     // fused epilogue y = alpha * (H psi) + beta * v when v != nullptr
     const void *v;
     double ar, ai, br, bi;

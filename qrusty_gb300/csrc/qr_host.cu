@@ -102,7 +102,7 @@ struct Plan {
     bool has_diag = false;
     DevBuf groups, tables, fat_z, fat_c, blk_hi, blk_g0, diag;
     // compensated-c64 kernel tables
-    uint32_t nsub = 0, nruns = 0, nchunks = 0;
+    uint32_t nsub = 0, nruns = 0, nchunks = 0, npairs = 0;
     DevBuf sub;
     DevBuf tdesc, tdata, blk_r0, run_g0, run_key, chunks;
 };
@@ -589,6 +589,37 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     for (size_t j = 0; j < bhi.size(); ++j)
         if (bhi[j] == 0 && pl.diag_block < 0) pl.diag_block = (int)j;
 
+    // single-chunk c64c plans: partner blocks are visited in pairs (two
+    // stages behind one barrier, one ring slot); each pair's sub-groups are
+    // merged and sorted by run key, their block recorded as the half
+    std::vector<uint32_t> half(ord.size(), 0u), pg0;
+    pl.npairs = 0;
+    if (f32 && tile_bits < 0 && ord.size() <= (size_t)kTabCap && pl.nblocks >= 2 &&
+        pl.amps == 8) {
+        const uint32_t np = (pl.nblocks + 1) / 2;
+        std::vector<size_t> ord2;
+        std::vector<uint32_t> half2;
+        ord2.reserve(ord.size());
+        for (uint32_t p = 0; p < np; ++p) {
+            pg0.push_back((uint32_t)ord2.size());
+            const uint32_t ga = bg0[2 * p], gm = bg0[std::min(2 * p + 1, pl.nblocks)],
+                           gb = bg0[std::min(2 * p + 2, pl.nblocks)];
+            std::vector<uint32_t> items;
+            for (uint32_t i = ga; i < gb; ++i) items.push_back(i);
+            std::stable_sort(items.begin(), items.end(), [&](uint32_t x, uint32_t y) {
+                return runkey(subs[ord[x]]) < runkey(subs[ord[y]]);
+            });
+            for (uint32_t i : items) {
+                ord2.push_back(ord[i]);
+                half2.push_back(i >= gm ? 1u : 0u);
+            }
+        }
+        pg0.push_back((uint32_t)ord2.size());
+        ord.swap(ord2);
+        half.swap(half2);
+        pl.npairs = np;
+    }
+
     std::vector<unsigned char> tab, fc;
     std::vector<uint64_t> fz;
     uint32_t ntab = 0, nfat_terms = 0;
@@ -661,7 +692,8 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
             // threads == 1 << kC64ThreadBits whenever lo has register bits
             const uint32_t lt = (uint32_t)(sg.lo & tmask_t), lm = sg.lo >> pl.tb;
             const uint32_t dx = (lt << 3) | (lm << (pl.tb + 3));
-            td.push_back(make_uint2(dx | (tvar << 31), zt | (bt0 << 10) | (bt1 << 20)));
+            td.push_back(make_uint2(dx | (half[i] << 15) | (tvar << 31),
+                                    zt | (bt0 << 10) | (bt1 << 20)));
             TileDataC64 d;
             memset(&d, 0, sizeof(d));
             d.z0h = sg.z0 >> pl.b;
@@ -671,11 +703,14 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
                 d.T[u] = make_float2((float)sg.table[u].re, (float)sg.table[u].im);
             tdd.push_back(d);
         }
-        for (uint32_t j = 0; j < pl.nblocks; ++j) {
+        // runs per block, or per pair of blocks
+        const std::vector<uint32_t> &rng = pl.npairs ? pg0 : bg0;
+        const uint32_t nunits = pl.npairs ? pl.npairs : pl.nblocks;
+        for (uint32_t j = 0; j < nunits; ++j) {
             r0v.push_back((uint32_t)rkey.size());
-            for (uint32_t g = bg0[j]; g < bg0[j + 1]; ++g) {
+            for (uint32_t g = rng[j]; g < rng[j + 1]; ++g) {
                 const uint32_t k = runkey(subs[ord[g]]) & 31u;
-                if (g == bg0[j] || k != rkey.back()) {
+                if (g == rng[j] || k != rkey.back()) {
                     rkey.push_back(k);
                     rg0.push_back(g);
                 }
@@ -1036,6 +1071,7 @@ static int apply_impl(const char *name, qr_op *op, int32_t dtype, const void *ps
     a.nruns = pl.nruns;
     a.chunks = pl.chunks.as<uint4>();
     a.nchunks = pl.nchunks;
+    a.npairs = pl.npairs;
     a.v = v;
     if (v) {
         a.ar = alpha[0];
