@@ -415,17 +415,17 @@ constexpr int kTabEnt = 4;  // per-tile table entries (float4) per sub-group
 // full barriers, stage counters and the abort flag, rounded to 8 bytes
 constexpr size_t kTabBarBytes = ((size_t)kTabStages * 12u + 4u + 7u) & ~(size_t)7u;
 
-template <int AMPS, int ZM, bool XM>
+template <int AMPS, int ZM, bool XM, bool TV>
 __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                         const unsigned char *sm, uint32_t soff,
                                         const float4 *s_tab, const uint2 *tdesc, uint32_t g0,
                                         uint32_t g1, uint32_t t, uint32_t t8) {
     for (uint32_t g = g0; g < g1; ++g) {
         const uint2 d = tdesc[g];
-        // thread parities against the three masks, skipped (warp-uniformly)
-        // when the factor does not depend on the thread
+        // thread parities against the three masks, only in runs whose factor
+        // depends on the thread (compile-time: no branch per sub-group)
         uint32_t u = 0, sg = 0;
-        if (d.x >> 31) {
+        if constexpr (TV) {
             sg = (uint32_t)__popc(t & (d.y & 0x3ffu)) & 1u;
             u = ((uint32_t)__popc(t & ((d.y >> 10) & 0x3ffu)) & 1u) |
                 (((uint32_t)__popc(t & ((d.y >> 20) & 0x3ffu)) & 1u) << 1);
@@ -467,19 +467,17 @@ __device__ __forceinline__ void run_tab_dispatch(uint32_t key, float2 (&A)[AMPS]
 #define QR_RUN_CASE(k)                                                                    \
     case k:                                                                               \
         if constexpr ((k & 15) < AMPS)                                                    \
-            run_tab<AMPS, (k & 15), (k >> 4) != 0>(A, B, sm, soff, s_tab, tdesc, g0, g1, t, t8); \
+            run_tab<AMPS, (k & 15), ((k >> 4) & 1) != 0, (k >> 5) != 0>(A, B, sm, soff, s_tab, \
+                                                                       tdesc, g0, g1, t, t8); \
         break;
+#define QR_RUN_CASE8(k) QR_RUN_CASE(k) QR_RUN_CASE(k + 1) QR_RUN_CASE(k + 2) QR_RUN_CASE(k + 3) \
+    QR_RUN_CASE(k + 4) QR_RUN_CASE(k + 5) QR_RUN_CASE(k + 6) QR_RUN_CASE(k + 7)
     switch (key) {
-        QR_RUN_CASE(0) QR_RUN_CASE(1) QR_RUN_CASE(2) QR_RUN_CASE(3)
-        QR_RUN_CASE(4) QR_RUN_CASE(5) QR_RUN_CASE(6) QR_RUN_CASE(7)
-        QR_RUN_CASE(8) QR_RUN_CASE(9) QR_RUN_CASE(10) QR_RUN_CASE(11)
-        QR_RUN_CASE(12) QR_RUN_CASE(13) QR_RUN_CASE(14) QR_RUN_CASE(15)
-        QR_RUN_CASE(16) QR_RUN_CASE(17) QR_RUN_CASE(18) QR_RUN_CASE(19)
-        QR_RUN_CASE(20) QR_RUN_CASE(21) QR_RUN_CASE(22) QR_RUN_CASE(23)
-        QR_RUN_CASE(24) QR_RUN_CASE(25) QR_RUN_CASE(26) QR_RUN_CASE(27)
-        QR_RUN_CASE(28) QR_RUN_CASE(29) QR_RUN_CASE(30) QR_RUN_CASE(31)
+        QR_RUN_CASE8(0) QR_RUN_CASE8(8) QR_RUN_CASE8(16) QR_RUN_CASE8(24)
+        QR_RUN_CASE8(32) QR_RUN_CASE8(40) QR_RUN_CASE8(48) QR_RUN_CASE8(56)
         default: break;
     }
+#undef QR_RUN_CASE8
 #undef QR_RUN_CASE
 }
 

@@ -80,7 +80,7 @@ struct ApplyArgs {
     const TileDataC64 *tdata;
     const uint32_t *blk_r0;   // runs of block (pair) j: [blk_r0[j], blk_r0[j+1])
     const uint32_t *run_g0;   // sub-groups of run r: [run_g0[r], run_g0[r+1])
-    const uint32_t *run_key;  // key = zm | xm << 4
+    const uint32_t *run_key;  // key = zm | xm << 4 | tv << 5 (factor depends on the thread)
     uint32_t nruns;
     // chunks of consecutive blocks with at most kTabCap sub-groups:
     // {first sub-group, first run, first block, 0}, nchunks + 1 entries

@@ -544,9 +544,14 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     // order: partner tile ascending, then (c64c) run key zm with fat last
     std::vector<size_t> ord(subs.size());
     for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+    // run key: register-bit sign pattern zm, register bits in the partner
+    // XOR (xm), and whether the factor depends on the thread index (tv)
     auto runkey = [&](const SubGroup &g) -> uint32_t {
         if (g.d == kFat || g.d > 2) return 0xffffffffu;
-        return (g.zm & 15u) | (((g.lo >> pl.tb) != 0 ? 1u : 0u) << 4);
+        const uint64_t tm = (uint64_t)pl.threads - 1;
+        const uint64_t b0 = g.d > 0 ? g.beta[0] : 0, b1 = g.d > 1 ? g.beta[1] : 0;
+        const uint32_t tv = ((g.z0 | b0 | b1) & tm) != 0 ? 1u : 0u;
+        return (g.zm & 15u) | (((g.lo >> pl.tb) != 0 ? 1u : 0u) << 4) | (tv << 5);
     };
     std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
         if (subs[a].hi != subs[b].hi) return subs[a].hi < subs[b].hi;
@@ -709,7 +714,7 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         for (uint32_t j = 0; j < nunits; ++j) {
             r0v.push_back((uint32_t)rkey.size());
             for (uint32_t g = rng[j]; g < rng[j + 1]; ++g) {
-                const uint32_t k = runkey(subs[ord[g]]) & 31u;
+                const uint32_t k = runkey(subs[ord[g]]) & 63u;
                 if (g == rng[j] || k != rkey.back()) {
                     rkey.push_back(k);
                     rg0.push_back(g);
