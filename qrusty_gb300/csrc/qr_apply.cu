@@ -416,11 +416,11 @@ constexpr int kTabEnt = 4;  // per-tile table entries (float4) per sub-group
 constexpr size_t kTabBarBytes = ((size_t)kTabStages * 12u + 4u + 7u) & ~(size_t)7u;
 
 template <int AMPS, int ZM, bool XM, bool TV>
-__device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                        const unsigned char *sm, uint32_t soff,
-                                        const float4 *s_tab, const uint2 *tdesc, uint32_t g0,
-                                        uint32_t g1, uint32_t t, uint32_t t8) {
-    for (uint32_t g = g0; g < g1; ++g) {
+__device__ __forceinline__ void sub_tab_one(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                            const unsigned char *sm, uint32_t soff,
+                                            const float4 *s_tab, const uint2 *tdesc, uint32_t g,
+                                            uint32_t t, uint32_t t8) {
+    {
         const uint2 d = tdesc[g];
         // thread parities against the three masks, only in runs whose factor
         // depends on the thread (compile-time: no branch per sub-group)
@@ -456,6 +456,21 @@ __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
             B[m] = __ffma2_rn(neg ? bn : bp, p[m], B[m]);
         }
     }
+}
+
+// two sub-groups per iteration: the second one's loads can issue ahead of
+// the first one's packed FMAs
+template <int AMPS, int ZM, bool XM, bool TV>
+__device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                        const unsigned char *sm, uint32_t soff,
+                                        const float4 *s_tab, const uint2 *tdesc, uint32_t g0,
+                                        uint32_t g1, uint32_t t, uint32_t t8) {
+    uint32_t g = g0;
+    for (; g + 1 < g1; g += 2) {
+        sub_tab_one<AMPS, ZM, XM, TV>(A, B, sm, soff, s_tab, tdesc, g, t, t8);
+        sub_tab_one<AMPS, ZM, XM, TV>(A, B, sm, soff, s_tab, tdesc, g + 1, t, t8);
+    }
+    if (g < g1) sub_tab_one<AMPS, ZM, XM, TV>(A, B, sm, soff, s_tab, tdesc, g, t, t8);
 }
 
 template <int AMPS>
