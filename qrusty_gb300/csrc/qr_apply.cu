@@ -473,6 +473,73 @@ __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
     if (g < g1) sub_tab_one<AMPS, ZM, XM, TV>(A, B, sm, soff, s_tab, tdesc, g, t, t8);
 }
 
+// Two sub-groups g, g+1 of one x group (same partner amplitudes) whose
+// register-bit sign patterns are ZM and ZM ^ (1 << BB): an x group split
+// because its terms' z differ on one register bit.  One set of partner loads
+// serves both; the factor at register index m is
+//   (-1)^popc(m & ZM) * (F_g + (-1)^(m_BB) F_{g+1}),
+// with F the thread-signed table entries, so the pair costs the packed FMAs
+// of a single sub-group plus four packed adds.
+template <int AMPS, int ZM, int BB, bool XM, bool TV>
+__device__ __forceinline__ void sub_tab_fused(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                              const unsigned char *sm, uint32_t soff,
+                                              const float4 *s_tab, const uint2 *tdesc, uint32_t g,
+                                              uint32_t t, uint32_t t8) {
+    const uint2 da = tdesc[g], db = tdesc[g + 1];
+    uint32_t ua = 0, sa = 0, ub = 0, sb = 0;
+    if constexpr (TV) {
+        sa = (uint32_t)__popc(t & (da.y & 0x3ffu)) & 1u;
+        ua = ((uint32_t)__popc(t & ((da.y >> 10) & 0x3ffu)) & 1u) |
+             (((uint32_t)__popc(t & ((da.y >> 20) & 0x3ffu)) & 1u) << 1);
+        sb = (uint32_t)__popc(t & (db.y & 0x3ffu)) & 1u;
+        ub = ((uint32_t)__popc(t & ((db.y >> 10) & 0x3ffu)) & 1u) |
+             (((uint32_t)__popc(t & ((db.y >> 20) & 0x3ffu)) & 1u) << 1);
+    }
+    const float4 Ta = s_tab[g * 4 + ua];
+    const float4 Tb = s_tab[(g + 1) * 4 + ub];
+    const float sva = __uint_as_float(0x3f800000u | (sa << 31));
+    const float svb = __uint_as_float(0x3f800000u | (sb << 31));
+    const float2 apa = __fmul2_rn(make_float2(Ta.x, Ta.y), make_float2(sva, sva));
+    const float2 bpa = __fmul2_rn(make_float2(Ta.z, Ta.w), make_float2(sva, sva));
+    // F_a + F_b and F_a - F_b: one rounding each (the sign products are exact)
+    const float2 a0 = __ffma2_rn(make_float2(Tb.x, Tb.y), make_float2(svb, svb), apa);
+    const float2 b0 = __ffma2_rn(make_float2(Tb.z, Tb.w), make_float2(svb, svb), bpa);
+    const float2 a1 = __ffma2_rn(make_float2(Tb.x, Tb.y), make_float2(-svb, -svb), apa);
+    const float2 b1 = __ffma2_rn(make_float2(Tb.z, Tb.w), make_float2(-svb, -svb), bpa);
+    const uint32_t off = soff | (t8 ^ (da.x & 0xffffu));
+    float2 p[AMPS];
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        const uint32_t o = XM ? (off ^ ((uint32_t)m << kMsh)) : (off + ((uint32_t)m << kMsh));
+        p[m] = *reinterpret_cast<const float2 *>(sm + o);
+    }
+    float2 na0 = a0, nb0 = b0, na1 = a1, nb1 = b1;
+    if constexpr (ZM != 0) {
+        na0 = __fmul2_rn(a0, make_float2(-1.f, -1.f));
+        nb0 = __fmul2_rn(b0, make_float2(-1.f, -1.f));
+        na1 = __fmul2_rn(a1, make_float2(-1.f, -1.f));
+        nb1 = __fmul2_rn(b1, make_float2(-1.f, -1.f));
+    }
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
+        const bool sel = ((m >> BB) & 1) != 0;
+        const float2 fa = neg ? (sel ? na1 : na0) : (sel ? a1 : a0);
+        const float2 fb = neg ? (sel ? nb1 : nb0) : (sel ? b1 : b0);
+        A[m] = __ffma2_rn(fa, p[m], A[m]);
+        B[m] = __ffma2_rn(fb, p[m], B[m]);
+    }
+}
+
+template <int AMPS, int ZM, int BB, bool XM, bool TV>
+__device__ __forceinline__ void run_fused(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                          const unsigned char *sm, uint32_t soff,
+                                          const float4 *s_tab, const uint2 *tdesc, uint32_t g0,
+                                          uint32_t g1, uint32_t t, uint32_t t8) {
+    for (uint32_t g = g0; g + 1 < g1; g += 2)
+        sub_tab_fused<AMPS, ZM, BB, XM, TV>(A, B, sm, soff, s_tab, tdesc, g, t, t8);
+}
+
 template <int AMPS>
 __device__ __forceinline__ void run_tab_dispatch(uint32_t key, float2 (&A)[AMPS],
                                                  float2 (&B)[AMPS], const unsigned char *sm,
@@ -494,6 +561,38 @@ __device__ __forceinline__ void run_tab_dispatch(uint32_t key, float2 (&A)[AMPS]
     }
 #undef QR_RUN_CASE8
 #undef QR_RUN_CASE
+}
+
+// Pair-plan runs: keys below 64 as run_tab_dispatch; 64 + (ZM | BB << 3 |
+// XM << 5 | TV << 6) is a run of fused sub-group pairs (sub_tab_fused).
+template <int AMPS>
+__device__ __forceinline__ void run_pair_dispatch(uint32_t key, float2 (&A)[AMPS],
+                                                  float2 (&B)[AMPS], const unsigned char *sm,
+                                                  uint32_t soff, const float4 *s_tab,
+                                                  const uint2 *tdesc, uint32_t g0, uint32_t g1,
+                                                  uint32_t t, uint32_t t8) {
+    if (key < 64u) {
+        run_tab_dispatch<AMPS>(key, A, B, sm, soff, s_tab, tdesc, g0, g1, t, t8);
+        return;
+    }
+#define QR_FUSED_CASE(k)                                                                  \
+    case k:                                                                               \
+        if constexpr ((k & 7) < AMPS && (1 << ((k >> 3) & 3)) < AMPS)                     \
+            run_fused<AMPS, (k & 7), ((k >> 3) & 3), ((k >> 5) & 1) != 0, ((k >> 6) & 1) != 0>( \
+                A, B, sm, soff, s_tab, tdesc, g0, g1, t, t8);                             \
+        break;
+#define QR_FUSED_CASE8(k) QR_FUSED_CASE(k) QR_FUSED_CASE(k + 1) QR_FUSED_CASE(k + 2) \
+    QR_FUSED_CASE(k + 3) QR_FUSED_CASE(k + 4) QR_FUSED_CASE(k + 5) QR_FUSED_CASE(k + 6) \
+    QR_FUSED_CASE(k + 7)
+    switch (key - 64u) {
+        QR_FUSED_CASE8(0) QR_FUSED_CASE8(8) QR_FUSED_CASE8(16)
+        QR_FUSED_CASE8(32) QR_FUSED_CASE8(40) QR_FUSED_CASE8(48)
+        QR_FUSED_CASE8(64) QR_FUSED_CASE8(72) QR_FUSED_CASE8(80)
+        QR_FUSED_CASE8(96) QR_FUSED_CASE8(104) QR_FUSED_CASE8(112)
+        default: break;
+    }
+#undef QR_FUSED_CASE8
+#undef QR_FUSED_CASE
 }
 
 template <int AMPS, bool WIDE, bool MULTI>
@@ -855,8 +954,8 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
         uint32_t rw = s_run[s_blk[p]];
         for (uint32_t r = s_blk[p]; r < r1; ++r) {
             const uint32_t rn = s_run[r + 1];
-            run_tab_dispatch<AMPS>(rw >> 16, A, B, smem_raw, soff, s_tab, tdesc, rw & 0xffffu,
-                                   rn & 0xffffu, t, t8);
+            run_pair_dispatch<AMPS>(rw >> 16, A, B, smem_raw, soff, s_tab, tdesc, rw & 0xffffu,
+                                    rn & 0xffffu, t, t8);
             rw = rn;
         }
 

@@ -597,7 +597,7 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     // single-chunk c64c plans: partner blocks are visited in pairs (two
     // stages behind one barrier, one ring slot); each pair's sub-groups are
     // merged and sorted by run key, their block recorded as the half
-    std::vector<uint32_t> half(ord.size(), 0u), pg0;
+    std::vector<uint32_t> half(ord.size(), 0u), pg0, pkey;
     pl.npairs = 0;
     if (f32 && tile_bits < 0 && ord.size() <= (size_t)kTabCap && pl.nblocks >= 2 &&
         pl.amps == 8) {
@@ -605,18 +605,61 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         std::vector<size_t> ord2;
         std::vector<uint32_t> half2;
         ord2.reserve(ord.size());
+        const uint64_t tm = (uint64_t)pl.threads - 1;
+        auto small = [&](const SubGroup &g) { return g.d != kFat && g.d <= 2; };
+        auto thread_var = [&](const SubGroup &g) -> uint32_t {
+            const uint64_t b0 = g.d > 0 ? g.beta[0] : 0, b1 = g.d > 1 ? g.beta[1] : 0;
+            return ((g.z0 | b0 | b1) & tm) != 0 ? 1u : 0u;
+        };
         for (uint32_t p = 0; p < np; ++p) {
             pg0.push_back((uint32_t)ord2.size());
             const uint32_t ga = bg0[2 * p], gm = bg0[std::min(2 * p + 1, pl.nblocks)],
                            gb = bg0[std::min(2 * p + 2, pl.nblocks)];
+            // fused pairs: two sub-groups of one x group (same partner
+            // amplitudes) whose register-bit sign patterns differ in one bit
             std::vector<uint32_t> items;
-            for (uint32_t i = ga; i < gb; ++i) items.push_back(i);
+            std::vector<char> used(gb - ga, 0);
+            struct Fused { uint32_t key, a, b; };
+            std::vector<Fused> fused;
+            for (uint32_t i = ga; i < gb; ++i) {
+                const SubGroup &si = subs[ord[i]];
+                if (used[i - ga]) continue;
+                for (uint32_t j = i + 1; j < gb && small(si); ++j) {
+                    const SubGroup &sj = subs[ord[j]];
+                    if (used[j - ga] || !small(sj) || si.hi != sj.hi || si.lo != sj.lo ||
+                        (i >= gm) != (j >= gm))
+                        continue;
+                    const uint32_t diff = si.zm ^ sj.zm;
+                    if (__builtin_popcount(diff) != 1) continue;
+                    const uint32_t a = si.zm < sj.zm ? i : j, b = si.zm < sj.zm ? j : i;
+                    const uint32_t bb = (uint32_t)__builtin_ctz(diff);
+                    const uint32_t xm = (si.lo >> pl.tb) != 0 ? 1u : 0u;
+                    const uint32_t tv = thread_var(si) | thread_var(sj);
+                    // key 64 + (ZM | BB << 3 | XM << 5 | TV << 6): 64..191
+                    fused.push_back({64u + ((subs[ord[a]].zm & 7u) | (bb << 3) | (xm << 5) |
+                                            (tv << 6)),
+                                     a, b});
+                    used[i - ga] = used[j - ga] = 1;
+                    break;
+                }
+                if (!used[i - ga]) items.push_back(i);
+            }
             std::stable_sort(items.begin(), items.end(), [&](uint32_t x, uint32_t y) {
                 return runkey(subs[ord[x]]) < runkey(subs[ord[y]]);
             });
+            std::stable_sort(fused.begin(), fused.end(),
+                             [](const Fused &x, const Fused &y) { return x.key < y.key; });
             for (uint32_t i : items) {
                 ord2.push_back(ord[i]);
                 half2.push_back(i >= gm ? 1u : 0u);
+                pkey.push_back(runkey(subs[ord[i]]) & 63u);
+            }
+            for (const Fused &f : fused) {
+                for (uint32_t i : {f.a, f.b}) {
+                    ord2.push_back(ord[i]);
+                    half2.push_back(i >= gm ? 1u : 0u);
+                    pkey.push_back(f.key);
+                }
             }
         }
         pg0.push_back((uint32_t)ord2.size());
@@ -714,7 +757,8 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         for (uint32_t j = 0; j < nunits; ++j) {
             r0v.push_back((uint32_t)rkey.size());
             for (uint32_t g = rng[j]; g < rng[j + 1]; ++g) {
-                const uint32_t k = runkey(subs[ord[g]]) & 63u;
+                // pair plans: per-position keys (fused pairs carry keys >= 64)
+                const uint32_t k = pl.npairs ? pkey[g] : (runkey(subs[ord[g]]) & 63u);
                 if (g == rng[j] || k != rkey.back()) {
                     rkey.push_back(k);
                     rg0.push_back(g);
