@@ -138,6 +138,71 @@ def test_adjoint(cuda, oracle):
     assert rel(y64.astype(np.complex128), want) <= TOL_C64C
 
 
+def register_split_op(rng, n, ngroups):
+    """x groups whose terms' z differ in register bits of the compensated
+    kernel's layout (bits 9-11 of a 4,096-amplitude tile; thread t holds
+    amplitudes t + 512 m, m < 8).  Variant by group index g: the split bit
+    cycles through 9, 10, 11; the sign pattern z & 0xe00 is zero or not; z on
+    the thread bits (0-8) is zero or not; the group has rank 0, 1 (a tile
+    bit) or 2 (a thread bit too) inside each half; every fifth group is split
+    on two register bits (four sub-groups)."""
+    xs, zs, ph = [], [], []
+    seen = set()
+    for g in range(ngroups):
+        while True:
+            hi = int(rng.integers(0, 1 << (n - 12)))
+            reg = int(rng.integers(0, 8)) if g % 2 else 0
+            x = (hi << 12) | (reg << 9) | int(rng.integers(0, 1 << 9))
+            if x and x not in seen:
+                seen.add(x)
+                break
+        z0 = int(rng.integers(0, 1 << n))
+        if g % 3 == 0:
+            z0 &= ~0x1ff          # factor constant over the thread index
+        if g % 4 == 1:
+            z0 &= ~0xe00          # no register-bit sign pattern
+        bb = 1 << (9 + g % 3)
+        zg = [z0, z0 ^ bb]
+        if g % 5 == 4:
+            b2 = 1 << (9 + (g + 1) % 3)
+            zg += [z0 ^ b2, z0 ^ bb ^ b2]
+        if g % 4 >= 2:            # rank 1 on a tile bit
+            t1 = 1 << int(rng.integers(12, n))
+            zg += [z ^ t1 for z in zg]
+        if g % 4 == 3:            # rank 2: a thread bit too
+            t2 = 1 << int(rng.integers(0, 9))
+            zg += [z ^ t2 for z in zg]
+        for z in zg:
+            xs.append(x)
+            zs.append(z)
+            ph.append(int(rng.integers(0, 4)))
+    T = len(xs)
+    c = rng.standard_normal(T) + 1j * rng.standard_normal(T)
+    return (np.array(xs, np.uint64), np.array(zs, np.uint64), np.array(ph, np.uint8), c)
+
+
+@pytest.mark.parametrize("n,ngroups", [(13, 40), (15, 90)])
+def test_register_bit_split_groups(cuda, oracle, n, ngroups):
+    """Sub-groups of one x group that differ in one register bit of z share
+    their partner loads in the compensated kernel (fused pairs): every key
+    variant, forward and adjoint, against the oracle."""
+    import torch
+    rng = np.random.default_rng(31 * n + ngroups)
+    x, z, ph, c = register_split_op(rng, n, ngroups)
+    psi = W.random_state(rng, 1 << n)
+    op, _, _ = check(cuda, oracle, n, x, z, ph, c, psi)
+    assert ngroups < op.info()["nsub"] <= 512
+    cp = oracle.make_params(ph, c)
+    ip, ij, d = oracle.csr_build(n, x, z, cp)
+    A = sps.csr_matrix((d, ij.astype(np.int64), ip.astype(np.int64)), shape=(1 << n, 1 << n))
+    want = A.conj().T @ psi
+    p = torch.from_numpy(psi).to(cuda)
+    y128 = op.apply(p, adjoint=True).cpu().numpy()
+    y64 = op.apply(p.to(torch.complex64), adjoint=True).cpu().numpy()
+    assert rel(y128, want) <= TOL_C128
+    assert rel(y64.astype(np.complex128), want) <= TOL_C64C
+
+
 def test_multi_state(cuda, oracle):
     import torch
     t, _ = W.cfg1(with_state=False, n=14)
