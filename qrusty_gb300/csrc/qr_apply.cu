@@ -412,23 +412,24 @@ __device__ __forceinline__ void big_group_c64(float2 (&A)[AMPS], float2 (&B)[AMP
 constexpr int kTabStages = 4;  // partner-tile ring depth (timed best of 3, 4, 5)
 constexpr size_t kMaxSmemPerBlock = 227u * 1024u;  // sm_100-family opt-in limit
 constexpr int kTabEnt = 4;  // per-tile table entries (float4) per sub-group
-// full barriers, stage counters and the abort flag, rounded to 8 bytes
-constexpr size_t kTabBarBytes = ((size_t)kTabStages * 12u + 4u + 7u) & ~(size_t)7u;
+// full barriers, stage counters and the abort flag, rounded to 16 bytes so
+// that the 16-byte thread descriptors after them stay aligned
+constexpr size_t kTabBarBytes = ((size_t)kTabStages * 12u + 4u + 15u) & ~(size_t)15u;
+static_assert(kTabBarBytes % 16 == 0, "thread descriptors need 16-byte alignment");
 
 template <int AMPS, int ZM, bool XM, bool TV>
 __device__ __forceinline__ void sub_tab_one(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                             const unsigned char *sm, uint32_t soff,
-                                            const float4 *s_tab, const uint2 *tdesc, uint32_t g,
+                                            const float4 *s_tab, const uint4 *tdesc, uint32_t g,
                                             uint32_t t, uint32_t t8) {
     {
-        const uint2 d = tdesc[g];
+        const uint4 d = tdesc[g];
         // thread parities against the three masks, only in runs whose factor
         // depends on the thread (compile-time: no branch per sub-group)
         uint32_t u = 0, sg = 0;
         if constexpr (TV) {
-            sg = (uint32_t)__popc(t & (d.y & 0x3ffu)) & 1u;
-            u = ((uint32_t)__popc(t & ((d.y >> 10) & 0x3ffu)) & 1u) |
-                (((uint32_t)__popc(t & ((d.y >> 20) & 0x3ffu)) & 1u) << 1);
+            sg = (uint32_t)__popc(t & d.y) & 1u;
+            u = ((uint32_t)__popc(t & d.z) & 1u) | (((uint32_t)__popc(t & d.w) & 1u) << 1);
         }
         const float4 T = s_tab[g * 4 + u];
         // thread sign (-1)^sg on both factor pairs: one packed multiply each
@@ -463,7 +464,7 @@ __device__ __forceinline__ void sub_tab_one(float2 (&A)[AMPS], float2 (&B)[AMPS]
 template <int AMPS, int ZM, bool XM, bool TV>
 __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                         const unsigned char *sm, uint32_t soff,
-                                        const float4 *s_tab, const uint2 *tdesc, uint32_t g0,
+                                        const float4 *s_tab, const uint4 *tdesc, uint32_t g0,
                                         uint32_t g1, uint32_t t, uint32_t t8) {
     uint32_t g = g0;
     for (; g + 1 < g1; g += 2) {
@@ -483,17 +484,15 @@ __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
 template <int AMPS, int ZM, int BB, bool XM, bool TV>
 __device__ __forceinline__ void sub_tab_fused(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                               const unsigned char *sm, uint32_t soff,
-                                              const float4 *s_tab, const uint2 *tdesc, uint32_t g,
+                                              const float4 *s_tab, const uint4 *tdesc, uint32_t g,
                                               uint32_t t, uint32_t t8) {
-    const uint2 da = tdesc[g], db = tdesc[g + 1];
+    const uint4 da = tdesc[g], db = tdesc[g + 1];
     uint32_t ua = 0, sa = 0, ub = 0, sb = 0;
     if constexpr (TV) {
-        sa = (uint32_t)__popc(t & (da.y & 0x3ffu)) & 1u;
-        ua = ((uint32_t)__popc(t & ((da.y >> 10) & 0x3ffu)) & 1u) |
-             (((uint32_t)__popc(t & ((da.y >> 20) & 0x3ffu)) & 1u) << 1);
-        sb = (uint32_t)__popc(t & (db.y & 0x3ffu)) & 1u;
-        ub = ((uint32_t)__popc(t & ((db.y >> 10) & 0x3ffu)) & 1u) |
-             (((uint32_t)__popc(t & ((db.y >> 20) & 0x3ffu)) & 1u) << 1);
+        sa = (uint32_t)__popc(t & da.y) & 1u;
+        ua = ((uint32_t)__popc(t & da.z) & 1u) | (((uint32_t)__popc(t & da.w) & 1u) << 1);
+        sb = (uint32_t)__popc(t & db.y) & 1u;
+        ub = ((uint32_t)__popc(t & db.z) & 1u) | (((uint32_t)__popc(t & db.w) & 1u) << 1);
     }
     const float4 Ta = s_tab[g * 4 + ua];
     const float4 Tb = s_tab[(g + 1) * 4 + ub];
@@ -534,7 +533,7 @@ __device__ __forceinline__ void sub_tab_fused(float2 (&A)[AMPS], float2 (&B)[AMP
 template <int AMPS, int ZM, int BB, bool XM, bool TV>
 __device__ __forceinline__ void run_fused(float2 (&A)[AMPS], float2 (&B)[AMPS],
                                           const unsigned char *sm, uint32_t soff,
-                                          const float4 *s_tab, const uint2 *tdesc, uint32_t g0,
+                                          const float4 *s_tab, const uint4 *tdesc, uint32_t g0,
                                           uint32_t g1, uint32_t t, uint32_t t8) {
     for (uint32_t g = g0; g + 1 < g1; g += 2)
         sub_tab_fused<AMPS, ZM, BB, XM, TV>(A, B, sm, soff, s_tab, tdesc, g, t, t8);
@@ -544,7 +543,7 @@ template <int AMPS>
 __device__ __forceinline__ void run_tab_dispatch(uint32_t key, float2 (&A)[AMPS],
                                                  float2 (&B)[AMPS], const unsigned char *sm,
                                                  uint32_t soff, const float4 *s_tab,
-                                                 const uint2 *tdesc, uint32_t g0, uint32_t g1,
+                                                 const uint4 *tdesc, uint32_t g0, uint32_t g1,
                                                  uint32_t t, uint32_t t8) {
 #define QR_RUN_CASE(k)                                                                    \
     case k:                                                                               \
@@ -569,7 +568,7 @@ template <int AMPS>
 __device__ __forceinline__ void run_pair_dispatch(uint32_t key, float2 (&A)[AMPS],
                                                   float2 (&B)[AMPS], const unsigned char *sm,
                                                   uint32_t soff, const float4 *s_tab,
-                                                  const uint2 *tdesc, uint32_t g0, uint32_t g1,
+                                                  const uint4 *tdesc, uint32_t g0, uint32_t g1,
                                                   uint32_t t, uint32_t t8) {
     if (key < 64u) {
         run_tab_dispatch<AMPS>(key, A, B, sm, soff, s_tab, tdesc, g0, g1, t, t8);
@@ -612,7 +611,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
     // sub-group descriptors, runs (g0 | key << 16) and per-block run ranges of
     // the current chunk, indices relative to the chunk; with one chunk they
     // are staged once per CTA
-    uint2 *s_td = reinterpret_cast<uint2 *>(reinterpret_cast<unsigned char *>(s_lo) +
+    uint4 *s_td = reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(s_lo) +
                                             (size_t)AMPS * threads * 8u + kTabBarBytes);
     uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + kTabCap);
     uint32_t *s_blk = s_run + kTabCap + 1;
@@ -622,7 +621,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
             s_run[i] = a.run_g0[i] | (i < a.nruns ? a.run_key[i] << 16 : 0u);
         for (uint32_t i = t; i <= a.nblocks; i += threads) s_blk[i] = a.blk_r0[i];
     }
-    const uint2 *tdesc = s_td;
+    const uint4 *tdesc = s_td;
 
     const float2 *psi = static_cast<const float2 *>(a.psi);
     float2 *y = static_cast<float2 *>(a.y);
@@ -835,7 +834,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
     uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kTabStages);
     volatile uint32_t *s_abort = cnt + kTabStages;
-    uint2 *s_td = reinterpret_cast<uint2 *>(reinterpret_cast<unsigned char *>(s_lo) +
+    uint4 *s_td = reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(s_lo) +
                                             (size_t)AMPS * threads * 8u + kTabBarBytes);
     uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + kTabCap);
     uint32_t *s_blk = s_run + kTabCap + 1;
@@ -844,7 +843,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     for (uint32_t i = t; i <= a.nruns; i += threads)
         s_run[i] = a.run_g0[i] | (i < a.nruns ? a.run_key[i] << 16 : 0u);
     for (uint32_t i = t; i <= np; i += threads) s_blk[i] = a.blk_r0[i];
-    const uint2 *tdesc = s_td;
+    const uint4 *tdesc = s_td;
 
     const float2 *psi = static_cast<const float2 *>(a.psi);
     float2 *y = static_cast<float2 *>(a.y);
@@ -950,13 +949,22 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
             }
         }
 
-        const uint32_t r1 = skip ? 0u : s_blk[p + 1];
-        uint32_t rw = s_run[s_blk[p]];
-        for (uint32_t r = s_blk[p]; r < r1; ++r) {
-            const uint32_t rn = s_run[r + 1];
-            run_pair_dispatch<AMPS>(rw >> 16, A, B, smem_raw, soff, s_tab, tdesc, rw & 0xffffu,
-                                    rn & 0xffffu, t, t8);
-            rw = rn;
+        // bit 31 of a pair's first run: exactly two sub-groups of key 0
+        const uint32_t bw = s_blk[p];
+        const uint32_t rb = bw & 0x7fffffffu;
+        if (!skip && (bw >> 31) != 0) {
+            const uint32_t g0 = s_run[rb] & 0xffffu;
+            sub_tab_one<AMPS, 0, false, false>(A, B, smem_raw, soff, s_tab, tdesc, g0, t, t8);
+            sub_tab_one<AMPS, 0, false, false>(A, B, smem_raw, soff, s_tab, tdesc, g0 + 1, t, t8);
+        } else {
+            const uint32_t r1 = skip ? 0u : (s_blk[p + 1] & 0x7fffffffu);
+            uint32_t rw = s_run[rb];
+            for (uint32_t r = rb; r < r1; ++r) {
+                const uint32_t rn = s_run[r + 1];
+                run_pair_dispatch<AMPS>(rw >> 16, A, B, smem_raw, soff, s_tab, tdesc,
+                                        rw & 0xffffu, rn & 0xffffu, t, t8);
+                rw = rn;
+            }
         }
 
         const bool last = (p == np - 1);
@@ -1033,7 +1041,7 @@ static size_t tab_smem_bytes(const ApplyArgs &a, int threads) {
     const uint32_t tabn = a.nsub < kTabCap ? a.nsub : kTabCap;
     return (size_t)kTabStages * tile_bytes + (size_t)tabn * 16u * kTabEnt +
            (size_t)AMPS * threads * 8u + kTabBarBytes +
-           (size_t)kTabCap * 8u + (2u * (size_t)kTabCap + 3u) * 4u;
+           (size_t)kTabCap * sizeof(uint4) + (2u * (size_t)kTabCap + 3u) * 4u;
 }
 
 template <int AMPS, bool WIDE>

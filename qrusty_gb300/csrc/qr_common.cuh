@@ -72,15 +72,18 @@ struct ApplyArgs {
     // compensated-c64 plan: one SubDescC64 per sub-group (see qr_apply.cu)
     const SubDescC64 *sub;
     uint32_t nsub;
-    // per-tile-table kernel: per sub-group an 8-byte thread descriptor
-    // {partner byte-offset XOR | pair half << 15 | tvar << 31,
-    //  z0_t | beta0_t << 10 | beta1_t << 20} and its TileDataC64; sub-groups
-    // of a block (or pair of blocks) in runs of equal key
-    const uint2 *tdesc;
+    // per-tile-table kernel: per sub-group a 16-byte thread descriptor
+    // {partner byte-offset XOR | pair half << 15 | tvar << 31, z0_t, beta0_t,
+    //  beta1_t} (the thread-bit parts of z0 and of the basis) and its
+    // TileDataC64; sub-groups of a block (or pair of blocks) in runs of
+    // equal key
+    const uint4 *tdesc;
     const TileDataC64 *tdata;
     const uint32_t *blk_r0;   // runs of block (pair) j: [blk_r0[j], blk_r0[j+1])
     const uint32_t *run_g0;   // sub-groups of run r: [run_g0[r], run_g0[r+1])
-    const uint32_t *run_key;  // key = zm | xm << 4 | tv << 5 (factor depends on the thread)
+    const uint32_t *run_key;  // key = zm | xm << 4 | tv << 5 (factor depends on the thread);
+                              // pair plans: 64 + (zm | bb << 3 | xm << 5 | tv << 6) for
+                              // runs of fused sub-group pairs
     uint32_t nruns;
     // chunks of consecutive blocks with at most kTabCap sub-groups:
     // {first sub-group, first run, first block, 0}, nchunks + 1 entries

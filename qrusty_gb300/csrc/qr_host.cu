@@ -724,7 +724,7 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     }
     if (f32) {
         // per-tile-table kernel arrays
-        std::vector<uint2> td;
+        std::vector<uint4> td;
         std::vector<TileDataC64> tdd;
         std::vector<uint32_t> r0v, rg0, rkey;
         const uint64_t tmask_t = (uint64_t)pl.threads - 1;
@@ -740,8 +740,7 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
             // threads == 1 << kC64ThreadBits whenever lo has register bits
             const uint32_t lt = (uint32_t)(sg.lo & tmask_t), lm = sg.lo >> pl.tb;
             const uint32_t dx = (lt << 3) | (lm << (pl.tb + 3));
-            td.push_back(make_uint2(dx | (half[i] << 15) | (tvar << 31),
-                                    zt | (bt0 << 10) | (bt1 << 20)));
+            td.push_back(make_uint4(dx | (half[i] << 15) | (tvar << 31), zt, bt0, bt1));
             TileDataC64 d;
             memset(&d, 0, sizeof(d));
             d.z0h = sg.z0 >> pl.b;
@@ -779,13 +778,22 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         ch.push_back(make_uint4((uint32_t)ord.size(), (uint32_t)rkey.size(), pl.nblocks, 0));
         QR_CUDA(pl.chunks.upload(ch), "upload chunks");
         if (td.empty()) {
-            td.push_back(make_uint2(0, 0));
+            td.push_back(make_uint4(0, 0, 0, 0));
             TileDataC64 z;
             memset(&z, 0, sizeof(z));
             tdd.push_back(z);
         }
         QR_CUDA(pl.tdesc.upload(td), "upload thread descriptors");
         QR_CUDA(pl.tdata.upload(tdd), "upload tile data");
+        // pair plans: bit 31 of a pair's first run marks a pair of exactly two
+        // sub-groups with key 0 (no sign pattern, no register-bit XOR, factor
+        // constant over the threads), which the kernel runs without the run
+        // list
+        if (pl.npairs) {
+            for (uint32_t j = 0; j < pl.npairs; ++j)
+                if (pg0[j + 1] - pg0[j] == 2 && pkey[pg0[j]] == 0 && pkey[pg0[j] + 1] == 0)
+                    r0v[j] |= 0x80000000u;
+        }
         QR_CUDA(pl.blk_r0.upload(r0v), "upload block runs");
         QR_CUDA(pl.run_g0.upload(rg0), "upload runs");
         QR_CUDA(pl.run_key.upload(rkey), "upload run keys");
@@ -1112,7 +1120,7 @@ static int apply_impl(const char *name, qr_op *op, int32_t dtype, const void *ps
     a.err = op->d_err.as<int>();
     a.sub = pl.sub.as<SubDescC64>();
     a.nsub = pl.nsub;
-    a.tdesc = pl.tdesc.as<uint2>();
+    a.tdesc = pl.tdesc.as<uint4>();
     a.tdata = pl.tdata.as<TileDataC64>();
     a.blk_r0 = pl.blk_r0.as<uint32_t>();
     a.run_g0 = pl.run_g0.as<uint32_t>();
