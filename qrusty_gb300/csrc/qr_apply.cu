@@ -118,6 +118,19 @@ __device__ __forceinline__ void two_sum_into(float &hi, float &lo, float b) {
     hi = s;
     lo = __fadd_rn(lo, e);
 }
+// The same error-free transformation on (re, im) at once with packed FP32
+// operations; x - y is formed as fma(y, -1, x) (y * -1 is exact, so the one
+// rounding is that of x - y): bit-identical to two_sum_into per component.
+__device__ __forceinline__ float2 sub2_rn(float2 x, float2 y) {
+    return __ffma2_rn(y, make_float2(-1.f, -1.f), x);
+}
+__device__ __forceinline__ void two_sum_into2(float2 &hi, float2 &lo, float2 b) {
+    const float2 s = __fadd2_rn(hi, b);
+    const float2 bb = sub2_rn(s, hi);
+    const float2 e = __fadd2_rn(sub2_rn(hi, sub2_rn(s, bb)), sub2_rn(b, bb));
+    hi = s;
+    lo = __fadd2_rn(lo, e);
+}
 template <typename Real>
 __device__ __forceinline__ Cplx<Real> cneg_if(const Cplx<Real> &d, uint32_t s) {
     Cplx<Real> r;
@@ -900,8 +913,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     float2 *mylo = s_lo + t;
     uint32_t p = 0, s = 0, par = 0;
     // compensated fold every 8 pairs (16 partner tiles): half the fold work
-    // of kFlush for ~10 % more rounding error (2.3e-7 vs 2.0e-7 relative on
-    // the 26-qubit Jordan-Wigner operator)
+    // of kFlush; relative error 2.0e-7 on the 26-qubit Jordan-Wigner operator
     constexpr uint32_t kFlushPairs = 8;
 
     for (uint64_t L = 0; L < total; ++L) {
@@ -925,15 +937,20 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
             }
             __syncthreads();
         }
-        bool skip = *s_abort != 0;
-        if (!skip && !mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
-            if (lane == 0) {
-                atomicExch(a.err, kErrMbarTimeout);
-                *s_abort = 1;
+        // fast path: the stage is complete for the whole warp; otherwise the
+        // bounded wait, which also honours another warp's abort
+        bool skip = false;
+        if (!__all_sync(0xffffffffu, mbar_try_wait(&full[s], par))) {
+            skip = *s_abort != 0;
+            if (!skip && !mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
+                if (lane == 0) {
+                    atomicExch(a.err, kErrMbarTimeout);
+                    *s_abort = 1;
+                }
+                skip = true;
             }
-            skip = true;
+            skip = __any_sync(0xffffffffu, skip);
         }
-        skip = __any_sync(0xffffffffu, skip);
         const uint32_t soff = s * slot_bytes;
 
         if (!skip && (int)p == diag_pair && diag != nullptr) {
@@ -971,11 +988,10 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
         if (last || (p % kFlushPairs) == kFlushPairs - 1) {
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
-                const float yr = __fsub_rn(A[m].x, B[m].y);
-                const float yi = __fadd_rn(A[m].y, B[m].x);
+                const float2 yv =
+                    make_float2(__fsub_rn(A[m].x, B[m].y), __fadd_rn(A[m].y, B[m].x));
                 float2 lm = mylo[m * threads];
-                two_sum_into(hi[m].x, lm.x, yr);
-                two_sum_into(hi[m].y, lm.y, yi);
+                two_sum_into2(hi[m], lm, yv);
                 mylo[m * threads] = lm;
                 A[m] = B[m] = make_float2(0.f, 0.f);
             }
