@@ -89,3 +89,33 @@ def terms_of_labels(labels, coeffs):
         ph.append((bp + ny) % 4)
     return (n, np.array(xs, dtype=np.uint64), np.array(zs, dtype=np.uint64),
             np.array(ph, dtype=np.uint8), np.asarray(coeffs, dtype=np.complex128))
+
+
+# Pure-Python restatement of the rowwise path, independent of the C oracle.
+_UNIT_PHASE = [complex(1.0, 0.0), complex(0.0, -1.0), complex(-1.0, 0.0), complex(0.0, 1.0)]
+
+
+def make_params_py(phase, coeffs):
+    """qrusty/src/accel.rs:141-157: c'_k = m(phase_k) * c_k, m = 1, -i, -1, i,
+    with num-complex's product (ac - bd, ad + bc); CPython's complex product
+    is the same formula, and every factor of m is 0 or +-1, so each product
+    is exact."""
+    return [_UNIT_PHASE[int(p) % 4] * complex(c) for p, c in zip(phase, coeffs)]
+
+
+def make_row_py(x, z, cprime, r):
+    """qrusty/src/accel.rs:171-210 for row r: (r ^ x_k, +-c'_k) per term, the
+    sign flipped (both parts) when popcount(r & z_k) is odd, a stable sort by
+    column, then a left fold that merges equal columns by adding in term
+    order starting from the first value (explicit zeros kept)."""
+    v = [(r ^ xk, -ck if bin(r & zk).count("1") & 1 else ck)
+         for xk, zk, ck in zip(x, z, cprime)]
+    v.sort(key=lambda e: e[0])
+    cols, vals = [], []
+    for col, val in v:
+        if cols and cols[-1] == col:
+            vals[-1] = vals[-1] + val
+        else:
+            cols.append(col)
+            vals.append(val)
+    return cols, vals

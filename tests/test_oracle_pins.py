@@ -13,7 +13,9 @@ re-running the reference's known-answer tests against it:
   * axpby / axpy / ax known answers pyqrusty/tests/test_it.py:232-276
   * precond / precond2 on H2       pyqrusty/tests/test_it.py:278-313 (the
                                   reference's printed rv, tests/golden/precond.npz)
-plus structural invariants of make_row's output (accel.rs:171-210).
+plus structural invariants of make_row's output (accel.rs:171-210), and
+sampled rows of the larger fixtures H8 / HJ against a pure-Python
+restatement of make_params / make_row (tests/helpers.py), bit for bit.
 """
 import os
 
@@ -21,7 +23,8 @@ import numpy as np
 import pytest
 import scipy.sparse as sps
 
-from tests.helpers import csr_to_dense, kron_dense, rowwise_dense, terms_of_labels
+from tests.helpers import (csr_to_dense, kron_dense, make_params_py, make_row_py,
+                           rowwise_dense, terms_of_labels)
 
 I2 = np.array([[1, 0], [0, 1]], dtype=complex)
 X2 = np.array([[0, 1], [1, 0]], dtype=complex)
@@ -116,6 +119,32 @@ def test_row_structure(oracle, golden, name):
     ux = np.unique(x)
     for r in (0, 1, N // 3, N - 1):
         assert np.array_equal(np.sort(np.uint64(r) ^ ux), rows[r])
+
+
+@pytest.mark.parametrize("name,ranges", [
+    ("H8", [(0, 48), (40000, 40032), (65520, 65536)]),
+    ("HJ", [(0, 32), (1 << 26, (1 << 26) + 32), ((1 << 27) - 32, 1 << 27)]),
+])
+def test_large_fixture_rows_bit_exact(oracle, golden, name, ranges):
+    """H8 (16 qubits, 5,793 terms) and HJ (27 qubits) from H_fixtures.py are
+    too large for a dense Kronecker check: sampled row ranges of the oracle's
+    chunked build must equal, bit for bit (signed zeros included), a
+    pure-Python restatement of make_params and make_row."""
+    labels, coeffs = golden[name]
+    n, x, z, ph, c = terms_of_labels(labels, coeffs)
+    cp = oracle.make_params(ph, c)
+    cpy = np.array(make_params_py(ph, c), dtype=np.complex128)
+    assert np.array_equal(cp.view(np.uint64), cpy.view(np.uint64))
+    xl, zl, cl = x.tolist(), z.tolist(), list(cpy)
+    for lo, hi in ranges:
+        ip, ij, d = oracle.csr_build(n, x, z, cp, step=16, nthreads=2, rows=(lo, hi))
+        assert len(ip) == hi - lo + 1
+        for k, r in enumerate(range(lo, hi)):
+            cols, vals = make_row_py(xl, zl, cl, r)
+            a, b = int(ip[k] - ip[0]), int(ip[k + 1] - ip[0])
+            assert ij[a:b].tolist() == cols
+            want = np.array(vals, dtype=np.complex128)
+            assert np.array_equal(d[a:b].view(np.uint64), want.view(np.uint64))
 
 
 def test_explicit_zeros_kept(oracle):
