@@ -20,6 +20,11 @@ Arms:
 Multi-GPU (torchrun, N > 1): replicas -- every rank applies the operator to
 its own state (weak scaling, no data-path collective); max time over ranks.
 
+The default line also carries, under "secondary", compact measurements of
+the other configurations (each on its own CUDA-event clock, each checked
+against the FP64 oracle): chain, grad, batch, csr and spmv below
+(--no-secondary leaves them out).
+
 Secondary workloads (--workload, one JSON line each, 1 GPU):
   chain   the 22-qubit TFIM+XXZ chain (85 terms), same metric.
   batch   256 uneven operators (n 10-20, 50-5,000 terms) x 8 complex64 states
@@ -95,15 +100,57 @@ def peaks():
         return 6800.0, "fallback"
 
 
+_FP64 = {}
+
+
+def fp64_peak():
+    """Measured FP64 FMA rate of this GPU (TFLOP/s, 2 flops per DFMA) from
+    libqrusty_probe.so's chain kernel, or None when the probe is unavailable."""
+    if "v" not in _FP64:
+        _FP64["v"] = None
+        try:
+            import ctypes as C
+            from qrusty_gb300 import build as B
+            L = C.CDLL(B.PROBE)
+            L.qr_probe_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_float)]
+            L.qr_probe_fp64_peak.restype = C.c_int
+            best = 0.0
+            for _ in range(3):
+                tf, ms = C.c_double(), C.c_float()
+                if L.qr_probe_fp64_peak(20000, C.byref(tf), C.byref(ms)) == 0:
+                    best = max(best, tf.value)
+            _FP64["v"] = best or None
+        except Exception as e:  # reported as absent, never guessed
+            log("fp64 probe unavailable: %s" % e)
+    return _FP64["v"]
+
+
+# Sources whose change invalidates a recorded DRAM-traffic figure: the apply
+# kernels, their shared types and the plan builder.
+TRAFFIC_SOURCES = ("qrusty_gb300/csrc/qr_apply.cu", "qrusty_gb300/csrc/qr_common.cuh",
+                   "qrusty_gb300/csrc/qr_host.cu")
+
+
+def source_hash() -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for rel in TRAFFIC_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
 def ncu_traffic():
     """DRAM bytes per launch of the c64c apply kernel from the committed ncu
-    summary (profiles/ncu_traffic.json), scaled to the bench workload."""
+    summary (profiles/ncu_traffic.json).  Used only when it was captured from
+    the same kernel sources as this run (source hash), else None."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f)
+            d = json.load(f)
     except Exception:
         return None
+    return d if d.get("source_sha256_16") == source_hash() else None
 
 
 class ClockSampler:
@@ -199,6 +246,25 @@ def cpu_reference(t, rows, reps, nthreads):
     return t_build, times
 
 
+def cpu_sample_text(rows, n, t_build, ms_spmv, nthreads):
+    """What the CPU figure is: qrusty's method on a row sample, CSR*vector
+    timed with the CSR already built; the build is excluded although one
+    H psi from scratch costs build + CSR*vector."""
+    full = t_build * (1 << n) / rows
+    return ("rows [0, %d) of 2^%d on %d thread(s): CSR*vector %.2f ms per step, CSR prebuilt "
+            "(the most favourable reading for the CPU); the sample's CSR build (make_row, "
+            "1024-row chunks) took %.2f s and is excluded -- %.0f s extrapolated to all rows"
+            % (rows, n, nthreads, ms_spmv, t_build, full))
+
+
+def cpu_one_thread(t, rows):
+    """The same method on one host thread (a smaller row sample)."""
+    t_build, times = cpu_reference(t, rows, 3, 1)
+    ms = 1e3 * statistics.median(times)
+    return {"value": t.T * rows / (ms / 1e3), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": cpu_sample_text(rows, t.n, t_build, ms, 1)}
+
+
 def run_reference_arm(args, t, desc):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -210,8 +276,7 @@ def run_reference_arm(args, t, desc):
     ms = 1e3 * statistics.mean(timed)
     units = t.T * rows
     value = units / (ms / 1e3)
-    sample = ("rows [0, %d) of 2^%d: CSR build %.2f s (make_row, chunks of 1024), then one "
-              "CSR*vector per step; value = sample term*amp / SpMV time" % (rows, t.n, t_build))
+    sample = cpu_sample_text(rows, t.n, t_build, ms, nthreads)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -222,6 +287,7 @@ def run_reference_arm(args, t, desc):
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "csr_build_s": t_build,
+        "cpu_baseline_1thread": cpu_one_thread(t, max(1024, rows // 8)),
     }
     print(json.dumps(out), flush=True)
 
@@ -295,10 +361,14 @@ def run_gpu_arm(args, t, desc):
     op.sync_check()
     ms128 = tot128 / s128
 
-    # --- accuracy at full size: c64c against c128 (checked against the FP64
-    # oracle on sampled rows in the test suite)
+    # --- accuracy at full size (outside the timed region): c64c against c128
+    # over the whole state, and both against the FP64 oracle on a block of
+    # 65,536 rows (16 output tiles, unaligned start)
     rel64 = float(torch.linalg.vector_norm(y64.to(torch.complex128) - y128)
                   / torch.linalg.vector_norm(y128))
+    rel_rows = None
+    if rank == 0 and not args.quick and not args.no_cpu:
+        rel_rows = oracle_rows_errors(t, psi128, psi64, y128, y64)
 
     # --- end to end through the C-ABI host entry (pinned host buffers)
     e2e = None
@@ -337,6 +407,9 @@ def run_gpu_arm(args, t, desc):
     traffic = None
     if tr and tr.get("workload") == desc:
         traffic = tr.get("bytes_per_launch")
+    rel_err = {"c64c_vs_c128_full": rel64}
+    if rel_rows:
+        rel_err.update(rel_rows)
     out = {
         "metric": METRIC, "value": whole_job_rate(ws, T * N, ms64 / 1e3), "unit": UNIT,
         "n_gpus": ws,
@@ -356,16 +429,9 @@ def run_gpu_arm(args, t, desc):
                      "b_group_bytes": (int(info["ngroups"]) + 1) * N * 8,
                      "b_group_rule": "(G+1)*2^n*8: one gather pass per distinct x mask",
                      "peak_source": peak_kind},
-        "c128": {"value": whole_job_rate(ws, T * N, ms128 / 1e3), "ms_per_step": ms128,
-                 "steps": s128,
-                 # 4 DFMA (8 flops) per amplitude and x group; GB300 FP64 is
-                 # 1.25 TFLOP/s nominal (no measured FP64 peak is recorded)
-                 "fp64_tflops": 8.0 * N * int(info["ngroups"]) / (ms128 / 1e3) / 1e12,
-                 "fp64_frac_of_nominal": 8.0 * N * int(info["ngroups"]) / (ms128 / 1e3)
-                                         / 1.25e12,
-                 "hbm_achieved_gbs": ach128, "hbm_frac": ach128 / hbm},
+        "c128": c128_line(ws, T, N, int(info["ngroups"]), ms128, s128, ach128, hbm, alg128),
         "speedup_c64c_vs_c128": ms128 / ms64,
-        "rel_err": {"c64c_vs_c128_full": rel64},
+        "rel_err": rel_err,
         "e2e": e2e,
         "clocks": clk,
         "gpu_launches": int(launches),
@@ -378,12 +444,54 @@ def run_gpu_arm(args, t, desc):
         cpu_val = T * args.cpu_rows / (ms_cpu / 1e3)
         out["cpu_baseline"] = {
             "value": cpu_val, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": ("rows [0, %d) of 2^%d; CSR build %.2f s, CSR*vector %.1f ms (median of 3)"
-                       % (args.cpu_rows, n, t_build, ms_cpu))}
+            "sample": cpu_sample_text(args.cpu_rows, n, t_build, ms_cpu, nthreads)}
+        out["cpu_baseline_1thread"] = cpu_one_thread(t, max(1024, args.cpu_rows // 8))
+    del y64, y128, psi64, psi128
+    if not args.quick and not args.no_secondary and ws == 1:
+        out["secondary"] = run_secondary(args)
     print(json.dumps(out), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def c128_line(ws, T, N, G, ms128, steps, ach128, hbm, alg128):
+    """The plain complex128 kernel: 4 DFMA (8 flops) per amplitude and x
+    group, so GB300's FP64 rate bounds it long before HBM does; the fraction
+    is against the FP64 rate measured on this GPU by the probe kernel."""
+    flops = 8.0 * N * G
+    tf = flops / (ms128 / 1e3) / 1e12
+    peak = fp64_peak()
+    d = {"value": whole_job_rate(ws, T * N, ms128 / 1e3), "ms_per_step": ms128, "steps": steps,
+         "fp64_tflops": tf, "fp64_peak_measured_tflops": peak,
+         "fp64_frac_of_measured": (tf / peak) if peak else None,
+         "fp64_floor_ms": (flops / (peak * 1e12) * 1e3) if peak else None,
+         "hbm_floor_ms": alg128 / (hbm * 1e9) * 1e3,
+         "hbm_achieved_gbs": ach128, "hbm_frac": ach128 / hbm,
+         "note": "FP64-bound: >= 70% of HBM is out of reach for native FP64 on GB300"}
+    return d
+
+
+def oracle_rows_errors(t, psi128, psi64, y128, y64, rows=65536):
+    """Relative errors of both kernels against the FP64 oracle on one block of
+    rows: c128 and c64c on their own inputs, and c64c against the oracle on
+    the FP64 state before its rounding to complex64."""
+    from oracle import oracle as O
+    O.build()
+    N = 1 << t.n
+    lo = ((0x2A5B << 12) + 777) % max(1, N - rows) if N > rows else 0
+    hi = min(N, lo + rows)
+    cp = O.make_params(t.phase, t.coeff)
+    p128 = psi128.cpu().numpy()
+    p64 = psi64.cpu().numpy().astype(np.complex128)
+    r128 = O.apply_rows(t.x, t.z, cp, p128, lo, hi)
+    r64 = O.apply_rows(t.x, t.z, cp, p64, lo, hi)
+    a = y128[lo:hi].cpu().numpy()
+    b = y64[lo:hi].cpu().numpy().astype(np.complex128)
+    e = lambda u, v: float(np.linalg.norm(u - v) / np.linalg.norm(v))
+    return {"c128_vs_oracle_rows": e(a, r128), "c64c_vs_oracle_rows": e(b, r64),
+            "c64c_vs_oracle_rows_fp64_input": e(b, r128),
+            "oracle_rows": "[%d, %d) of 2^%d" % (lo, hi, t.n)}
 
 
 # ----------------------------------------------------------------------------- secondary
@@ -410,8 +518,74 @@ def _base_line(args, metric, value, unit, ms, dtype, config, **kw):
     return out
 
 
-def run_batch(args):
+def _roof(alg_bytes, ms, hbm, peak_kind, rule, note=None):
+    ach = alg_bytes / (ms / 1e3) / 1e9
+    d = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+         "traffic": None, "alg_bytes_per_launch": alg_bytes, "alg_bytes_rule": rule,
+         "peak_source": peak_kind}
+    if note:
+        d["note"] = note
+    return d
+
+
+def _randn_state(n_amp, dev, seed, dtype):
     import torch
+    g = torch.Generator(device=dev).manual_seed(seed)
+    p = torch.complex(torch.randn(n_amp, device=dev, dtype=torch.float64, generator=g),
+                      torch.randn(n_amp, device=dev, dtype=torch.float64, generator=g))
+    return (p / torch.linalg.vector_norm(p)).to(dtype)
+
+
+def measure_chain(steps=3, warmup=3, matvecs=100, n=22):
+    """The TFIM+XXZ open chain, n = 22 (85 terms, G = 44): a step is 100
+    repeated matvecs y = H psi (the reference's driver shape: CSR built once,
+    then repeated CSR*vector), complex64-compensated and complex128.  The
+    state (32 / 64 MiB) sits in L2, so the HBM fraction is nominal."""
+    import torch
+    from oracle import oracle as O
+    from qrusty_gb300 import PauliOperator, _lib
+    from qrusty_gb300 import workloads as W
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    t, _ = W.cfg1(with_state=False, n=n)
+    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
+    N = 1 << n
+    P = W.alg_blocks(t, 13)
+    hbm, peak_kind = peaks()
+    psi = _randn_state(N, dev, 21, torch.complex128)
+    O.build()
+    ref = O.apply(n, t.x, t.z, O.make_params(t.phase, t.coeff), psi.cpu().numpy())
+    out = {"workload": "tfim+xxz open chain n=%d, %d terms, %d matvecs per step (seed %d)"
+                       % (n, t.T, matvecs, W.SEED0 + 1)}
+    for name, dt, esz in (("c64c", torch.complex64, 8), ("c128", torch.complex128, 16)):
+        x = psi.to(dt)
+        y = torch.empty_like(x)
+
+        def step():
+            for _ in range(matvecs):
+                op.apply(x, out=y)
+        l0 = _lib.launch_count()
+        ms = _events_time(step, steps, warmup, stream)
+        launches = (_lib.launch_count() - l0) / (steps + warmup)
+        op.sync_check()
+        yh = y.cpu().numpy().astype(np.complex128)
+        mv = ms / matvecs
+        out[name] = {
+            "ms_per_step": ms, "ms_per_matvec": mv, "value": t.T * N * matvecs / (ms / 1e3),
+            "unit": UNIT, "gpu_launches_per_step": launches,
+            "roofline": _roof((P + 1) * N * esz, mv, hbm, peak_kind,
+                              "(P+1)*2^n*%d per matvec, P=%d" % (esz, P),
+                              "state L2-resident: nominal"),
+            "rel_err_vs_oracle": float(np.linalg.norm(yh - ref) / np.linalg.norm(ref))}
+    return out
+
+
+def measure_batch(steps=3, warmup=3, per_op=True):
+    """256 uneven operators (n ~ U{10..20}, T ~ U{50..5000}) x 8 complex64
+    states behind one graph launch per step; a dozen operators (every qubit
+    count) against the FP64 oracle on row blocks of every state."""
+    import torch
+    from oracle import oracle as O
     from qrusty_gb300 import Batch, PauliOperator, _lib
     from qrusty_gb300 import workloads as W
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -422,14 +596,12 @@ def run_batch(args):
     ops = [PauliOperator(t.n, t.x, t.z, t.phase, t.coeff) for t in terms]
     t_create = time.perf_counter() - t0
     g = torch.Generator(device=dev).manual_seed(7)
-    psis, ys, psis128, ys128 = [], [], [], []
+    psis, ys = [], []
     for t in terms:
         p = torch.complex(torch.randn(ns << t.n, device=dev, generator=g),
                           torch.randn(ns << t.n, device=dev, generator=g))
         psis.append(p)
         ys.append(torch.empty_like(p))
-        psis128.append(p.to(torch.complex128))
-        ys128.append(torch.empty_like(psis128[-1]))
     units = sum(t.T * (ns << t.n) for t in terms)
     alg = sum((W.alg_blocks(t, 13) + 1) * (ns << t.n) * 8 for t in terms)
     t0 = time.perf_counter()
@@ -438,54 +610,62 @@ def run_batch(args):
     torch.cuda.synchronize()
     t_tune = time.perf_counter() - t0
     l0 = _lib.launch_count()
-    ms_b = _events_time(lambda: b.apply(psis, ys), args.steps, args.warmup, stream)
-    launches = (_lib.launch_count() - l0) / (args.steps + args.warmup)
-
-    def per_op(ps, outs):
-        for op, p, y in zip(ops, ps, outs):
-            op.apply(p, out=y)
-    s2 = max(3, args.steps // 5)
-    ms_128 = _events_time(lambda: per_op(psis128, ys128), s2, 3, stream)
-    ms_64 = _events_time(lambda: per_op(psis, ys), s2, 3, stream)
-    # accuracy: batched c64c against per-operator c128 on the same states
-    b.apply(psis, ys)
-    per_op(psis128, ys128)
+    ms_b = _events_time(lambda: b.apply(psis, ys), steps, warmup, stream)
+    launches = (_lib.launch_count() - l0) / (steps + warmup)
     torch.cuda.synchronize()
-    worst = max(float(torch.linalg.vector_norm(y.to(torch.complex128) - r)
-                      / torch.linalg.vector_norm(r)) for y, r in zip(ys, ys128))
+    # oracle on row blocks of every state of one operator per qubit count
+    O.build()
+    by_n = {}
+    for i, t in enumerate(terms):
+        by_n.setdefault(t.n, []).append(i)
+    pick = [max(v, key=lambda i: terms[i].T) for _, v in sorted(by_n.items())]
+    rng = np.random.default_rng(0)
+    worst = 0.0
+    for i in pick:
+        t = terms[i]
+        N = 1 << t.n
+        cp = O.make_params(t.phase, t.coeff)
+        Pm = psis[i].cpu().numpy().reshape(ns, N).astype(np.complex128)
+        Ym = ys[i].cpu().numpy().reshape(ns, N).astype(np.complex128)
+        for s_ in range(ns):
+            lo = 0 if N <= 8192 else int(rng.integers(0, N - 4096))
+            hi = N if N <= 8192 else lo + 4096
+            r = O.apply_rows(t.x, t.z, cp, Pm[s_], lo, hi)
+            worst = max(worst, float(np.linalg.norm(Ym[s_, lo:hi] - r) / np.linalg.norm(r)))
     hbm, peak_kind = peaks()
-    ach = alg / (ms_b / 1e3) / 1e9
-    out = _base_line(
-        args, "batched Pauli-sum H·ψ term·amp/s (sum over operators and states)",
-        units / (ms_b / 1e3), UNIT, ms_b, "c64c (fp32 + two-sum)",
-        {"workload": "256 operators, n ~ U{10..20}, T ~ U{50..5000} random letters (seed %d), "
-                     "8 complex64 states each" % (W.SEED0 + 3),
-         "operators": len(terms), "states_per_op": ns,
-         "amplitudes_total": int(sum(ns << t.n for t in terms)),
-         "tile_bits_autotuned": b.tile_bits,
-         "l2": "total state %d MiB; no flush" % (sum((ns << t.n) * 8 for t in terms) >> 20)},
-        roofline={"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-                  "frac": ach / hbm, "traffic": None, "alg_bytes_per_launch": alg,
-                  "alg_bytes_rule": "sum over ops of (P+1)*states*2^n*8", "peak_source": peak_kind},
-        per_op_c128={"ms_per_step": ms_128, "launches_per_step": len(ops),
-                     "value": units / (ms_128 / 1e3)},
-        per_op_c64c={"ms_per_step": ms_64, "value": units / (ms_64 / 1e3)},
-        speedup_vs_per_op_c128=ms_128 / ms_b,
-        rel_err={"batched_c64c_vs_c128_worst_op": worst},
-        setup_s={"create_ops": t_create, "autotune_and_capture": t_tune},
-        gpu_launches=launches)
-    print(json.dumps(out), flush=True)
+    out = {"workload": "256 operators, n ~ U{10..20}, T ~ U{50..5000} random letters (seed %d), "
+                       "8 complex64 states each" % (W.SEED0 + 3),
+           "ms_per_step": ms_b, "value": units / (ms_b / 1e3), "unit": UNIT,
+           "mode": "persistent work-list kernel" if b.mode == 0 else "graph of per-operator kernels",
+           "tile_bits": b.tile_bits, "gpu_launches_per_step": launches,
+           "roofline": _roof(alg, ms_b, hbm, peak_kind,
+                             "sum over ops of (P+1)*states*2^n*8"),
+           "rel_err_vs_oracle": {"worst": worst, "operators": len(pick),
+                                 "rows": "4096-row block (all rows for 2^n <= 8192), every state"},
+           "setup_s": {"create_ops": t_create, "autotune_and_capture": t_tune}}
+    if per_op:
+        def per_op_apply():
+            for op, p, y in zip(ops, psis, ys):
+                op.apply(p, out=y)
+        ms_64 = _events_time(per_op_apply, 2, 1, stream)
+        out["per_op_c64c_ms"] = ms_64
+        out["speedup_vs_per_op_c64c"] = ms_64 / ms_b
+    return out, (ops, psis, ys, terms, b)
 
 
-def run_grad(args):
+def measure_grad(steps=10, warmup=3):
+    """y = H(c) psi, L = Re<y, w> (n = 20, 2,000 terms, complex64 psi): one
+    training step = forward, backward to c and psi, SGD update of c."""
     import torch
+    from oracle import oracle as O
+    from qrusty_gb300 import _lib
     from qrusty_gb300 import workloads as W
     from qrusty_gb300.autograd import PauliTerms, pauli_apply
     dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.current_stream(dev)
     t, psi, w = W.cfg4()
     terms = PauliTerms(t.n, t.x, t.z, t.phase)
-    c = torch.tensor(t.coeff.real, dtype=torch.float64, requires_grad=True)
+    c = torch.tensor(t.coeff.real, dtype=torch.float64, device=dev, requires_grad=True)
     p = torch.from_numpy(psi.astype(np.complex64)).to(dev).requires_grad_(True)
     wd = torch.from_numpy(w.astype(np.complex64)).to(dev)
 
@@ -495,35 +675,166 @@ def run_grad(args):
         y = pauli_apply(c, p, terms)
         torch.vdot(y, wd).real.backward()
         with torch.no_grad():
-            c.add_(c.grad, alpha=-1e-3)  # an SGD update: the next step sees new coefficients
+            c.add_(c.grad, alpha=-1e-3)  # SGD: the next step sees new coefficients
 
-    ms = _events_time(step, args.steps, args.warmup, stream)
-    N = 1 << t.n
-    # where a step goes: coefficient update (plans rebuilt), forward, adjoint,
-    # per-term inner products
-    cc = t.coeff.real.astype(np.complex128)
-    reps = 5
+    l0 = _lib.launch_count()
+    ms = _events_time(step, steps, warmup, stream)
+    launches = (_lib.launch_count() - l0) / (steps + warmup)
+    # gradients at the current coefficients against the FP64 oracle
+    c.grad = None
+    p.grad = None
+    y = pauli_apply(c, p, terms)
+    torch.vdot(y, wd).real.backward()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(reps):
-        cc[0] += 1e-6
-        op = terms.operator(cc)
-        op.apply(p.detach(), out=torch.empty_like(p))  # plans are rebuilt lazily on first use
-        torch.cuda.synchronize()
-    ms_update_fwd = 1e3 * (time.perf_counter() - t0) / reps
-    pd, gd = p.detach(), wd
-    ms_fwd = _events_time(lambda: op.apply(pd), 10, 3, stream)
-    ms_adj = _events_time(lambda: op.apply(gd, adjoint=True), 10, 3, stream)
-    ms_tg = _events_time(lambda: op.term_grad(pd, gd), 10, 3, stream)
-    out = _base_line(
-        args, "differentiable H(c)·ψ training step term·amp/s (forward terms x amplitudes / step)",
-        t.T * N / (ms / 1e3), UNIT, ms, "c64c forward / adjoint, fp64 reductions",
-        {"workload": "n=%d, %d random-letter terms, real c, complex64 psi, L = Re<H(c)psi, w> "
-                     "(seed %d)" % (t.n, t.T, W.SEED0 + 4),
-         "step": "forward + backward (grad_c, grad_psi) + SGD update of c",
-         "l2": "state 8 MiB: L2-resident"},
-        breakdown_ms={"coeff_update_and_forward_incl_plan_rebuild": ms_update_fwd,
-                      "forward_apply": ms_fwd, "adjoint_apply": ms_adj, "term_grad": ms_tg})
+    O.build()
+    ch = c.detach().cpu().numpy().astype(np.complex128)
+    ph = p.detach().cpu().numpy().astype(np.complex128)
+    wh = wd.cpu().numpy().astype(np.complex128)
+    tg = O.term_grad(t.n, t.x, t.z, t.phase, ph, wh).real
+    gc = c.grad.cpu().numpy()
+    cp = O.make_params(t.phase, ch)
+    yref = O.apply(t.n, t.x, t.z, cp, ph)
+    yh = y.detach().cpu().numpy().astype(np.complex128)
+    N = 1 << t.n
+    return {"workload": "n=%d, %d random-letter terms, real c, complex64 psi, L = Re<H(c)psi, w> "
+                        "(seed %d)" % (t.n, t.T, W.SEED0 + 4),
+            "step": "forward + backward (grad_c, grad_psi) + SGD update of c",
+            "ms_per_step": ms, "value": t.T * N / (ms / 1e3), "unit": UNIT,
+            "gpu_launches_per_step": launches,
+            "rel_err_vs_oracle": {
+                "forward_y": float(np.linalg.norm(yh - yref) / np.linalg.norm(yref)),
+                "grad_c": float(np.linalg.norm(gc - tg) / np.linalg.norm(tg))}}
+
+
+def measure_csr(steps=5, warmup=3, n=22):
+    """Device CSR build (indptr, indices, data) of the chain at n = 22 and
+    CSR*vector on it; 64 rows of the build against make_row bit for bit and
+    the CSR*vector against the oracle's on a row sample."""
+    import torch
+    from oracle import oracle as O
+    from qrusty_gb300 import PauliOperator, _lib
+    from qrusty_gb300 import workloads as W
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    t, _ = W.cfg1(with_state=False, n=n)
+    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
+    nr, nz = op.csr_size()
+    G = nz // nr
+    indptr = torch.empty(nr + 1, dtype=torch.int64, device=dev)
+    indices = torch.empty(nz, dtype=torch.int64, device=dev)
+    data = torch.empty(nz, dtype=torch.complex128, device=dev)
+    L = _lib.load()
+    st = stream.cuda_stream
+    fn = lambda: _lib.check(L.qr_csr_build(op.handle, indptr.data_ptr(), indices.data_ptr(),
+                                           data.data_ptr(), _lib.QR_MEM_DEVICE, st))
+    l0 = _lib.launch_count()
+    ms = _events_time(fn, steps, warmup, stream)
+    launches = (_lib.launch_count() - l0) / (steps + warmup)
+    op.sync_check()
+    hbm, peak_kind = peaks()
+    written = 8 * (nr + 1) + 24 * nz
+    O.build()
+    cp = O.make_params(t.phase, t.coeff)
+    rng = np.random.default_rng(7)
+    rows = np.unique(np.concatenate([[0, nr - 1], rng.integers(0, nr, 62)])).astype(np.int64)
+    rd = torch.from_numpy(rows).to(dev)
+    pos = (rd[:, None] * G + torch.arange(G, device=dev)[None, :]).reshape(-1)
+    cols = indices[pos].cpu().numpy().view(np.uint64).reshape(len(rows), G)
+    vals = data[pos].cpu().numpy().reshape(len(rows), G)
+    exact = 0
+    for k, r in enumerate(rows.tolist()):
+        oc, ov = O.make_row(t.x, t.z, cp, r)
+        exact += int(np.array_equal(cols[k], oc)
+                     and np.array_equal(vals[k].view(np.uint64), ov.view(np.uint64)))
+    csr = {"workload": "tfim+xxz open chain n=%d, %d terms, G=%d, %d stored entries (seed %d)"
+                       % (n, t.T, G, nz, W.SEED0 + 1),
+           "ms_per_step": ms, "value": nz / (ms / 1e3), "unit": "nnz/s",
+           "gpu_launches_per_step": launches,
+           "roofline": _roof(written, ms, hbm, peak_kind, "8(N+1) + 24 nnz written"),
+           "rows_bit_exact_vs_make_row": "%d/%d" % (exact, len(rows))}
+    # CSR * vector on the matrix just built
+    v = _randn_state(nr, dev, 3, torch.complex128)
+    y = torch.empty_like(v)
+    fs = lambda: L.qr_csr_spmv(nr, nr, indptr.data_ptr(), indices.data_ptr(), data.data_ptr(),
+                               v.data_ptr(), y.data_ptr(), st)
+    l0 = _lib.launch_count()
+    ms_s = _events_time(fs, steps, warmup, stream)
+    launches_s = (_lib.launch_count() - l0) / (steps + warmup)
+    torch.cuda.synchronize()
+    srows = 1 << 16
+    ipc, ijc, dc = O.csr_build(n, t.x, t.z, cp, rows=(0, srows))
+    ys = O.spmv(ipc, ijc, dc, v.cpu().numpy())
+    yg = y[:srows].cpu().numpy()
+    alg = 24 * nz + 8 * (nr + 1) + 16 * nr
+    spmv = {"workload": csr["workload"] + ", CSR built on the device",
+            "ms_per_step": ms_s, "value": nz / (ms_s / 1e3), "unit": "nnz/s",
+            "gpu_launches_per_step": launches_s,
+            "roofline": _roof(alg, ms_s, hbm, peak_kind, "24 nnz + 8 (N+1) + 16 N",
+                              "FP64-bound on GB300 (4 DFMA per stored entry)"),
+            "fp64_tflops": 8.0 * nz / (ms_s / 1e3) / 1e12,
+            "fp64_frac_of_measured": (8.0 * nz / (ms_s / 1e3) / 1e12 / fp64_peak())
+                                     if fp64_peak() else None,
+            "rel_err_vs_oracle_rows": float(np.linalg.norm(yg - ys) / np.linalg.norm(ys)),
+            "oracle_rows": "[0, %d)" % srows}
+    return csr, spmv
+
+
+def run_secondary(args):
+    """Compact lines of the other configurations, each on its own clock (CUDA
+    events on the launching stream), for the default bench line."""
+    out = {}
+    for name, fn in (("chain", lambda: measure_chain()),
+                     ("grad", lambda: measure_grad()),
+                     ("batch", lambda: measure_batch(per_op=True)[0]),
+                     ("csr_spmv", lambda: measure_csr())):
+        t0 = time.perf_counter()
+        try:
+            r = fn()
+        except Exception as e:  # reported, never silently dropped
+            r = {"error": "%s: %s" % (type(e).__name__, e)}
+        if name == "csr_spmv" and isinstance(r, tuple):
+            out["csr"], out["spmv"] = r
+        else:
+            out[name] = r
+        log("secondary %s: %.1f s" % (name, time.perf_counter() - t0))
+        import torch
+        torch.cuda.empty_cache()
+    return out
+
+
+def run_batch(args):
+    r, (ops, psis, ys, terms, b) = measure_batch(args.steps, args.warmup, per_op=True)
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    # one complex128 launch per operator on the same states
+    p128 = [p.to(torch.complex128) for p in psis]
+    y128 = [torch.empty_like(p) for p in p128]
+
+    def per_op():
+        for op, p, y in zip(ops, p128, y128):
+            op.apply(p, out=y)
+    ms_128 = _events_time(per_op, 2, 1, stream)
+    out = _base_line(args, "batched Pauli-sum H·ψ term·amp/s (sum over operators and states)",
+                     r["value"], UNIT, r["ms_per_step"], "c64c (fp32 + two-sum)",
+                     {"workload": r["workload"], "tile_bits_autotuned": r["tile_bits"],
+                      "mode": r["mode"]},
+                     roofline=r["roofline"], rel_err=r["rel_err_vs_oracle"],
+                     per_op_c128={"ms_per_step": ms_128, "launches_per_step": len(ops)},
+                     speedup_vs_per_op_c128=ms_128 / r["ms_per_step"],
+                     per_op_c64c_ms=r.get("per_op_c64c_ms"), setup_s=r["setup_s"],
+                     gpu_launches=r["gpu_launches_per_step"])
+    print(json.dumps(out), flush=True)
+
+
+def run_grad(args):
+    r = measure_grad(args.steps, args.warmup)
+    out = _base_line(args, "differentiable H(c)·ψ training step term·amp/s "
+                           "(forward terms x amplitudes / step)",
+                     r["value"], UNIT, r["ms_per_step"], "c64c forward / adjoint, fp64 reductions",
+                     {"workload": r["workload"], "step": r["step"],
+                      "l2": "state 8 MiB: L2-resident"},
+                     rel_err=r["rel_err_vs_oracle"], gpu_launches=r["gpu_launches_per_step"])
     print(json.dumps(out), flush=True)
 
 
@@ -564,116 +875,28 @@ def run_vec(args):
         head["ms"], "c128",
         {"workload": "axpby / axpy / ax / precond2 over 2^%d elements" % args.n,
          "l2": "inputs %d MiB > L2; no flush" % ((N * 16) >> 20)},
-        roofline={"bound": "hbm", "achieved": head["GB/s"], "peak": hbm, "unit": "GB/s",
-                  "frac": head["GB/s"] / hbm, "traffic": None,
-                  "alg_bytes_per_launch": 48 * N, "alg_bytes_rule": "read x, y + write z",
-                  "peak_source": peak_kind},
+        roofline=_roof(48 * N, head["ms"], hbm, peak_kind, "read x, y + write z"),
         all=res)
     print(json.dumps(out), flush=True)
 
 
 def run_csr(args):
-    import torch
-    from qrusty_gb300 import PauliOperator
-    from qrusty_gb300 import workloads as W
-    dev = torch.device("cuda", torch.cuda.current_device())
-    stream = torch.cuda.current_stream(dev)
-    n = args.n if args.n != 26 else 22
-    t, _ = W.cfg1(with_state=False, n=n)
-    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
-    nr, nz = op.csr_size()
-    indptr = torch.empty(nr + 1, dtype=torch.int64, device=dev)
-    indices = torch.empty(nz, dtype=torch.int64, device=dev)
-    data = torch.empty(nz, dtype=torch.complex128, device=dev)
-    from qrusty_gb300 import _lib
-    L = _lib.load()
-    st = stream.cuda_stream
-    fn = lambda: _lib.check(L.qr_csr_build(op.handle, indptr.data_ptr(), indices.data_ptr(),
-                                           data.data_ptr(), _lib.QR_MEM_DEVICE, st))
-    ms = _events_time(fn, args.steps, args.warmup, stream)
-    op.sync_check()
-    written = 8 * (nr + 1) + 24 * nz
-    hbm, peak_kind = peaks()
-    gbs = written / (ms / 1e3) / 1e9
-    out = _base_line(
-        args, "rowwise CSR build nnz/s (indptr, indices, data on the device)",
-        nz / (ms / 1e3), "nnz/s", ms, "u64 indices, c128 data",
-        {"workload": "tfim+xxz open chain n=%d, %d terms, G=%d (seed %d)"
-                     % (n, t.T, nz // nr, W.SEED0 + 1),
-         "nnz": int(nz), "bytes_written": int(written)},
-        roofline={"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
-                  "frac": gbs / hbm, "traffic": None, "alg_bytes_per_launch": written,
-                  "alg_bytes_rule": "8(N+1) + 24 nnz written", "peak_source": peak_kind})
-    if not args.no_cpu:
-        from oracle import oracle as O
-        O.build()
-        rows = min(nr, args.cpu_rows * 4)
-        cp = O.make_params(t.phase, t.coeff)
-        nth = os.cpu_count() or 1
-        t0 = time.perf_counter()
-        O.csr_build(t.n, t.x, t.z, cp, step=1024, nthreads=nth, rows=(0, rows))
-        dt = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": rows * (nz // nr) / dt, "unit": "nnz/s", "cores": nth,
-                               "kind": "port",
-                               "sample": "rows [0, %d) of 2^%d, make_row chunks of 1024" % (rows, n)}
+    csr, _ = measure_csr(args.steps, args.warmup, n=args.n if args.n != 26 else 22)
+    out = _base_line(args, "rowwise CSR build nnz/s (indptr, indices, data on the device)",
+                     csr["value"], "nnz/s", csr["ms_per_step"], "u64 indices, c128 data",
+                     {"workload": csr["workload"]}, roofline=csr["roofline"],
+                     rows_bit_exact_vs_make_row=csr["rows_bit_exact_vs_make_row"],
+                     gpu_launches=csr["gpu_launches_per_step"])
     print(json.dumps(out), flush=True)
 
 
 def run_spmv(args):
-    import torch
-    from qrusty_gb300 import PauliOperator, _lib
-    from qrusty_gb300 import workloads as W
-    dev = torch.device("cuda", torch.cuda.current_device())
-    stream = torch.cuda.current_stream(dev)
-    n = args.n if args.n != 26 else 22
-    t, _ = W.cfg1(with_state=False, n=n)
-    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
-    ip, ij, d = op.csr_device()
-    N = 1 << n
-    g = torch.Generator(device=dev).manual_seed(3)
-    v = torch.randn(N, dtype=torch.complex128, device=dev, generator=g)
-    y = torch.empty_like(v)
-    L = _lib.load()
-    st = stream.cuda_stream
-    fn = lambda: L.qr_csr_spmv(N, N, ip.data_ptr(), ij.data_ptr(), d.data_ptr(), v.data_ptr(),
-                               y.data_ptr(), st)
-    ms = _events_time(fn, args.steps, args.warmup, stream)
-    nnz = d.numel()
-    alg = 24 * nnz + 8 * (N + 1) + 16 * N  # entries + indptr + y; v gathers hit L2 (64 MiB)
-    ref = op.apply(v)
-    err = float(torch.linalg.vector_norm(y - ref) / torch.linalg.vector_norm(ref))
-    hbm, peak_kind = peaks()
-    gbs = alg / (ms / 1e3) / 1e9
-    out = _base_line(
-        args, "CSR*vector nnz/s (qr_csr_spmv, complex128)", nnz / (ms / 1e3), "nnz/s", ms,
-        "c128",
-        {"workload": "tfim+xxz open chain n=%d, %d terms, CSR built on the device (seed %d)"
-                     % (n, t.T, W.SEED0 + 1), "nnz": int(nnz),
-         "l2": "CSR %d MiB > L2; vector 64 MiB" % ((24 * nnz) >> 20)},
-        roofline={"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
-                  "frac": gbs / hbm, "traffic": None, "alg_bytes_per_launch": alg,
-                  "alg_bytes_rule": "24 nnz + 8 (N+1) + 16 N", "peak_source": peak_kind},
-        rel_err={"vs_matrix_free_c128": err},
-        # complex128 multiply-add = 4 FP64 FMAs (8 flops) per entry; GB300's
-        # nominal FP64 rate (1.25 TFLOP/s) bounds this kernel before HBM does
-        fp64={"tflops": 8.0 * nnz / (ms / 1e3) / 1e12,
-              "frac_of_nominal": 8.0 * nnz / (ms / 1e3) / 1.25e12,
-              "hbm_floor_ms": alg / (hbm * 1e9) * 1e3,
-              "fp64_floor_ms": 8.0 * nnz / 1.25e12 * 1e3})
-    if not args.no_cpu:
-        from oracle import oracle as O
-        O.build()
-        rows = min(N, args.cpu_rows * 4)
-        ipc, ijc, dc = O.csr_build(n, t.x, t.z, O.make_params(t.phase, t.coeff), rows=(0, rows))
-        vh = v.cpu().numpy()
-        nth = os.cpu_count() or 1
-        O.spmv(ipc, ijc, dc, vh, nthreads=nth)
-        t0 = time.perf_counter()
-        for _ in range(3):
-            O.spmv(ipc, ijc, dc, vh, nthreads=nth)
-        dt = (time.perf_counter() - t0) / 3
-        out["cpu_baseline"] = {"value": len(dc) / dt, "unit": "nnz/s", "cores": nth, "kind": "port",
-                               "sample": "rows [0, %d) of 2^%d, chunks of 1024 rows" % (rows, n)}
+    _, sp = measure_csr(args.steps, args.warmup, n=args.n if args.n != 26 else 22)
+    out = _base_line(args, "CSR*vector nnz/s (qr_csr_spmv, complex128)", sp["value"], "nnz/s",
+                     sp["ms_per_step"], "c128", {"workload": sp["workload"]},
+                     roofline=sp["roofline"], fp64_tflops=sp["fp64_tflops"],
+                     rel_err_vs_oracle_rows=sp["rel_err_vs_oracle_rows"],
+                     gpu_launches=sp["gpu_launches_per_step"])
     print(json.dumps(out), flush=True)
 
 
@@ -695,6 +918,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--quick", action="store_true",
                     help="no clock sampling, e2e or CPU baseline (profiling runs)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="headline only: skip the secondary workloads of the default line")
     args = ap.parse_args()
     if args.warmup < 3 and not args.quick:
         raise SystemExit("--warmup must be >= 3")

@@ -152,6 +152,40 @@ int qr_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
  * gradient-based coefficient optimisation. */
 int qr_op_set_coeffs(qr_op *op, const double *coeff);
 
+/* qr_op_set_coeffs with the coefficients in DEVICE memory (T (re, im)
+ * doubles, same order and meaning), asynchronous on `stream`, with no host
+ * synchronisation: for training loops whose coefficients live on the GPU.
+ * Replaces building a new SparsePauliOp (qrusty/src/lib.rs:354-376) like
+ * qr_op_set_coeffs.  Kernels on `stream` recompute c' (make_params,
+ * qrusty/src/accel.rs:141-157), the merged sums and every coefficient table
+ * of the plans already built (qr_apply / qr_apply_axpby / qr_expect /
+ * batches of this operator, and their diagonals), with the same FP64
+ * operations in the same order as a host build, so results are bit for bit
+ * those of an operator created with these coefficients.  Work on other
+ * streams that reads the operator must be ordered after it by the caller;
+ * `coeff` may be reused once the stream has passed this call.  A batch keeps
+ * its graph (its tables are rewritten in place).  Host-side consumers of the
+ * coefficients -- a plan built later, qr_csr_build, qr_op_diagonal -- fetch
+ * them once (synchronous).  The first call uploads the operator's fold
+ * structure (synchronous). */
+int qr_op_set_coeffs_device(qr_op *op, const double *coeff, void *stream);
+
+/* TEST HOOKS -- not for production use; no reference counterpart.  They let
+ * the test suite reach code that ordinary inputs do not:
+ *  - flags & QR_TEST_FORCE_WIDE: this operator's CSR fill and compensated
+ *    complex64 apply kernels use the 64-bit row-word instantiations that
+ *    operators with n > 32 need, at any n (results are identical);
+ *  - wait_ns: bound of every mbarrier wait of this operator's apply kernels
+ *    (0 = the default 2 s; otherwise at least 1 ms);
+ *  - withhold_step >= 0: in this operator's apply kernels, CTA 0 never
+ *    issues the partner-tile copy of that step of its ring, so the wait for
+ *    it runs out after wait_ns.  The kernel then stops computing, waits for
+ *    the copies it did issue, records the error word and returns; qr_check
+ *    reports QR_EKERNEL.  -1 = off.
+ * Hooks stay set until changed; (0, 0, -1) restores normal operation. */
+enum { QR_TEST_FORCE_WIDE = 1 };
+int qr_op_set_test_hooks(qr_op *op, uint32_t flags, uint64_t wait_ns, int64_t withhold_step);
+
 /* out[s] = <a_s, b_s> = sum_r conj(a_s[r]) * b_s[r] for nstates states of
  * 2^n amplitudes, accumulated in FP64 (complex128 out: 2 doubles per state,
  * device pointer).  dtype QR_C128 or QR_C64C (inputs complex64).  New: no
@@ -203,15 +237,17 @@ int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32
  * counterpart (qrusty applies one operator at a time).
  *
  * qr_batch_create: ops[i] (all on the current device, n <= 32) with
- * nstates[i] states each.  The operators must outlive the batch, and their
- * coefficients must not change while it exists.
+ * nstates[i] states each.  The operators must outlive the batch.  When an
+ * operator's coefficients change (qr_op_set_coeffs), the next
+ * qr_batch_apply synchronises `stream`, rebuilds the plan tables and makes
+ * its graph again before launching.
  * qr_batch_apply: psi[i] / y[i] are device pointers to operator i's
  * nstates[i] complex64 states (back to back).  The first call times, on the
  * given buffers (y is overwritten), (a) one persistent kernel over a work list
- * of (operator, state, amplitude tile) items at tile widths 2^12, 2^11, 2^10
- * and (b) a graph of one apply kernel per operator on four parallel
- * branches, keeps the fastest and captures it into a CUDA graph; every call
- * launches that graph on `stream`.  A call whose pointers differ from the
+ * of (operator, state, amplitude tile) items and (b) a graph of one apply
+ * kernel per operator on four parallel branches, keeps the faster and
+ * captures it into a CUDA graph; every call launches that graph on
+ * `stream`.  A call whose pointers differ from the
  * previous call's synchronises `stream` first (and, for (b), captures the
  * graph again). */
 typedef struct qr_batch qr_batch;

@@ -31,7 +31,10 @@ EXPORTS = (
     "qr_batch_apply", "qr_batch_tile_bits", "qr_batch_mode", "qr_batch_set_mode", "qr_axpby", "qr_axpy", "qr_ax", "qr_precond2",
     "qr_csr_diagonal", "qr_op_diagonal", "qr_apply_axpby", "qr_rawio_info", "qr_rawio_read", "qr_rawio_write",
     "qr_mm_write", "qr_mm_open", "qr_mm_fetch", "qr_mm_close", "qr_last_error", "qr_launch_count",
+    "qr_op_set_test_hooks", "qr_op_set_coeffs_device",
 )
+
+QR_TEST_FORCE_WIDE = 1
 
 
 class CsrFileInfo(C.Structure):
@@ -84,6 +87,8 @@ def load(build_if_missing: bool = True):
     L.qr_apply_host.argtypes = [vp, i32, vp, vp, i32, i32]
     L.qr_csr_spmv.argtypes = [u64, u64, vp, vp, vp, vp, vp, vp]
     L.qr_op_set_coeffs.argtypes = [vp, vp]
+    L.qr_op_set_test_hooks.argtypes = [vp, C.c_uint32, u64, C.c_int64]
+    L.qr_op_set_coeffs_device.argtypes = [vp, vp, vp]
     L.qr_vdot.argtypes = [i32, i32, vp, vp, i32, vp, vp]
     L.qr_expect.argtypes = [vp, i32, vp, i32, vp, vp]
     L.qr_vdot_noalloc.argtypes = [i32, i32, vp, vp, i32, vp, vp]

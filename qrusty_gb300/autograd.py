@@ -11,6 +11,12 @@ hand-written backward:
 Here P_k is term k without its coefficient, (1, -i, -1, +i)[phase_k] X^x Z^z,
 and <a, b> = sum conj(a) b.  complex64 states run the compensated-c64
 kernels, complex128 states the plain c128 kernels.
+
+Coefficients on the GPU stay there: each forward hands them to
+``qr_op_set_coeffs_device``, whose kernels rebuild the operator's plan
+tables on the current stream, so a training step (forward, backward,
+optimizer update) has no host synchronisation once the plans exist.
+Coefficients in host memory take ``qr_op_set_coeffs`` (synchronous).
 """
 from __future__ import annotations
 
@@ -33,26 +39,48 @@ class PauliTerms:
         self.T = len(self.x)
         self._op = None
         self._cur = None
+        self._dev_ref = None
+        self._dev_ver = -1
 
-    def operator(self, coeffs: np.ndarray) -> PauliOperator:
-        c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+    def _ensure(self, c_host=None) -> PauliOperator:
         if self._op is None:
+            c = np.zeros(self.T, dtype=np.complex128) if c_host is None else c_host
             self._op = PauliOperator(self.n, self.x, self.z, self.phase, c)
-        elif self._cur is None or not np.array_equal(self._cur, c):
+            self._cur = None if c_host is None else c_host.copy()
+        return self._op
+
+    def operator(self, coeffs) -> PauliOperator:
+        """The operator with these coefficients: a CUDA tensor updates it on
+        the device (no host synchronisation), anything else on the host."""
+        if isinstance(coeffs, torch.Tensor) and coeffs.is_cuda:
+            op = self._ensure()
+            # the same tensor object at the same version was loaded last time
+            # (a backward after its forward): nothing to do.  The reference
+            # held here keeps its memory from being reused by another tensor.
+            if not (coeffs is self._dev_ref and coeffs._version == self._dev_ver):
+                op.set_coeffs_device(coeffs)
+                self._dev_ref, self._dev_ver = coeffs, coeffs._version
+            self._cur = None
+            return op
+        c = np.ascontiguousarray(
+            coeffs.detach().to("cpu", torch.complex128).numpy()
+            if isinstance(coeffs, torch.Tensor) else coeffs, dtype=np.complex128)
+        if self._op is None:
+            return self._ensure(c)
+        if self._cur is None or not np.array_equal(self._cur, c):
             self._op.set_coeffs(c)
-        self._cur = c.copy()
+            self._cur = c.copy()
+        self._dev_ref = None
         return self._op
 
 
 class _PauliApply(torch.autograd.Function):
     @staticmethod
     def forward(ctx, coeffs, psi, terms):
-        c_host = coeffs.detach().to("cpu", torch.complex128).numpy()
-        op = terms.operator(c_host)
+        op = terms.operator(coeffs)
         y = op.apply(psi.contiguous())
-        ctx.save_for_backward(psi)
+        ctx.save_for_backward(psi, coeffs)
         ctx.terms = terms
-        ctx.c_host = c_host
         ctx.real = not coeffs.is_complex()
         ctx.cdtype = coeffs.dtype
         ctx.cdevice = coeffs.device
@@ -60,8 +88,9 @@ class _PauliApply(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, gy):
-        (psi,) = ctx.saved_tensors
-        op = ctx.terms.operator(ctx.c_host)
+        psi, coeffs = ctx.saved_tensors
+        # the operator may have seen other coefficients since this forward
+        op = ctx.terms.operator(coeffs)
         gy = gy.contiguous()
         grad_c = grad_psi = None
         if ctx.needs_input_grad[1]:

@@ -18,7 +18,7 @@ OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libqrusty_gpu.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
-SOURCES = ["qr_host.cu", "qr_apply.cu", "qr_csr.cu", "qr_reduce.cu", "qr_vec.cu"]
+SOURCES = ["qr_host.cu", "qr_apply.cu", "qr_csr.cu", "qr_reduce.cu", "qr_vec.cu", "qr_coef.cu"]
 HOST_SOURCES = ["qr_io.cpp"]  # host-only C++ (file formats), compiled by the host compiler
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
@@ -41,6 +41,25 @@ def _stale(target: str, deps) -> bool:
 
 def cuda_include() -> str:
     return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "include")
+
+
+PROBE = os.path.join(PKG, "libqrusty_probe.so")
+
+
+def _build_probe(force: bool, verbose: bool) -> None:
+    """libqrusty_probe.so: measurement kernels of the benchmark (the FP64
+    peak behind the complex128 roofline); not part of the product ABI."""
+    src = os.path.join(CSRC, "qr_probe.cu")
+    if not force and not _stale(PROBE, [src]):
+        return
+    tmp = PROBE + ".tmp%d" % os.getpid()
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", src, "-o", tmp]
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
+    os.replace(tmp, PROBE)
 
 
 def build(force: bool = False, verbose: bool = False, extra=()) -> str:
@@ -79,6 +98,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES) + len(HOST_SOURCES)) as ex:
         list(ex.map(compile_one, jobs))
+    _build_probe(force, verbose)
     objs = [os.path.join(OBJ, s.replace(".cu", ".o")) for s in SOURCES]
     objs += [os.path.join(OBJ, s.replace(".cpp", ".o")) for s in HOST_SOURCES]
     if force or jobs or _stale(LIB, objs):

@@ -180,6 +180,7 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
         const uint64_t src_tile = q ^ a.blk_hi[j];
         const C *src = psi + st * a.N + (src_tile << a.b);
         const int s = (int)(L % (uint64_t)stages);
+        if (blockIdx.x == 0 && (int64_t)L == a.withhold) return;  // test hook: never issued
         mbar_expect_tx(&full[s], tile_bytes);
         bulk_g2s(bufs + (size_t)s * tile, src, tile_bytes, &full[s]);
     };
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
         }
         const int s = (int)(L % (uint64_t)stages);
         const uint32_t par = (uint32_t)((L / (uint64_t)stages) & 1ull);
-        const bool ok = mbar_wait_bounded(&full[s], par, kWaitLimitNs);
+        const bool ok = mbar_wait_bounded(&full[s], par, a.wait_ns);
         const C *buf = bufs + (size_t)s * tile;
 
         if constexpr (COMP) {
@@ -328,8 +329,12 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
         if (__syncthreads_or(ok ? 0 : 1)) {
             if (t == 0) {
                 atomicExch(a.err, kErrMbarTimeout);
-                // Drain copies still in flight into this CTA's stages.
+                // Drain the copies issued into this CTA's stages (steps L ..
+                // L + stages - 1; a withheld test step was never issued).  The
+                // drain keeps the full 2 s bound whatever a test set for the
+                // waits above: an issued copy always completes.
                 for (uint64_t L2 = L; L2 < total && L2 < L + (uint64_t)stages; ++L2) {
+                    if (blockIdx.x == 0 && (int64_t)L2 == a.withhold) continue;
                     const int s2 = (int)(L2 % (uint64_t)stages);
                     mbar_wait_bounded(&full[s2], (uint32_t)((L2 / stages) & 1ull), kWaitLimitNs);
                 }
@@ -341,8 +346,8 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 }
 
 // ---------------------------------------------------------------- c64c kernels
-// Compensated complex64 path.  A 4096-amplitude tile is held by T threads x
-// AMPS amplitudes (single-operator kernel: 512 x 8, batched kernel: 256 x 16);
+// Compensated complex64 path.  A 4096-amplitude tile is held by T = 512
+// threads x AMPS = 8 amplitudes (single-operator and batched kernels);
 // thread t owns r_lo = t + T m.  The host splits every x-group into
 // sub-groups whose z masks agree on the register bits [kTb, kTb + log2 AMPS)
 // and whose z differences span rank <= 2, so for a thread the sub-group's
@@ -360,55 +365,18 @@ __global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyAr
 // decoupled: each waits on the stage's full mbarrier, consumes it, and counts
 // itself out on a shared counter; the last warp out refills the stage with
 // the tile a ring length ahead.  No CTA-wide barrier sits on the
-// steady-state path.  The single-operator kernel runs 16 warps per SM
-// (512 x 8 hides more latency than 256 x 16, and fewer register bits leave
-// fewer sign patterns to split on); the batched kernel keeps 256 x 16, its
-// register budget at 512 threads spills.
+// steady-state path.  The kernels run 16 warps per SM (512 x 8 hides more
+// latency than 256 x 16, and fewer register bits leave fewer sign patterns
+// to split on).
 constexpr int kTb = kC64ThreadBits;       // log2(threads) whenever AMPS >= 2
 constexpr int kMsh = kTb + 3;             // byte shift of the register index m
 constexpr int kFlush = 8;                 // partner tiles per compensated fold
 constexpr int kC64Threads = 1 << kTb;
-constexpr int kC64Stages = 6;
-constexpr int kBatchTb = kBatchThreadBits;
-constexpr int kBatchMsh = kBatchTb + 3;
-constexpr int kBatchThreads = 1 << kBatchTb;
 
 template <bool WIDE>
 __device__ __forceinline__ uint32_t parity(uint64_t r, uint64_t m) {
     if constexpr (WIDE) return (uint32_t)__popcll(r & m) & 1u;
     else return (uint32_t)__popc((uint32_t)r & (uint32_t)m) & 1u;
-}
-
-// Rank 3-4 (table) or term-by-term ("fat") sub-group through GroupDesc.
-template <int AMPS, int MSH = kMsh>
-__device__ __forceinline__ void big_group_c64(float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                           const unsigned char *sm, uint32_t off,
-                                           const GroupDesc &gd, uint64_t r0, int tb,
-                                           const float2 *tables, const uint64_t *fat_z,
-                                           const float2 *fat_c) {
-#pragma unroll
-    for (int m = 0; m < AMPS; ++m) {
-        const uint64_t r = r0 | ((uint64_t)m << tb);
-        float dr = 0.f, di = 0.f;
-        if (gd.d != kFat) {
-            uint32_t u = 0;
-            for (uint32_t i = 0; i < gd.d; ++i) u |= ((uint32_t)__popcll(r & gd.beta[i]) & 1u) << i;
-            const float2 T = tables[gd.off + u];
-            const bool ng = (__popcll(r & gd.z0) & 1) != 0;
-            dr = ng ? -T.x : T.x;
-            di = ng ? -T.y : T.y;
-        } else {
-            for (uint32_t kk = 0; kk < gd.cnt; ++kk) {
-                const float2 ck = fat_c[gd.off + kk];
-                const bool ng = (__popcll(r & fat_z[gd.off + kk]) & 1) != 0;
-                dr += ng ? -ck.x : ck.x;
-                di += ng ? -ck.y : ck.y;
-            }
-        }
-        const float2 p = *reinterpret_cast<const float2 *>(sm + (off ^ ((uint32_t)m << MSH)));
-        A[m] = __ffma2_rn(make_float2(dr, dr), p, A[m]);
-        B[m] = __ffma2_rn(make_float2(di, di), p, B[m]);
-    }
 }
 
 // ---------------------------------------------------------------- c64c, tile table
@@ -425,9 +393,10 @@ __device__ __forceinline__ void big_group_c64(float2 (&A)[AMPS], float2 (&B)[AMP
 constexpr int kTabStages = 4;  // partner-tile ring depth (timed best of 3, 4, 5)
 constexpr size_t kMaxSmemPerBlock = 227u * 1024u;  // sm_100-family opt-in limit
 constexpr int kTabEnt = 4;  // per-tile table entries (float4) per sub-group
-// full barriers, stage counters and the abort flag, rounded to 16 bytes so
-// that the 16-byte thread descriptors after them stay aligned
-constexpr size_t kTabBarBytes = ((size_t)kTabStages * 12u + 4u + 15u) & ~(size_t)15u;
+// full barriers, stage counters, the abort flag and per-stage issue counts,
+// rounded to 16 bytes so that the 16-byte thread descriptors after them stay
+// aligned
+constexpr size_t kTabBarBytes = ((size_t)kTabStages * 16u + 4u + 15u) & ~(size_t)15u;
 static_assert(kTabBarBytes % 16 == 0, "thread descriptors need 16-byte alignment");
 
 template <int AMPS, int ZM, bool XM, bool TV>
@@ -446,9 +415,13 @@ __device__ __forceinline__ void sub_tab_one(float2 (&A)[AMPS], float2 (&B)[AMPS]
         }
         const float4 T = s_tab[g * 4 + u];
         // thread sign (-1)^sg on both factor pairs: one packed multiply each
-        const float sv = __uint_as_float(0x3f800000u | (sg << 31));
-        const float2 ap = __fmul2_rn(make_float2(T.x, T.y), make_float2(sv, sv));
-        const float2 bp = __fmul2_rn(make_float2(T.z, T.w), make_float2(sv, sv));
+        // (runs whose factor does not depend on the thread have none)
+        float2 ap = make_float2(T.x, T.y), bp = make_float2(T.z, T.w);
+        if constexpr (TV) {
+            const float sv = __uint_as_float(0x3f800000u | (sg << 31));
+            ap = __fmul2_rn(ap, make_float2(sv, sv));
+            bp = __fmul2_rn(bp, make_float2(sv, sv));
+        }
         // partner byte offset: the XOR part (thread and register bits of lo) is
         // precomputed per sub-group; the stage offset occupies higher bits
         const uint32_t off = soff | (t8 ^ (d.x & 0xffffu));  // bit 15: pair half
@@ -511,8 +484,11 @@ __device__ __forceinline__ void sub_tab_fused(float2 (&A)[AMPS], float2 (&B)[AMP
     const float4 Tb = s_tab[(g + 1) * 4 + ub];
     const float sva = __uint_as_float(0x3f800000u | (sa << 31));
     const float svb = __uint_as_float(0x3f800000u | (sb << 31));
-    const float2 apa = __fmul2_rn(make_float2(Ta.x, Ta.y), make_float2(sva, sva));
-    const float2 bpa = __fmul2_rn(make_float2(Ta.z, Ta.w), make_float2(sva, sva));
+    float2 apa = make_float2(Ta.x, Ta.y), bpa = make_float2(Ta.z, Ta.w);
+    if constexpr (TV) {
+        apa = __fmul2_rn(apa, make_float2(sva, sva));
+        bpa = __fmul2_rn(bpa, make_float2(sva, sva));
+    }
     // F_a + F_b and F_a - F_b: one rounding each (the sign products are exact)
     const float2 a0 = __ffma2_rn(make_float2(Tb.x, Tb.y), make_float2(svb, svb), apa);
     const float2 b0 = __ffma2_rn(make_float2(Tb.z, Tb.w), make_float2(svb, svb), bpa);
@@ -621,6 +597,9 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
     uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
     uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kTabStages);
     volatile uint32_t *s_abort = cnt + kTabStages;
+    // copies issued into each stage: the drain after an expired wait waits
+    // for the last one's phase, so no copy is in flight when the CTA exits
+    uint32_t *s_iss = cnt + kTabStages + 1;
     // sub-group descriptors, runs (g0 | key << 16) and per-block run ranges of
     // the current chunk, indices relative to the chunk; with one chunk they
     // are staged once per CTA
@@ -656,6 +635,8 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
         const uint64_t q = item - st * a.ntiles;
         const float2 *src = psi + st * a.N + ((q ^ a.blk_hi[j]) << a.b);
         const int s = (int)(L % (uint64_t)kTabStages);
+        if (blockIdx.x == 0 && (int64_t)L == a.withhold) return;  // test hook: never issued
+        ++s_iss[s];
         mbar_expect_tx(&full[s], tile_bytes);
         bulk_g2s(smem_raw + (size_t)s * tile_bytes, src, tile_bytes, &full[s]);
     };
@@ -663,6 +644,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
         for (int s = 0; s < kTabStages; ++s) {
             mbar_init(&full[s], 1);
             cnt[s] = 0;
+            s_iss[s] = 0;
         }
         *s_abort = 0;
         mbar_fence_init();
@@ -721,7 +703,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
         // A wait that expires sets the abort flag; from then on every warp
         // skips waits and work but still reaches each tile barrier.
         bool skip = *s_abort != 0;
-        if (!skip && !mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
+        if (!skip && !mbar_wait_bounded(&full[s], par, a.wait_ns)) {
             if (lane == 0) {
                 atomicExch(a.err, kErrMbarTimeout);
                 *s_abort = 1;
@@ -802,8 +784,11 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
                         }
                     }
                     const float2 *src = psi + st2 * a.N + ((q2 ^ a.blk_hi[j2]) << a.b);
-                    mbar_expect_tx(&full[s], tile_bytes);
-                    bulk_g2s(smem_raw + (size_t)s * tile_bytes, src, tile_bytes, &full[s]);
+                    if (blockIdx.x != 0 || (int64_t)(L + kTabStages) != a.withhold) {
+                        ++s_iss[s];
+                        mbar_expect_tx(&full[s], tile_bytes);
+                        bulk_g2s(smem_raw + (size_t)s * tile_bytes, src, tile_bytes, &full[s]);
+                    }
                 }
             }
         }
@@ -820,9 +805,16 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
             }
         }
     }
-    if (*s_abort && t == 0) {
-        // bounded drain of copies that may still target this CTA's stages
-        for (int k = 0; k < kTabStages; ++k) mbar_wait_bounded(&full[k], 0, kWaitLimitNs / 8);
+    // After an expired wait: every warp has left the loop (no copy is issued
+    // after the abort flag is set), then a bounded wait for the last copy
+    // issued into each stage -- its phase parity is (issues - 1) & 1 -- so
+    // that no copy still targets this CTA's shared memory when it exits.
+    // The drain keeps the full 2 s bound whatever a test set for the waits:
+    // an issued copy always completes.
+    __syncthreads();
+    if (t == 0 && *s_abort) {
+        for (int k = 0; k < kTabStages; ++k)
+            if (s_iss[k] != 0) mbar_wait_bounded(&full[k], (s_iss[k] - 1u) & 1u, kWaitLimitNs);
     }
 }
 
@@ -847,6 +839,9 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
     uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kTabStages);
     volatile uint32_t *s_abort = cnt + kTabStages;
+    // copies issued into each stage: the drain after an expired wait waits
+    // for the last one's phase, so no copy is in flight when the CTA exits
+    uint32_t *s_iss = cnt + kTabStages + 1;
     uint4 *s_td = reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(s_lo) +
                                             (size_t)AMPS * threads * 8u + kTabBarBytes);
     uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + kTabCap);
@@ -873,9 +868,11 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     if (total == 0) return;
 
     // load pair p of tile (st, q) into slot s: one or two partner tiles
-    auto issue_pair = [&](uint32_t s, uint32_t p, uint64_t st, uint64_t q) {
+    auto issue_pair = [&](uint64_t L, uint32_t s, uint32_t p, uint64_t st, uint64_t q) {
+        if (blockIdx.x == 0 && (int64_t)L == a.withhold) return;  // test hook: never issued
         const uint32_t j0 = 2u * p;
         const uint32_t ntl = j0 + 1 < nb ? 2u : 1u;
+        ++s_iss[s];
         mbar_expect_tx(&full[s], ntl * tile_bytes);
         for (uint32_t h = 0; h < ntl; ++h) {
             const float2 *src = psi + st * a.N + ((q ^ a.blk_hi[j0 + h]) << a.b);
@@ -889,6 +886,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
         for (int s = 0; s < 2; ++s) {
             mbar_init(&full[s], 1);
             cnt[s] = 0;
+            s_iss[s] = 0;
         }
         *s_abort = 0;
         mbar_fence_init();
@@ -896,7 +894,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
         uint32_t p1 = 0;
         uint64_t q1 = q, st1 = st;
         for (uint64_t L = 0; L < total && L < 2; ++L) {
-            issue_pair((uint32_t)L, p1, st1, q1);
+            issue_pair(L, (uint32_t)L, p1, st1, q1);
             if (++p1 == np) {
                 p1 = 0;
                 q1 += gridDim.x;
@@ -943,7 +941,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
         bool skip = false;
         if (!__all_sync(0xffffffffu, mbar_try_wait(&full[s], par))) {
             skip = *s_abort != 0;
-            if (!skip && !mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
+            if (!skip && !mbar_wait_bounded(&full[s], par, a.wait_ns)) {
                 if (lane == 0) {
                     atomicExch(a.err, kErrMbarTimeout);
                     *s_abort = 1;
@@ -1031,7 +1029,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
                             ++st2;
                         }
                     }
-                    issue_pair(s, p2, st2, q2);
+                    issue_pair(L + 2, s, p2, st2, q2);
                 }
             }
         }
@@ -1046,9 +1044,11 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
             }
         }
     }
-    if (*s_abort && t == 0) {
-        // bounded drain of copies that may still target this CTA's stages
-        for (int k = 0; k < 2; ++k) mbar_wait_bounded(&full[k], 0, kWaitLimitNs / 8);
+    // drain after an expired wait, as in apply_c64c_tab
+    __syncthreads();
+    if (t == 0 && *s_abort) {
+        for (int k = 0; k < 2; ++k)
+            if (s_iss[k] != 0) mbar_wait_bounded(&full[k], (s_iss[k] - 1u) & 1u, kWaitLimitNs);
     }
 }
 
@@ -1069,8 +1069,7 @@ static cudaError_t launch_c64c_tab(const ApplyArgs &a, int threads, int nsm, cud
     auto kern = a.nchunks > 1 ? apply_c64c_tab<AMPS, WIDE, true> : apply_c64c_tab<AMPS, WIDE, false>;
     if constexpr (AMPS == 8)
         if (a.npairs > 0 && a.nchunks <= 1) kern = apply_c64c_pair<AMPS, WIDE>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = ensure_dyn_smem(reinterpret_cast<const void *>(kern), smem);
     if (e != cudaSuccess) return e;
     uint64_t grid = a.nitems < (uint64_t)nsm ? a.nitems : (uint64_t)nsm;
     if (grid == 0) return cudaSuccess;
@@ -1083,96 +1082,72 @@ template <int AMPS>
 static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
     // shared memory: partner ring, one table chunk, low parts, run lists
     if (tab_smem_bytes<AMPS>(a, threads) > kMaxSmemPerBlock) return cudaErrorInvalidValue;
-    if (a.n > 32) return launch_c64c_tab<AMPS, true>(a, threads, nsm, st);
+    if (a.n > 32 || a.wide) return launch_c64c_tab<AMPS, true>(a, threads, nsm, st);
     return launch_c64c_tab<AMPS, false>(a, threads, nsm, st);
 }
 
 // ---------------------------------------------------------------- batched c64c
 // Many operators (different n, term counts and state counts) in ONE
 // persistent launch over a host-built work list of (operator, state, tile)
-// items.  Same partner-tile ring and inner step as apply_c64c_tab; the operator's
-// parameters come from a device array per item, tiles of operators with
-// n < 12 use the first 2^n amplitudes of a stage, and the warp that refills a
-// stage walks the work list six steps ahead to find the tile to load.
-template <int AMPS, int ZM, bool XM>
-__device__ __forceinline__ void mloop_plain(float2 (&A)[AMPS], float2 (&B)[AMPS],
-                                            const unsigned char *sm, uint32_t off, float2 D) {
-    float2 p[AMPS];
-#pragma unroll
-    for (int m = 0; m < AMPS; ++m) {
-        const uint32_t o = XM ? (off ^ ((uint32_t)m << kBatchMsh)) : (off + ((uint32_t)m << kBatchMsh));
-        p[m] = *reinterpret_cast<const float2 *>(sm + o);
-    }
-    const float2 ap = make_float2(D.x, D.x), an = make_float2(-D.x, -D.x);
-    const float2 bp = make_float2(D.y, D.y), bn = make_float2(-D.y, -D.y);
-#pragma unroll
-    for (int m = 0; m < AMPS; ++m) {
-        const bool neg = (__builtin_popcount((unsigned)(m & ZM)) & 1) != 0;
-        A[m] = __ffma2_rn(neg ? an : ap, p[m], A[m]);
-        B[m] = __ffma2_rn(neg ? bn : bp, p[m], B[m]);
-    }
-}
-
-template <int AMPS>
-__device__ __forceinline__ void mloop_plain_dispatch(uint32_t key, float2 (&A)[AMPS],
-                                                     float2 (&B)[AMPS], const unsigned char *sm,
-                                                     uint32_t off, float2 D) {
-#define QR_ZM_CASE(k)                                                                   \
-    case k:                                                                             \
-        if constexpr ((k & 15) < AMPS) mloop_plain<AMPS, (k & 15), (k >> 4) != 0>(A, B, sm, off, D); \
-        break;
-    switch (key) {
-        QR_ZM_CASE(0) QR_ZM_CASE(1) QR_ZM_CASE(2) QR_ZM_CASE(3)
-        QR_ZM_CASE(4) QR_ZM_CASE(5) QR_ZM_CASE(6) QR_ZM_CASE(7)
-        QR_ZM_CASE(8) QR_ZM_CASE(9) QR_ZM_CASE(10) QR_ZM_CASE(11)
-        QR_ZM_CASE(12) QR_ZM_CASE(13) QR_ZM_CASE(14) QR_ZM_CASE(15)
-        QR_ZM_CASE(16) QR_ZM_CASE(17) QR_ZM_CASE(18) QR_ZM_CASE(19)
-        QR_ZM_CASE(20) QR_ZM_CASE(21) QR_ZM_CASE(22) QR_ZM_CASE(23)
-        QR_ZM_CASE(24) QR_ZM_CASE(25) QR_ZM_CASE(26) QR_ZM_CASE(27)
-        QR_ZM_CASE(28) QR_ZM_CASE(29) QR_ZM_CASE(30) QR_ZM_CASE(31)
-        default: break;
-    }
-#undef QR_ZM_CASE
-}
-
-template <int AMPS>
-__global__ void __launch_bounds__(kBatchThreads, 1) apply_c64c_batch(const BatchArgs a) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
+// items, with the inner loop of apply_c64c_tab: per output tile the
+// operator's per-tile factor table is built in shared memory -- one chunk of
+// at most kTabCap sub-groups at a time, its thread descriptors and run lists
+// staged beside it -- partner tiles stream through the TMA ring, and each
+// run of sub-groups with equal key is one dispatch.  512 threads x 8
+// amplitudes; an operator with n < 12 has tiles of 2^n amplitudes, held by
+// threads t < tact and register indices m < mcount (the other lanes compute
+// on in-bounds shared memory and store nothing).  The lane that releases a
+// stage walks the work list kTabStages steps ahead to find the tile it
+// loads next.
+__global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchArgs a) {
+    constexpr int AMPS = 8;
     constexpr uint32_t kStageBytes = 4096u * 8u;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t threads = blockDim.x;
     const uint32_t nwarps = threads >> 5;
     const uint32_t t = threadIdx.x;
     const uint32_t lane = t & 31;
-    float2 *s_lo = reinterpret_cast<float2 *>(smem_raw + (size_t)kC64Stages * kStageBytes);
+    const uint32_t t8 = t << 3;
+    float4 *s_tab = reinterpret_cast<float4 *>(smem_raw + (size_t)kTabStages * kStageBytes);
+    float2 *s_lo = reinterpret_cast<float2 *>(s_tab + kTabEnt * (size_t)kTabCap);
     uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
-    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kC64Stages);
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kTabStages);
+    volatile uint32_t *s_abort = cnt + kTabStages;
+    uint32_t *s_iss = cnt + kTabStages + 1;  // copies issued per stage (drain)
+    uint4 *s_td = reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(s_lo) +
+                                            (size_t)AMPS * threads * 8u + kTabBarBytes);
+    uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + kTabCap);
+    uint32_t *s_blk = s_run + kTabCap + 1;
     const uint32_t stride = gridDim.x;
     if (blockIdx.x >= a.nitems) return;
 
-    // step cursor (item index, block of that item's operator) -> next step
+    // step cursor (work-list index, block of that item's operator) -> next step
     auto advance = [&](uint32_t &ik, uint32_t &j) {
         if (++j == a.ops[a.items[ik].op].nblocks) {
             j = 0;
             ik += stride;
         }
     };
-    auto issue = [&](uint32_t ik, uint32_t j, int s) {
+    auto issue = [&](uint32_t ik, uint32_t j, uint32_t s) {
         const BatchItem it = a.items[ik];
         const BatchOp &o = a.ops[it.op];
         const uint32_t bytes = (1u << o.b) * 8u;
         const float2 *src =
             a.psi[it.op] + (uint64_t)it.state * o.N + (((uint64_t)it.tile ^ o.blk_hi[j]) << o.b);
+        ++s_iss[s];
         mbar_expect_tx(&full[s], bytes);
         bulk_g2s(smem_raw + (size_t)s * kStageBytes, src, bytes, &full[s]);
     };
     if (t == 0) {
-        for (int s = 0; s < kC64Stages; ++s) {
+        for (int s = 0; s < kTabStages; ++s) {
             mbar_init(&full[s], 1);
             cnt[s] = 0;
+            s_iss[s] = 0;
         }
+        *s_abort = 0;
         mbar_fence_init();
         uint32_t ik = blockIdx.x, j = 0;
-        for (int s = 0; s < kC64Stages && ik < a.nitems; ++s) {
+        for (uint32_t s = 0; s < (uint32_t)kTabStages && ik < a.nitems; ++s) {
             issue(ik, j, s);
             advance(ik, j);
         }
@@ -1182,30 +1157,65 @@ __global__ void __launch_bounds__(kBatchThreads, 1) apply_c64c_batch(const Batch
     float2 A[AMPS], B[AMPS], hi[AMPS];
     float2 *mylo = s_lo + t;
     uint32_t ik = blockIdx.x, j = 0, s = 0, par = 0;
+    uint32_t cidx = 0, cj0 = 0, next_j = 0;  // table chunk, its first block, the next's
     while (ik < a.nitems) {
         const BatchItem it = a.items[ik];
         const BatchOp &o = a.ops[it.op];
-        const uint32_t tmask = (uint32_t)o.tact - 1;
-        const uint64_t r0 = ((uint64_t)it.tile << o.b) | t;
-        const bool active = t < (uint32_t)o.tact;
+        const uint64_t q = it.tile;
+        const uint32_t tact = (uint32_t)o.tact, mcount = (uint32_t)o.mcount;
         if (j == 0) {
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
                 A[m] = B[m] = hi[m] = make_float2(0.f, 0.f);
                 mylo[m * threads] = make_float2(0.f, 0.f);
             }
+            cidx = 0;
         }
-        if (!mbar_wait_bounded(&full[s], par, kWaitLimitNs)) {
-            if (lane == 0) atomicExch(a.err, kErrMbarTimeout);
-            return;
+        if (j == 0 || j == next_j) {
+            // table, descriptors and run lists of the chunk starting at block
+            // j of this item's operator: every warp is done with the last one
+            if (j != 0) ++cidx;
+            __syncthreads();
+            const uint4 c0 = o.chunks[cidx], c1 = o.chunks[cidx + 1];
+            cj0 = c0.z;
+            next_j = c1.z;
+            for (uint32_t i = t; i < c1.x - c0.x; i += threads) s_td[i] = o.tdesc[c0.x + i];
+            for (uint32_t i = t; i <= c1.y - c0.y; i += threads) {
+                const uint32_t r = c0.y + i;
+                s_run[i] = (o.run_g0[r] - c0.x) | (r < o.nruns ? o.run_key[r] << 16 : 0u);
+            }
+            for (uint32_t i = t; i <= c1.z - c0.z; i += threads) s_blk[i] = o.blk_r0[c0.z + i] - c0.y;
+            for (uint32_t gi = t; gi < c1.x - c0.x; gi += threads) {
+                const TileDataC64 &d = o.tdata[c0.x + gi];
+                const uint32_t uq = parity<false>(q, d.b0h) | (parity<false>(q, d.b1h) << 1);
+                const float sq = parity<false>(q, d.z0h) ? -1.f : 1.f;
+#pragma unroll
+                for (uint32_t u = 0; u < 4; ++u) {
+                    const float2 v = d.T[u ^ uq];
+                    s_tab[gi * 4 + u] = make_float4(sq * v.x, sq * v.x, sq * v.y, sq * v.y);
+                }
+            }
+            __syncthreads();
         }
+        // an expired wait sets the abort flag; from then on every warp skips
+        // waits and work but still reaches each chunk barrier
+        bool skip = *s_abort != 0;
+        if (!skip && !mbar_wait_bounded(&full[s], par, a.wait_ns)) {
+            if (lane == 0) {
+                atomicExch(a.err, kErrMbarTimeout);
+                *s_abort = 1;
+            }
+            skip = true;
+        }
+        skip = __any_sync(0xffffffffu, skip);
         const uint32_t soff = s * kStageBytes;
-        if ((int)j == o.diag_block && o.diag != nullptr && active) {
-            const float2 *dg = o.diag + ((uint64_t)it.tile << o.b);
+
+        if (!skip && (int)j == o.diag_block && o.diag != nullptr) {
+            const float2 *dg = o.diag + (q << o.b);
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
-                if (m < o.mcount) {
-                    const uint32_t rl = t + (uint32_t)o.tact * (uint32_t)m;
+                if (t < tact && (uint32_t)m < mcount) {
+                    const uint32_t rl = t + tact * (uint32_t)m;
                     const float2 d = dg[rl];
                     const float2 p = *reinterpret_cast<const float2 *>(smem_raw + soff + rl * 8u);
                     A[m] = __ffma2_rn(make_float2(d.x, d.x), p, A[m]);
@@ -1213,84 +1223,82 @@ __global__ void __launch_bounds__(kBatchThreads, 1) apply_c64c_batch(const Batch
                 }
             }
         }
-        const uint32_t g1 = o.blk_g0[j + 1];
-        for (uint32_t g = o.blk_g0[j]; g < g1; ++g) {
-            const SubDescC64 *sd = o.sub + g;
-            const uint32_t lo = sd->lo, kind = sd->kind;
-            const uint32_t off = soff | ((t ^ (lo & tmask)) << 3) | ((lo >> o.tb) << kBatchMsh);
-            if ((kind >> 8) == 0) {
-                const uint32_t u = parity<false>(r0, sd->beta0) |
-                                   (parity<false>(r0, sd->beta1) << 1);
-                float dx = (u & 2u) ? ((u & 1u) ? sd->tab[6] : sd->tab[4])
-                                    : ((u & 1u) ? sd->tab[2] : sd->tab[0]);
-                float dy = (u & 2u) ? ((u & 1u) ? sd->tab[7] : sd->tab[5])
-                                    : ((u & 1u) ? sd->tab[3] : sd->tab[1]);
-                if (parity<false>(r0, sd->z0)) {
-                    dx = -dx;
-                    dy = -dy;
-                }
-                mloop_plain_dispatch<AMPS>(kind & 31u, A, B, smem_raw, off, make_float2(dx, dy));
-            } else {
-                big_group_c64<AMPS, kBatchMsh>(A, B, smem_raw, off, o.groups[g], r0, o.tb, o.tables,
-                                    o.fat_z, o.fat_c);
-            }
+
+        const uint32_t jl = j - cj0;
+        const uint32_t r1 = skip ? 0u : s_blk[jl + 1];
+        uint32_t rw = s_run[s_blk[jl]];
+        for (uint32_t r = s_blk[jl]; r < r1; ++r) {
+            const uint32_t rn = s_run[r + 1];
+            run_tab_dispatch<AMPS>(rw >> 16, A, B, smem_raw, soff, s_tab, s_td, rw & 0xffffu,
+                                   rn & 0xffffu, t, t8);
+            rw = rn;
         }
+
         const bool last = (j == o.nblocks - 1);
         if (last || (j % kFlush) == kFlush - 1) {
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
-                const float yr = __fsub_rn(A[m].x, B[m].y);
-                const float yi = __fadd_rn(A[m].y, B[m].x);
+                const float2 yv =
+                    make_float2(__fsub_rn(A[m].x, B[m].y), __fadd_rn(A[m].y, B[m].x));
                 float2 lm = mylo[m * threads];
-                two_sum_into(hi[m].x, lm.x, yr);
-                two_sum_into(hi[m].y, lm.y, yi);
+                two_sum_into2(hi[m], lm, yv);
                 mylo[m * threads] = lm;
                 A[m] = B[m] = make_float2(0.f, 0.f);
             }
         }
-        if (last && active) {
-            float2 *yo = a.y[it.op] + (uint64_t)it.state * o.N + ((uint64_t)it.tile << o.b);
+        if (last && t < tact) {
+            float2 *yo = a.y[it.op] + (uint64_t)it.state * o.N + (q << o.b);
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
-                if (m < o.mcount) {
+                if ((uint32_t)m < mcount) {
                     const float2 lm = mylo[m * threads];
-                    yo[t + (uint32_t)o.tact * (uint32_t)m] =
+                    yo[t + tact * (uint32_t)m] =
                         make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
                 }
             }
         }
+
         __syncwarp();
         if (lane == 0) {
             __threadfence_block();
             const uint32_t old = atomicAdd(&cnt[s], 1u);
             if (old == nwarps - 1) {
                 cnt[s] = 0;
-                uint32_t ik2 = ik, j2 = j;
-                for (int k = 0; k < kC64Stages && ik2 < a.nitems; ++k) advance(ik2, j2);
-                if (ik2 < a.nitems) {
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    issue(ik2, j2, (int)s);
+                if (*s_abort == 0) {
+                    uint32_t ik2 = ik, j2 = j;
+                    for (int k = 0; k < kTabStages && ik2 < a.nitems; ++k) advance(ik2, j2);
+                    if (ik2 < a.nitems) {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        issue(ik2, j2, s);
+                    }
                 }
             }
         }
-        if (++s == kC64Stages) {
+        if (++s == (uint32_t)kTabStages) {
             s = 0;
             par ^= 1u;
         }
         advance(ik, j);
     }
+    // drain after an expired wait, as in apply_c64c_tab
+    __syncthreads();
+    if (t == 0 && *s_abort) {
+        for (int k = 0; k < kTabStages; ++k)
+            if (s_iss[k] != 0) mbar_wait_bounded(&full[k], (s_iss[k] - 1u) & 1u, kWaitLimitNs);
+    }
 }
 
 cudaError_t launch_batch_c64c(const BatchArgs &a, int nsm, cudaStream_t st) {
-    const size_t smem = (size_t)kC64Stages * 4096u * 8u + (size_t)16 * kBatchThreads * 8u +
-                        kC64Stages * (sizeof(uint64_t) + 4);
-    auto kern = apply_c64c_batch<16>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    constexpr int AMPS = 8;
+    const size_t smem = (size_t)kTabStages * 4096u * 8u + (size_t)kTabCap * 16u * kTabEnt +
+                        (size_t)AMPS * kC64Threads * 8u + kTabBarBytes +
+                        (size_t)kTabCap * sizeof(uint4) + (2u * (size_t)kTabCap + 3u) * 4u;
+    if (smem > kMaxSmemPerBlock) return cudaErrorInvalidValue;
+    cudaError_t e = ensure_dyn_smem(reinterpret_cast<const void *>(apply_c64c_batch), smem);
     if (e != cudaSuccess) return e;
     const uint32_t grid = a.nitems < (uint32_t)nsm ? a.nitems : (uint32_t)nsm;
     if (grid == 0) return cudaSuccess;
-    kern<<<grid, kBatchThreads, smem, st>>>(a);
+    apply_c64c_batch<<<grid, kC64Threads, smem, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }
@@ -1303,8 +1311,7 @@ static cudaError_t launch_one(const ApplyArgs &a, int threads, int nsm, cudaStre
     if (stages < 2) stages = 2;
     const size_t smem = (size_t)stages * tile_bytes + kMaxStages * sizeof(uint64_t);
     auto kern = apply_tiled<Real, AMPS, COMP>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = ensure_dyn_smem(reinterpret_cast<const void *>(kern), smem);
     if (e != cudaSuccess) return e;
     uint64_t grid = a.nitems < (uint64_t)nsm ? a.nitems : (uint64_t)nsm;
     if (grid == 0) return cudaSuccess;
@@ -1399,8 +1406,7 @@ cudaError_t launch_diag(int dtype, int n, int db, uint64_t ntiles, const uint64_
                         const double *tc, void *out, cudaStream_t st) {
     (void)n;
     const size_t smem = ((size_t)1 << db) * sizeof(double2);
-    cudaError_t e = cudaFuncSetAttribute(diag_wht, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = ensure_dyn_smem(reinterpret_cast<const void *>(diag_wht), smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)(ntiles < 4096 ? ntiles : 4096);
     diag_wht<<<grid, 256, smem, st>>>(db, ntiles, bin_zlo, bin_off, nbins, tz, tc, out,

@@ -30,18 +30,6 @@ template <typename Real> struct Cplx;
 template <> struct alignas(8) Cplx<float> { float re, im; };
 template <> struct alignas(16) Cplx<double> { double re, im; };
 
-// Sub-group descriptor of the compensated-c64 kernel (64 bytes).  kind =
-// zm | xm << 4 | d << 5 | big << 8: zm is the z pattern on the register
-// bits, xm = 1 when x has register bits (partners permuted by XOR there),
-// d <= 2 the rank of the inline table, big marks a sub-group evaluated
-// through the side GroupDesc table instead (rank 3-4, or term by term).
-struct alignas(16) SubDescC64 {
-    uint64_t z0, beta0, beta1;
-    uint32_t lo;
-    uint32_t kind;
-    float tab[8];  // inline table: (re, im) x 4
-};
-
 // Per-sub-group data of the per-tile table of the compensated-c64 kernel:
 // the masks' tile-index parts (>> b) and the FP32 table T[u] of the factor.
 struct alignas(16) TileDataC64 {
@@ -69,8 +57,7 @@ struct ApplyArgs {
     const void *diag;       // Cplx<Real>[N] or null (only read in block hi == 0)
     int diag_block;         // index of the hi == 0 block, or -1
     int *err;               // device error word
-    // compensated-c64 plan: one SubDescC64 per sub-group (see qr_apply.cu)
-    const SubDescC64 *sub;
+    // compensated-c64 plan: sub-groups (see qr_apply.cu)
     uint32_t nsub;
     // per-tile-table kernel: per sub-group a 16-byte thread descriptor
     // {partner byte-offset XOR | pair half << 15 | tvar << 31, z0_t, beta0_t,
@@ -95,23 +82,29 @@ struct ApplyArgs {
     // fused epilogue y = alpha * (H psi) + beta * v when v != nullptr
     const void *v;
     double ar, ai, br, bi;
+    // bound of every mbarrier wait (ns); 2 s unless a test shortens it
+    uint64_t wait_ns;
+    // test hook (qr_op_set_test_hooks): the ring step whose partner-tile copy
+    // CTA 0 never issues, so that its wait runs out; -1 = none
+    int64_t withhold;
+    // 64-bit row words (the n > 32 instantiations) forced at any n (test hook)
+    int wide;
 };
 
 
 
-// One operator of a batched compensated-c64 launch (device copy).
+// One operator of a batched compensated-c64 launch (device copy): the
+// per-tile-table plan of the operator (no partner-tile pairs) and its tile
+// geometry.
 struct BatchOp {
     uint64_t N, ntiles;
-    int32_t b, tb, mcount, tact;      // tile bits, log2(active threads), amps used, threads used
-    uint32_t nblocks, nsub;
-    int32_t diag_block, pad;
-    const SubDescC64 *sub;
-    const GroupDesc *groups;
-    const float2 *tables;
-    const uint64_t *fat_z;
-    const float2 *fat_c;
+    int32_t b, mcount, tact, diag_block;  // tile bits, amplitudes / threads used, x = 0 block
+    uint32_t nblocks, nsub, nruns, nchunks;
+    const uint4 *tdesc;
+    const TileDataC64 *tdata;
     const uint64_t *blk_hi;
-    const uint32_t *blk_g0;
+    const uint32_t *blk_r0, *run_g0, *run_key;
+    const uint4 *chunks;
     const float2 *diag;
 };
 struct BatchItem {
@@ -119,13 +112,37 @@ struct BatchItem {
 };
 struct BatchArgs {
     const BatchOp *ops;
-    const BatchItem *items;
+    const BatchItem *items;  // sorted by decreasing work per tile
     uint32_t nitems;
     const float2 *const *psi;  // per operator: its first state; state s at + s * N
     float2 *const *y;
     int *err;
+    uint64_t wait_ns;          // bound of every mbarrier wait
 };
 cudaError_t launch_batch_c64c(const BatchArgs &a, int nsm, cudaStream_t st);
+
+// One entry of a plan's coefficient program (qr_op_set_coeffs_device): the
+// value(s) at dst computed from merged strings [m0, m0 + cnt) of the plan's
+// coefficients c_m (the merged coefficients, or for an adjoint plan
+// conj(c_m) (-1)^popc(x_m & z_m)).  kind 0: 2^d FP32 table entries (float2),
+// entry u = the fold from 0 of +-c_m in member order, sign (-1)^popc(u &
+// coord_m); kind 1: the same in FP64 (double2); kind 2: c_m itself (double2,
+// cnt = 1).  The additions are those of the host plan builder, in its order.
+struct CoefSlot {
+    uint64_t dst;
+    uint32_t m0;
+    uint16_t cnt;
+    uint8_t d, kind;
+};
+static_assert(sizeof(CoefSlot) == 16, "CoefSlot layout");
+
+// qr_coef.cu
+cudaError_t launch_merge_coeffs(uint32_t M, const uint32_t *mm_off, const uint32_t *mm_terms,
+                                const double2 *coeff, const uint8_t *phase, double2 *mc,
+                                cudaStream_t st);
+cudaError_t launch_coef_program(const CoefSlot *slots, uint32_t nslots, const uint32_t *mem,
+                                const uint8_t *coord, const double2 *mc, const uint8_t *madj,
+                                int adjoint, cudaStream_t st);
 
 // Device error codes written to the error word.
 enum : int { kErrNone = 0, kErrMbarTimeout = 1, kErrCsrPos = 2 };
@@ -153,16 +170,20 @@ __device__ __forceinline__ float2 cx_axpby(float ar, float ai, float2 x, float b
 // sub-groups of one per-tile factor table of the compensated-complex64 kernel
 constexpr uint32_t kTabCap = 512;
 
-// log2 of the thread count of the compensated-complex64 kernels: the
-// single-operator kernels and the batched kernel (see qr_apply.cu).
+// log2 of the thread count of the compensated-complex64 kernels (the
+// single-operator kernels and the batched kernel, see qr_apply.cu).
 constexpr int kC64ThreadBits = 9;
-constexpr int kBatchThreadBits = 8;
 
 // Records msg as the calling thread's last error (qr_last_error) and returns code.
 int set_error(int code, const char *msg);
 
 // Per-process launch counter (all launches issued through this library).
 void count_launch(uint64_t k = 1);
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) for kernel fn on the
+// current device, only when `bytes` exceeds what was set before: steady-state
+// launches (and launches inside a stream capture) make no attribute calls.
+cudaError_t ensure_dyn_smem(const void *fn, size_t bytes);
 
 // Kernel launchers (qr_apply.cu / qr_csr.cu).
 cudaError_t launch_apply(int dtype, const ApplyArgs &a, int amps, int threads, int nsm,
@@ -213,6 +234,7 @@ struct CsrArgs {
     double *data;
     uint64_t row0, nrows;     // rows to fill
     int *err;                 // device error word (bad position => kErrCsrPos)
+    int wide;                 // 64-bit row words (the n > 32 kernels) forced (test hook)
 };
 cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st);
 cudaError_t launch_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,

@@ -500,7 +500,7 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
                 if ((size_t)a.nfold * R <= (size_t)kCsrThreads)
                     sm += (size_t)kCsrFvSlots * a.nfold * R * 16u;
             }
-            auto kern = a.n > 32 ? csr_fill_staged_kernel<true> : csr_fill_staged_kernel<false>;
+            auto kern = (a.n > 32 || a.wide) ? csr_fill_staged_kernel<true> : csr_fill_staged_kernel<false>;
             cudaError_t e0 =
                 cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             if (e0 != cudaSuccess) return e0;
@@ -524,7 +524,7 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
         const uint64_t nsig = a.G * (uint64_t)a.n;
         smem = nsig <= kCsrSmemSig ? (size_t)nsig * sizeof(int32_t) : 0;
     }
-    auto kern = a.n > 32 ? csr_fill_kernel<true> : csr_fill_kernel<false>;
+    auto kern = (a.n > 32 || a.wide) ? csr_fill_kernel<true> : csr_fill_kernel<false>;
     cudaError_t e0 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)(kCsrLutBytes + kCsrSmemCtab * sizeof(double2)) + 64);
     if (e0 != cudaSuccess) return e0;

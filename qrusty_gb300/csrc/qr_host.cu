@@ -12,9 +12,11 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <unordered_map>
 #include <utility>
@@ -27,6 +29,21 @@ namespace qr {
 
 static std::atomic<uint64_t> g_launches{0};
 void count_launch(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+cudaError_t ensure_dyn_smem(const void *fn, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> set;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_pair(dev, fn);
+    auto it = set.find(key);
+    if (it != set.end() && it->second >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) set[key] = bytes;
+    return e;
+}
 
 static thread_local std::string g_err;
 
@@ -103,8 +120,16 @@ struct Plan {
     DevBuf groups, tables, fat_z, fat_c, blk_hi, blk_g0, diag;
     // compensated-c64 kernel tables
     uint32_t nsub = 0, nruns = 0, nchunks = 0, npairs = 0;
-    DevBuf sub;
     DevBuf tdesc, tdata, blk_r0, run_g0, run_key, chunks;
+    // what the plan was built for, and its coefficient program: the slots
+    // that qr_op_set_coeffs_device recomputes on the device, with the
+    // diagonal's term list kept so that diag_wht can run again
+    int dtype = 0, adjoint = 0;
+    uint32_t nslots = 0;
+    DevBuf cslots, cmem, ccoord;
+    DevBuf dg_tz, dg_tc, dg_bz, dg_boff;
+    uint32_t dg_nbins = 0;
+    int dg_db = 0;
 };
 
 }  // namespace qr
@@ -145,6 +170,22 @@ struct qr_op {
     // host-call staging
     cudaStream_t hstream = nullptr;
     DevBuf stage_in, stage_out;
+    // bumped by every host coefficient update: a qr_batch built on this
+    // operator compares it with the value it recorded and rebuilds when they
+    // differ (device updates rewrite the built tables in place instead)
+    uint64_t coef_gen = 0;
+    // device coefficient updates (qr_op_set_coeffs_device): the last input,
+    // the merged-string fold lists, merged coefficients, adjoint signs and
+    // input phases on the device; host_coef_stale while cp / mc / tc on the
+    // host are older than d_coef
+    DevBuf d_coef, d_mc, d_mm_off, d_mm_terms, d_madj, d_cphase;
+    bool dev_coef_ready = false;
+    bool host_coef_stale = false;
+    // test hooks (qr_op_set_test_hooks): mbarrier wait bound (0 = default),
+    // withheld ring step (-1 = none), 64-bit row words forced
+    uint64_t test_wait_ns = 0;
+    int64_t test_withhold = -1;
+    int test_wide = 0;
 };
 
 namespace {
@@ -283,8 +324,15 @@ void build_csr_groups(const qr_op *op, std::vector<CsrGroup> &grp, std::vector<c
     }
 }
 
+int sync_host_coeffs(qr_op *op);
+
 int upload_csr_tables(qr_op *op) {
     if (op->csr_uploaded) return QR_OK;
+    {
+        const int rc = sync_host_coeffs(op);
+        if (rc) return rc;
+        if (op->csr_uploaded) return QR_OK;
+    }
     std::vector<CsrGroup> grp;
     std::vector<cd> ctab;
     std::vector<uint32_t> fold;
@@ -340,6 +388,52 @@ void merge_terms(qr_op *op) {
             c.im += op->cp[k].im;
         }
     }
+}
+
+// c'_k = m(phase_k) * c_k (make_params, qrusty/src/accel.rs:141-157: the
+// num-complex product, no FMA), the CSR-ordered copy, and the merged sums
+// (first term, then additions in input order, as merge_terms forms them).
+// Built plans are left as they are.
+void apply_host_coeffs(qr_op *op, const double *coeff) {
+    static const cd m[4] = {{1.0, 0.0}, {0.0, -1.0}, {-1.0, 0.0}, {0.0, 1.0}};
+    for (uint64_t k = 0; k < op->T; ++k) {
+        const cd a = m[op->ph[k] & 3];
+        const cd b{coeff[2 * k], coeff[2 * k + 1]};
+        op->cp[k].re = a.re * b.re - a.im * b.im;
+        op->cp[k].im = a.re * b.im + a.im * b.re;
+    }
+    for (uint64_t i = 0; i < op->T; ++i) op->tc[i] = op->cp[op->csr_order[i]];
+    op->csr_uploaded = false;
+    if (!op->mx.empty()) {
+        for (auto &c : op->mc) c = cd{0.0, 0.0};
+        std::vector<bool> seen(op->mx.size(), false);
+        for (uint64_t k = 0; k < op->T; ++k) {
+            const uint32_t mi = op->mmap[k];
+            if (!seen[mi]) {
+                op->mc[mi] = op->cp[k];
+                seen[mi] = true;
+            } else {
+                op->mc[mi].re += op->cp[k].re;
+                op->mc[mi].im += op->cp[k].im;
+            }
+        }
+    }
+}
+
+// After a device coefficient update the host copies (cp, tc, mc) are older
+// than the device ones: fetch the last device input (synchronous) before any
+// host-side use -- a plan built later, the CSR tables, the diagonal.
+int sync_host_coeffs(qr_op *op) {
+    if (!op->host_coef_stale) return QR_OK;
+    // the update ran on the caller's stream, which may not be ordered with
+    // the legacy stream: wait for the device
+    QR_CUDA(cudaDeviceSynchronize(), "fetch device coefficients: sync");
+    std::vector<double> c(2 * op->T);
+    QR_CUDA(cudaMemcpy(c.data(), op->d_coef.p, c.size() * sizeof(double), cudaMemcpyDeviceToHost),
+            "fetch device coefficients");
+    apply_host_coeffs(op, c.data());
+    op->host_coef_stale = false;
+    return QR_OK;
 }
 
 // GF(2) span of the z differences of one group: basis (pivot = msb, unique)
@@ -400,16 +494,44 @@ struct SubGroup {
     std::vector<cd> table; // 2^d entries
     std::vector<uint64_t> fz;
     std::vector<cd> fc;
+    // merged strings of the sub-group in fold order, each with its coordinate
+    // in the span basis (table entry u adds it with sign (-1)^popc(u & coord))
+    std::vector<uint32_t> mem;
+    std::vector<uint8_t> coord;
 };
 
 int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     Plan &pl = tile_bits < 0 ? op->plans[dtype][adjoint] : op->bplans[tile_bits];
     if (pl.built) return QR_OK;
+    {
+        const int rc = sync_host_coeffs(op);
+        if (rc) return rc;
+    }
     if (op->mx.empty()) merge_terms(op);
+    pl.dtype = dtype;
+    pl.adjoint = adjoint;
+    // coefficient program (see CoefSlot): members packed per slot
+    std::vector<CoefSlot> slots;
+    std::vector<uint32_t> cmem;
+    std::vector<uint8_t> ccoord;
+    auto add_slot = [&](uint64_t dst, const uint32_t *mem, const uint8_t *coord, size_t cnt,
+                        uint32_t d, uint8_t kind) {
+        CoefSlot sl;
+        sl.dst = dst;
+        sl.m0 = (uint32_t)cmem.size();
+        sl.cnt = (uint16_t)cnt;
+        sl.d = (uint8_t)d;
+        sl.kind = kind;
+        for (size_t k = 0; k < cnt; ++k) {
+            cmem.push_back(mem[k]);
+            ccoord.push_back(coord ? coord[k] : 0);
+        }
+        slots.push_back(sl);
+    };
     const int n = op->n;
     const bool f32 = dtype == QR_C64C;
     pl.b = tile_bits < 0 ? std::min(n, 12) : std::min(n, tile_bits);
-    const int tmax = !f32 ? 256 : (1 << (tile_bits < 0 ? kC64ThreadBits : kBatchThreadBits));
+    const int tmax = !f32 ? 256 : (1 << kC64ThreadBits);
     pl.threads = std::min(1 << pl.b, tmax);
     pl.amps = (1 << pl.b) / pl.threads;
     pl.tb = 0;
@@ -515,6 +637,10 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
                 sg.zm = (uint32_t)((sg.z0 & mmask) >> pl.tb);
                 for (size_t i = 0; i < sp.basis.size(); ++i) sg.beta[i] = sp.basis[i];
                 const uint32_t ent = 1u << sg.d;
+                for (size_t kk = 0; kk < part.size(); ++kk) {
+                    sg.mem.push_back((uint32_t)part[kk]);
+                    sg.coord.push_back((uint8_t)sp.coord[kk]);
+                }
                 for (uint32_t u = 0; u < ent; ++u) {
                     cd acc{0.0, 0.0};
                     for (size_t kk = 0; kk < part.size(); ++kk) {
@@ -535,6 +661,8 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
                 for (size_t k : part) {
                     sg.fz.push_back(op->mz[k]);
                     sg.fc.push_back(c[k]);
+                    sg.mem.push_back((uint32_t)k);
+                    sg.coord.push_back(0);
                 }
             }
             subs.push_back(std::move(sg));
@@ -672,7 +800,6 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     std::vector<uint64_t> fz;
     uint32_t ntab = 0, nfat_terms = 0;
     std::vector<GroupDesc> descs;           // c128 kernel
-    std::vector<SubDescC64> sd;             // c64c kernel
     pl.nfat = 0;
     for (size_t i = 0; i < ord.size(); ++i) {
         const SubGroup &sg = subs[ord[i]];
@@ -701,26 +828,6 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
             pl.nfat++;
         }
         descs.push_back(d);
-        if (f32) {
-            SubDescC64 c64;
-            memset(&c64, 0, sizeof(c64));
-            c64.z0 = sg.z0;
-            c64.lo = sg.lo;
-            const bool big = (sg.d == kFat) || sg.d > 2;
-            if (!big) {
-                c64.beta0 = sg.d > 0 ? sg.beta[0] : 0;
-                c64.beta1 = sg.d > 1 ? sg.beta[1] : 0;
-                for (size_t u = 0; u < sg.table.size(); ++u) {
-                    c64.tab[2 * u] = (float)sg.table[u].re;
-                    c64.tab[2 * u + 1] = (float)sg.table[u].im;
-                }
-                const uint32_t xm = ((sg.lo >> pl.tb) != 0) ? 1u : 0u;
-                c64.kind = (sg.zm & 15u) | (xm << 4) | (sg.d << 5);
-            } else {
-                c64.kind = 1u << 8;
-            }
-            sd.push_back(c64);
-        }
     }
     if (f32) {
         // per-tile-table kernel arrays
@@ -785,6 +892,13 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         }
         QR_CUDA(pl.tdesc.upload(td), "upload thread descriptors");
         QR_CUDA(pl.tdata.upload(tdd), "upload tile data");
+        for (size_t i = 0; i < ord.size(); ++i) {
+            const SubGroup &sg = subs[ord[i]];
+            if (sg.d == kFat || sg.d > 2 || sg.mem.size() > 0xffff)
+                return fail(QR_EINVAL, "plan: sub-group of rank > 2 in a complex64 plan");
+            add_slot((uint64_t)pl.tdata.p + i * sizeof(TileDataC64) + offsetof(TileDataC64, T),
+                     sg.mem.data(), sg.coord.data(), sg.mem.size(), sg.d, 0);
+        }
         // pair plans: bit 31 of a pair's first run marks a pair of exactly two
         // sub-groups with key 0 (no sign pattern, no register-bit XOR, factor
         // constant over the threads), which the kernel runs without the run
@@ -799,18 +913,27 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         QR_CUDA(pl.run_key.upload(rkey), "upload run keys");
         pl.nruns = (uint32_t)rkey.size();
         pl.nsub = (uint32_t)ord.size();
-        if (sd.empty()) {
-            SubDescC64 z;
-            memset(&z, 0, sizeof(z));
-            sd.push_back(z);
-        }
-        QR_CUDA(pl.sub.upload(sd), "upload sub-groups");
     }
-    if (descs.empty()) descs.push_back(GroupDesc{});  // keep a valid pointer
-    QR_CUDA(pl.groups.upload(descs), "upload groups");
-    QR_CUDA(pl.tables.upload(tab), "upload tables");
-    QR_CUDA(pl.fat_z.upload(fz), "upload fat z");
-    QR_CUDA(pl.fat_c.upload(fc), "upload fat c");
+    if (!f32) {  // the complex128 kernel's group descriptors, tables, term lists
+        if (descs.empty()) descs.push_back(GroupDesc{});  // keep a valid pointer
+        QR_CUDA(pl.groups.upload(descs), "upload groups");
+        QR_CUDA(pl.tables.upload(tab), "upload tables");
+        QR_CUDA(pl.fat_z.upload(fz), "upload fat z");
+        QR_CUDA(pl.fat_c.upload(fc), "upload fat c");
+        for (size_t i = 0; i < ord.size(); ++i) {
+            const SubGroup &sg = subs[ord[i]];
+            const GroupDesc &d = descs[i];
+            if (sg.d != kFat) {
+                if (sg.mem.size() > 0xffff) return fail(QR_EINVAL, "plan: group too large");
+                add_slot((uint64_t)pl.tables.p + (uint64_t)d.off * sizeof(Cplx<double>),
+                         sg.mem.data(), sg.coord.data(), sg.mem.size(), sg.d, 1);
+            } else {
+                for (size_t kk = 0; kk < sg.mem.size(); ++kk)
+                    add_slot((uint64_t)pl.fat_c.p + (uint64_t)(d.off + kk) * sizeof(Cplx<double>),
+                             &sg.mem[kk], nullptr, 1, 0, 2);
+            }
+        }
+    }
     QR_CUDA(pl.blk_hi.upload(bhi), "upload blocks");
     QR_CUDA(pl.blk_g0.upload(bg0), "upload block groups");
 
@@ -835,22 +958,35 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
             tcv.push_back(c[dt[i]].im);
         }
         boff.push_back((uint32_t)dt.size());
-        DevBuf d_tz, d_tc, d_bz, d_boff;
-        QR_CUDA(d_tz.upload(tz), "upload diag z");
-        QR_CUDA(d_tc.upload(tcv), "upload diag c");
-        QR_CUDA(d_bz.upload(bz), "upload diag bins");
-        QR_CUDA(d_boff.upload(boff), "upload diag bin offsets");
+        QR_CUDA(pl.dg_tz.upload(tz), "upload diag z");
+        QR_CUDA(pl.dg_tc.upload(tcv), "upload diag c");
+        QR_CUDA(pl.dg_bz.upload(bz), "upload diag bins");
+        QR_CUDA(pl.dg_boff.upload(boff), "upload diag bin offsets");
+        pl.dg_nbins = (uint32_t)bz.size();
+        pl.dg_db = db;
+        for (size_t i = 0; i < dt.size(); ++i) {
+            const uint32_t mi = (uint32_t)dt[i];
+            add_slot((uint64_t)pl.dg_tc.p + i * 2 * sizeof(double), &mi, nullptr, 1, 0, 2);
+        }
         const size_t esz = f32 ? sizeof(Cplx<float>) : sizeof(Cplx<double>);
         QR_CUDA(pl.diag.alloc(op->N * esz), "alloc diagonal");
-        QR_CUDA(launch_diag(dtype, n, db, op->N >> db, d_bz.as<uint64_t>(), d_boff.as<uint32_t>(),
-                            (uint32_t)bz.size(), d_tz.as<uint64_t>(), d_tc.as<double>(), pl.diag.p,
-                            nullptr),
+        QR_CUDA(launch_diag(dtype, n, db, op->N >> db, pl.dg_bz.as<uint64_t>(),
+                            pl.dg_boff.as<uint32_t>(), pl.dg_nbins, pl.dg_tz.as<uint64_t>(),
+                            pl.dg_tc.as<double>(), pl.diag.p, nullptr),
                 "diagonal kernel");
         QR_CUDA(cudaDeviceSynchronize(), "diagonal kernel sync");
     }
+    if (slots.empty()) slots.push_back(CoefSlot{});  // keep valid pointers
+    QR_CUDA(pl.cslots.upload(slots), "upload coefficient program");
+    QR_CUDA(pl.cmem.upload(cmem), "upload coefficient program members");
+    QR_CUDA(pl.ccoord.upload(ccoord), "upload coefficient program coordinates");
+    pl.nslots = cmem.empty() ? 0u : (uint32_t)slots.size();
     pl.built = true;
     return QR_OK;
 }
+
+// bound of every mbarrier wait of the apply kernels
+constexpr uint64_t kDefaultWaitNs = 2000000000ull;
 
 int check_device(const qr_op *op) {
     int dev = -1;
@@ -1015,6 +1151,7 @@ int qr_csr_build(qr_op *op, uint64_t *indptr, uint64_t *indices, double *data, i
     a.tz = op->d_tz.as<uint64_t>();
     a.tc = op->d_tc.as<double>();
     a.err = op->d_err.as<int>();
+    a.wide = op->test_wide;
     a.fvals = nullptr;
     // fold-mode values buffer (nfold x rows) for the staged fill; without
     // it the fold entries are stored in place after the fill
@@ -1118,7 +1255,6 @@ static int apply_impl(const char *name, qr_op *op, int32_t dtype, const void *ps
     a.diag = pl.has_diag ? pl.diag.p : nullptr;
     a.diag_block = pl.diag_block;
     a.err = op->d_err.as<int>();
-    a.sub = pl.sub.as<SubDescC64>();
     a.nsub = pl.nsub;
     a.tdesc = pl.tdesc.as<uint4>();
     a.tdata = pl.tdata.as<TileDataC64>();
@@ -1129,6 +1265,9 @@ static int apply_impl(const char *name, qr_op *op, int32_t dtype, const void *ps
     a.chunks = pl.chunks.as<uint4>();
     a.nchunks = pl.nchunks;
     a.npairs = pl.npairs;
+    a.wait_ns = op->test_wait_ns ? op->test_wait_ns : kDefaultWaitNs;
+    a.withhold = op->test_withhold;
+    a.wide = op->test_wide;
     a.v = v;
     if (v) {
         a.ar = alpha[0];
@@ -1288,33 +1427,86 @@ int qr_op_set_coeffs(qr_op *op, const double *coeff) {
     int rc = check_device(op);
     if (rc) return rc;
     QR_CUDA(cudaDeviceSynchronize(), "qr_op_set_coeffs sync");
-    static const cd m[4] = {{1.0, 0.0}, {0.0, -1.0}, {-1.0, 0.0}, {0.0, 1.0}};
-    for (uint64_t k = 0; k < op->T; ++k) {
-        const cd a = m[op->ph[k] & 3];
-        const cd b{coeff[2 * k], coeff[2 * k + 1]};
-        op->cp[k].re = a.re * b.re - a.im * b.im;
-        op->cp[k].im = a.re * b.im + a.im * b.re;
-    }
-    for (uint64_t i = 0; i < op->T; ++i) op->tc[i] = op->cp[op->csr_order[i]];
-    op->csr_uploaded = false;
-    if (!op->mx.empty()) {
-        for (auto &c : op->mc) c = cd{0.0, 0.0};
-        std::vector<bool> seen(op->mx.size(), false);
-        for (uint64_t k = 0; k < op->T; ++k) {
-            const uint32_t mi = op->mmap[k];
-            if (!seen[mi]) {
-                op->mc[mi] = op->cp[k];
-                seen[mi] = true;
-            } else {
-                op->mc[mi].re += op->cp[k].re;
-                op->mc[mi].im += op->cp[k].im;
-            }
-        }
-    }
+    apply_host_coeffs(op, coeff);
+    op->host_coef_stale = false;
     for (int d = 0; d < 2; ++d)
         for (int j = 0; j < 2; ++j) op->plans[d][j].built = false;
     // plans are rebuilt on next use into the buffers they already hold
     for (Plan &bp : op->bplans) bp.built = false;
+    ++op->coef_gen;
+    return QR_OK;
+}
+
+int qr_op_set_coeffs_device(qr_op *op, const double *coeff, void *stream) {
+    if (!op || !coeff) return fail(QR_EINVAL, "qr_op_set_coeffs_device: null argument");
+    int rc = check_device(op);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (!op->dev_coef_ready) {
+        // one-time (synchronous) upload of the fold structure: per merged
+        // string its input terms in input order, the adjoint sign
+        // parity(x & z), and the input phases
+        if (op->mx.empty()) merge_terms(op);
+        const size_t M = op->mx.size();
+        std::vector<uint32_t> off(M + 1, 0), terms(op->T);
+        for (uint64_t k = 0; k < op->T; ++k) ++off[op->mmap[k] + 1];
+        for (size_t i = 0; i < M; ++i) off[i + 1] += off[i];
+        std::vector<uint32_t> fill(off.begin(), off.end() - 1);
+        for (uint64_t k = 0; k < op->T; ++k) terms[fill[op->mmap[k]]++] = (uint32_t)k;
+        std::vector<uint8_t> adj(M);
+        for (size_t i = 0; i < M; ++i) adj[i] = __builtin_popcountll(op->mx[i] & op->mz[i]) & 1;
+        QR_CUDA(op->d_mm_off.upload(off), "upload merge offsets");
+        QR_CUDA(op->d_mm_terms.upload(terms), "upload merge terms");
+        QR_CUDA(op->d_madj.upload(adj), "upload adjoint signs");
+        QR_CUDA(op->d_cphase.upload(op->ph), "upload phases");
+        QR_CUDA(op->d_coef.alloc(op->T * 2 * sizeof(double)), "alloc device coefficients");
+        QR_CUDA(op->d_mc.alloc(M * sizeof(double2)), "alloc merged coefficients");
+        op->dev_coef_ready = true;
+    }
+    QR_CUDA(cudaMemcpyAsync(op->d_coef.p, coeff, op->T * 2 * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st),
+            "copy device coefficients");
+    QR_CUDA(launch_merge_coeffs((uint32_t)op->mx.size(), op->d_mm_off.as<uint32_t>(),
+                                op->d_mm_terms.as<uint32_t>(), op->d_coef.as<double2>(),
+                                op->d_cphase.as<uint8_t>(), op->d_mc.as<double2>(), st),
+            "merge coefficients");
+    auto refresh = [&](Plan &pl) -> int {
+        if (!pl.built) return QR_OK;
+        QR_CUDA(launch_coef_program(pl.cslots.as<CoefSlot>(), pl.nslots, pl.cmem.as<uint32_t>(),
+                                    pl.ccoord.as<uint8_t>(), op->d_mc.as<double2>(),
+                                    op->d_madj.as<uint8_t>(), pl.adjoint, st),
+                "coefficient program");
+        if (pl.has_diag)
+            QR_CUDA(launch_diag(pl.dtype, op->n, pl.dg_db, op->N >> pl.dg_db,
+                                pl.dg_bz.as<uint64_t>(), pl.dg_boff.as<uint32_t>(), pl.dg_nbins,
+                                pl.dg_tz.as<uint64_t>(), pl.dg_tc.as<double>(), pl.diag.p, st),
+                    "diagonal kernel");
+        return QR_OK;
+    };
+    for (int d = 0; d < 2; ++d)
+        for (int j = 0; j < 2; ++j) {
+            rc = refresh(op->plans[d][j]);
+            if (rc) return rc;
+        }
+    for (Plan &bp : op->bplans) {
+        rc = refresh(bp);
+        if (rc) return rc;
+    }
+    op->host_coef_stale = true;
+    op->csr_uploaded = false;
+    return QR_OK;
+}
+
+int qr_op_set_test_hooks(qr_op *op, uint32_t flags, uint64_t wait_ns, int64_t withhold_step) {
+    if (!op) return fail(QR_EINVAL, "qr_op_set_test_hooks: null operator");
+    if (flags & ~(uint32_t)QR_TEST_FORCE_WIDE)
+        return fail(QR_EINVAL, "qr_op_set_test_hooks: unknown flag bits 0x%x", flags);
+    if (wait_ns != 0 && wait_ns < 1000000ull)
+        return fail(QR_EINVAL, "qr_op_set_test_hooks: wait_ns below 1 ms");
+    if (withhold_step < -1) return fail(QR_EINVAL, "qr_op_set_test_hooks: withhold_step < -1");
+    op->test_wide = (flags & QR_TEST_FORCE_WIDE) ? 1 : 0;
+    op->test_wait_ns = wait_ns;
+    op->test_withhold = withhold_step;
     return QR_OK;
 }
 
@@ -1324,6 +1516,8 @@ int qr_vdot(int32_t n, int32_t dtype, const void *a, const void *b, int32_t nsta
     if (n < 1 || n > 40) return fail(QR_EINVAL, "qr_vdot: n=%d outside [1, 40]", n);
     if (dtype != QR_C128 && dtype != QR_C64C) return fail(QR_EINVAL, "qr_vdot: bad dtype");
     if (nstates < 1) return fail(QR_EINVAL, "qr_vdot: nstates=%d < 1", nstates);
+    // one grid row per state (gridDim.y)
+    if (nstates > 65535) return fail(QR_EINVAL, "qr_vdot: nstates=%d > 65535", nstates);
     int dev = 0, nsm = 0;
     QR_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     QR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "device attribute");
@@ -1345,6 +1539,7 @@ int qr_expect(qr_op *op, int32_t dtype, const void *psi, int32_t nstates, double
     if (!op || !psi || !out) return fail(QR_EINVAL, "qr_expect: null argument");
     if (dtype != QR_C128 && dtype != QR_C64C) return fail(QR_EINVAL, "qr_expect: bad dtype");
     if (nstates < 1) return fail(QR_EINVAL, "qr_expect: nstates=%d < 1", nstates);
+    if (nstates > 65535) return fail(QR_EINVAL, "qr_expect: nstates=%d > 65535", nstates);
     int rc = check_device(op);
     if (rc) return rc;
     const size_t esz = dtype == QR_C128 ? 16 : 8;
@@ -1397,6 +1592,9 @@ int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32
 
 }  // extern "C"
 
+// tile width of the persistent batched kernel: 512 threads x 8 amplitudes
+constexpr int kBatchTileBits = 12;
+
 struct qr_batch {
     static constexpr int kForks = 4;  // parallel branches of the per-operator graph
     int device = 0, nsm = 0;
@@ -1410,6 +1608,7 @@ struct qr_batch {
     std::vector<const void *> cur_psi;
     std::vector<void *> cur_y;
     bool ptrs_changed = false;
+    std::vector<uint64_t> gens;  // each operator's coef_gen when the graph was made
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t cap = nullptr;
@@ -1432,23 +1631,27 @@ int batch_build(qr_batch *bt, int tb) {
         BatchOp &o = bo[i];
         memset(&o, 0, sizeof(o));
         o.N = op->N;
+        o.ntiles = op->N >> pl.b;
         o.b = pl.b;
-        o.tb = pl.tb;
         o.mcount = pl.amps;
         o.tact = pl.threads;
-        o.ntiles = op->N >> pl.b;
+        o.diag_block = pl.diag_block;
         o.nblocks = pl.nblocks;
         o.nsub = pl.nsub;
-        o.diag_block = pl.diag_block;
-        o.sub = pl.sub.as<SubDescC64>();
-        o.groups = pl.groups.as<GroupDesc>();
-        o.tables = pl.tables.as<float2>();
-        o.fat_z = pl.fat_z.as<uint64_t>();
-        o.fat_c = pl.fat_c.as<float2>();
+        o.nruns = pl.nruns;
+        o.nchunks = pl.nchunks;
+        o.tdesc = pl.tdesc.as<uint4>();
+        o.tdata = pl.tdata.as<TileDataC64>();
         o.blk_hi = pl.blk_hi.as<uint64_t>();
-        o.blk_g0 = pl.blk_g0.as<uint32_t>();
+        o.blk_r0 = pl.blk_r0.as<uint32_t>();
+        o.run_g0 = pl.run_g0.as<uint32_t>();
+        o.run_key = pl.run_key.as<uint32_t>();
+        o.chunks = pl.chunks.as<uint4>();
         o.diag = pl.has_diag ? pl.diag.as<float2>() : nullptr;
-        cost.push_back({(double)(pl.nsub + 2 * pl.nblocks) * (double)(1u << pl.b), i});
+        // work per output tile: the sub-groups' inner steps plus per-block
+        // bookkeeping, over the tile's amplitudes
+        cost.push_back({(double)(pl.nsub + 2 * pl.nblocks + 4 * pl.nchunks) * (double)(1u << pl.b),
+                        i});
     }
     std::stable_sort(cost.begin(), cost.end(),
                      [](const std::pair<double, size_t> &a, const std::pair<double, size_t> &b) {
@@ -1478,6 +1681,7 @@ BatchArgs batch_args(qr_batch *bt) {
     a.psi = pp;
     a.y = pp + bt->ops.size();
     a.err = bt->d_err.as<int>();
+    a.wait_ns = kDefaultWaitNs;
     return a;
 }
 
@@ -1543,6 +1747,44 @@ int instantiate_per_op(qr_batch *bt) {
     if (rc) return rc;
     QR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0), "graph instantiate");
     return QR_OK;
+}
+
+// Graph of the one persistent work-list launch (tables of batch_build).
+int instantiate_persistent(qr_batch *bt) {
+    drop_graph(bt);
+    BatchArgs a = batch_args(bt);
+    QR_CUDA(cudaStreamBeginCapture(bt->cap, cudaStreamCaptureModeRelaxed), "begin capture");
+    cudaError_t e = launch_batch_c64c(a, bt->nsm, bt->cap);
+    cudaError_t e2 = cudaStreamEndCapture(bt->cap, &bt->graph);
+    if (e != cudaSuccess) return cuda_fail(e, "batch launch under capture");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
+    QR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0), "graph instantiate");
+    return QR_OK;
+}
+
+void record_gens(qr_batch *bt) {
+    bt->gens.resize(bt->ops.size());
+    for (size_t i = 0; i < bt->ops.size(); ++i) bt->gens[i] = bt->ops[i]->coef_gen;
+}
+
+// An operator's coefficients changed since the graph was made: its plan
+// tables are rebuilt (outside any capture) and the graph made again.
+int refresh_after_coeffs(qr_batch *bt, cudaStream_t st) {
+    bool stale = bt->gens.size() != bt->ops.size();
+    for (size_t i = 0; !stale && i < bt->ops.size(); ++i)
+        stale = bt->gens[i] != bt->ops[i]->coef_gen;
+    if (!stale) return QR_OK;
+    QR_CUDA(cudaStreamSynchronize(st), "qr_batch_apply sync before plan rebuild");
+    int rc = QR_OK;
+    if (bt->mode == 1) {
+        for (size_t i = 0; i < bt->ops.size() && !rc; ++i) rc = build_plan(bt->ops[i], QR_C64C, 0);
+        if (!rc) rc = instantiate_per_op(bt);
+    } else {
+        rc = batch_build(bt, bt->tile_bits);
+        if (!rc) rc = instantiate_persistent(bt);
+    }
+    if (!rc) record_gens(bt);
+    return rc;
 }
 
 }  // namespace
@@ -1615,6 +1857,10 @@ int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *s
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int rc = batch_upload_ptrs(bt, psi, y, st);
     if (rc) return rc;
+    if (bt->exec) {
+        rc = refresh_after_coeffs(bt, st);
+        if (rc) return rc;
+    }
     if (bt->exec && bt->mode == 1 && bt->ptrs_changed) {
         // per-operator graph nodes carry the state pointers: capture again
         rc = instantiate_per_op(bt);
@@ -1623,8 +1869,8 @@ int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *s
     bt->ptrs_changed = false;
     if (!bt->exec) {
         // autotuner: time each candidate on these buffers -- the persistent
-        // work-list kernel at tile widths 2^12, 2^11, 2^10, and a graph of
-        // one per-operator kernel each
+        // work-list kernel (4096-amplitude tiles) and a graph of one
+        // per-operator kernel each
         int best = -1;
         float best_ms = 0.f;
         cudaEvent_t e0, e1;
@@ -1640,20 +1886,14 @@ int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *s
             return e;
         };
         if (bt->force_mode != 1) {
-            for (int tb : {12, 11, 10}) {
-                rc = batch_build(bt, tb);
-                if (rc) break;
+            rc = batch_build(bt, kBatchTileBits);
+            if (!rc) {
                 BatchArgs a = batch_args(bt);
                 float ms = 0.f;
                 cudaError_t e = timed([&] { return launch_batch_c64c(a, bt->nsm, bt->cap); }, &ms);
-                if (e != cudaSuccess) {
-                    rc = cuda_fail(e, "qr_batch autotune");
-                    break;
-                }
-                if (best < 0 || ms < best_ms) {
-                    best = tb;
-                    best_ms = ms;
-                }
+                if (e != cudaSuccess) rc = cuda_fail(e, "qr_batch autotune");
+                best = kBatchTileBits;
+                best_ms = ms;
             }
         }
         if (!rc && bt->force_mode != 0) {
@@ -1679,18 +1919,12 @@ int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *s
             bt->mode = 1;
             bt->tile_bits = 12;
         } else {
-            drop_graph(bt);
             bt->mode = 0;
             rc = batch_build(bt, best);
+            if (!rc) rc = instantiate_persistent(bt);
             if (rc) return rc;
-            BatchArgs a = batch_args(bt);
-            QR_CUDA(cudaStreamBeginCapture(bt->cap, cudaStreamCaptureModeRelaxed), "begin capture");
-            cudaError_t e = launch_batch_c64c(a, bt->nsm, bt->cap);
-            cudaError_t e2 = cudaStreamEndCapture(bt->cap, &bt->graph);
-            if (e != cudaSuccess) return cuda_fail(e, "batch launch under capture");
-            if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
-            QR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0), "graph instantiate");
         }
+        record_gens(bt);
         QR_CUDA(cudaStreamSynchronize(bt->cap), "autotune sync");
         int h = 0;
         QR_CUDA(cudaMemcpy(&h, bt->d_err.p, sizeof(int), cudaMemcpyDeviceToHost), "error word");

@@ -256,6 +256,27 @@ class PauliOperator:
         check(_lib.load().qr_op_set_coeffs(self._h, c.ctypes.data))
         self._c = c
 
+    def set_coeffs_device(self, coeffs, stream=None):
+        """Replace the coefficients from a CUDA tensor (T values, real or
+        complex) without a host synchronisation: kernels on ``stream`` (the
+        current stream by default) rebuild every built plan's coefficient
+        tables in place (``qr_op_set_coeffs_device``)."""
+        import torch
+        if not (isinstance(coeffs, torch.Tensor) and coeffs.is_cuda):
+            raise TypeError("coeffs must be a CUDA tensor")
+        if coeffs.numel() != self.nterms:
+            raise ValueError("expected %d coefficients" % self.nterms)
+        c = coeffs.detach().reshape(-1)
+        if c.is_complex():
+            c = c.to(torch.complex128)
+        else:
+            c = torch.complex(c.to(torch.float64), torch.zeros_like(c, dtype=torch.float64))
+        c = c.contiguous()
+        st = stream if stream is not None else torch.cuda.current_stream(c.device).cuda_stream
+        check(_lib.load().qr_op_set_coeffs_device(self._h, c.data_ptr(), st))
+        self._c = None  # the host copy is no longer current
+        return c
+
     @staticmethod
     def _dtype_of(t):
         import torch
@@ -322,6 +343,13 @@ class PauliOperator:
         import torch
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         check(_lib.load().qr_check(self._h, st))
+
+    def set_test_hooks(self, force_wide=False, wait_ns=0, withhold_step=-1):
+        """Test-only knobs of ``qr_op_set_test_hooks``: 64-bit row-word
+        kernels at any n, a shorter mbarrier wait bound, and a ring step whose
+        partner copy CTA 0 never issues.  Defaults restore normal operation."""
+        flags = _lib.QR_TEST_FORCE_WIDE if force_wide else 0
+        check(_lib.load().qr_op_set_test_hooks(self._h, flags, int(wait_ns), int(withhold_step)))
 
 
 def _letters_masks(paulis):

@@ -293,7 +293,20 @@ def test_full_size_jw_properties(cuda, oracle):
         assert abs(y_h[r] - ref) <= 1e-12 * max(1e-300, float(np.abs(y_h).max())) * 10, r
     blk = oracle.apply_rows(t.x, t.z, cp, psi_h, 4096, 4096 + 512)
     assert rel(y_h[4096:4608], blk) <= TOL_C128
-    del psi_h, y_h
+    # a 65,536-row block (16 output tiles, unaligned start) against the FP64
+    # oracle: complex128 at 1e-12; compensated complex64 at 1e-6, both on
+    # the complex64-rounded state it was given (the kernel's own error) and
+    # on the FP64 state before rounding (what a caller converting sees)
+    lo = (0x2A5B << 12) + 777
+    hi = lo + 65536
+    ref = oracle.apply_rows(t.x, t.z, cp, psi_h, lo, hi)
+    assert rel(y_h[lo:hi], ref) <= TOL_C128
+    y64_h = y64.cpu().numpy()[lo:hi].astype(np.complex128)
+    assert rel(y64_h, ref) <= TOL_C64C
+    psi64_h = psi.to(torch.complex64).cpu().numpy().astype(np.complex128)
+    ref64 = oracle.apply_rows(t.x, t.z, cp, psi64_h, lo, hi)
+    assert rel(y64_h, ref64) <= TOL_C64C
+    del psi_h, y_h, psi64_h
     # linearity and Hermiticity
     phi = torch.complex(torch.randn(N, device=cuda, dtype=torch.float64, generator=g),
                         torch.randn(N, device=cuda, dtype=torch.float64, generator=g))

@@ -1,7 +1,8 @@
 """Batched H psi (one persistent, graph-replayed launch over many uneven
-operators) vs the per-operator kernels.  Tolerance: compensated-c64 results
-within 1e-6 relative of the per-operator complex128 results (themselves
-checked against the FP64 oracle in test_gpu_apply.py)."""
+operators).  Tolerance: compensated-c64 results within 1e-6 relative of the
+FP64 oracle (row blocks of every state of a dozen operators spanning every
+qubit count of the uneven workload), and of the per-operator complex128
+kernel for the rest."""
 import numpy as np
 import pytest
 
@@ -27,6 +28,42 @@ def make_batch(ops_terms, nstates, cuda, seed):
         psis.append(p.to(torch.complex64))
         ys.append(torch.empty_like(psis[-1]))
     return ops, psis, ys
+
+
+def check_against_oracle(oracle, terms, psis, ys, pick, rows=4096, seed=0):
+    """Rel. error of batched results against the FP64 oracle, per state, on
+    every row (2^n <= 2 rows) or on a random block of ``rows`` rows."""
+    rng = np.random.default_rng(seed)
+    worst = 0.0
+    for i in pick:
+        t = terms[i]
+        N = 1 << t.n
+        cp = oracle.make_params(t.phase, t.coeff)
+        P = psis[i].cpu().numpy().reshape(-1, N).astype(np.complex128)
+        Y = ys[i].cpu().numpy().reshape(-1, N).astype(np.complex128)
+        for s in range(P.shape[0]):
+            lo = 0 if N <= 2 * rows else int(rng.integers(0, N - rows))
+            hi = N if N <= 2 * rows else lo + rows
+            ref = oracle.apply_rows(t.x, t.z, cp, P[s], lo, hi)
+            e = float(np.linalg.norm(Y[s, lo:hi] - ref) / np.linalg.norm(ref))
+            worst = max(worst, e)
+    return worst
+
+
+def spread_pick(terms):
+    """One operator per qubit count (smallest and largest term count for the
+    two extreme qubit counts): a dozen or more operators of the workload."""
+    by_n = {}
+    for i, t in enumerate(terms):
+        by_n.setdefault(t.n, []).append(i)
+    pick = []
+    ns = sorted(by_n)
+    for n in ns:
+        idx = sorted(by_n[n], key=lambda i: terms[i].T)
+        pick.append(idx[-1])
+        if n in (ns[0], ns[-1]) and len(idx) > 1:
+            pick.append(idx[0])
+    return pick
 
 
 def check_against_c128(ops, psis, ys):
@@ -88,11 +125,49 @@ def test_batch_matches_single_operator_kernel(cuda):
     assert rel(ys[0], single.to(torch.complex128)) <= 1e-6
 
 
-def test_batch_uneven_workload(cuda):
+def test_batch_uneven_workload(cuda, oracle):
     """The uneven batch workload: 256 operators, n ~ U{10..20}, T ~ U{50..5000}
-    random-letter terms, 8 states each, one launch."""
+    random-letter terms, 8 states each, one launch; a dozen operators against
+    the oracle, every state, the rest against the complex128 kernel."""
     terms = W.cfg3()
     ops, psis, ys = make_batch(terms, [8] * len(terms), cuda, 3)
     b = Batch(ops, [8] * len(terms))
     b.apply(psis, ys)
+    pick = spread_pick(terms)
+    assert len(pick) >= 12 and len({terms[i].n for i in pick}) == 11
+    assert check_against_oracle(oracle, terms, psis, ys, pick) <= 1e-6
     assert check_against_c128(ops, psis, ys) <= 1e-6
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_batch_forms_vs_oracle(cuda, oracle, mode):
+    """Each launch form, forced, on a dozen operators of the uneven workload
+    (every qubit count) against the FP64 oracle, every state."""
+    terms = W.cfg3()
+    pick = spread_pick(terms)
+    sub = [terms[i] for i in pick]
+    ops, psis, ys = make_batch(sub, [8] * len(sub), cuda, 11)
+    b = Batch(ops, [8] * len(sub))
+    b.set_mode(mode)
+    b.apply(psis, ys)
+    assert b.mode == mode
+    assert check_against_oracle(oracle, sub, psis, ys, range(len(sub))) <= 1e-6
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_batch_after_set_coeffs(cuda, oracle, mode):
+    """A coefficient update of one operator reaches the batch's next apply."""
+    import torch
+    rng = np.random.default_rng(5)
+    terms = [W.random_letters_op(rng, int(rng.integers(10, 15)), int(rng.integers(50, 700)))
+             for _ in range(6)]
+    ops, psis, ys = make_batch(terms, [2] * len(terms), cuda, 12)
+    b = Batch(ops, [2] * len(terms))
+    b.set_mode(mode)
+    b.apply(psis, ys)
+    assert check_against_oracle(oracle, terms, psis, ys, range(len(terms))) <= 1e-6
+    terms[2].coeff = terms[2].coeff * -0.5 + 0.25j
+    ops[2].set_coeffs(terms[2].coeff)
+    b.apply(psis, ys)
+    torch.cuda.synchronize()
+    assert check_against_oracle(oracle, terms, psis, ys, range(len(terms))) <= 1e-6

@@ -281,3 +281,35 @@ def test_spmv_skips_out_of_range_columns(cuda):
     got = y.cpu().numpy()
     assert np.all(np.isfinite(got))
     assert np.allclose(got, want, rtol=1e-12, atol=1e-12)
+
+
+def test_chain22_sampled_rows_vs_make_row(cuda, oracle):
+    """The chain at its benchmark size, n = 22 (G = 44, 1.85e8 stored
+    entries, built on the device by the staged bulk-store kernel with the
+    fold-value buffer for the x = 0 group of 21 ZZ bonds): about 200 rows
+    spread over every region of the matrix against make_row
+    (qrusty/src/accel.rs:171-210) restated by the oracle, bit for bit."""
+    import torch
+    t, _ = W.cfg1(with_state=False, n=22)
+    op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
+    nr, nz = op.csr_size()
+    G = nz // nr
+    assert G == 44
+    ip, ij, dd = op.csr_device()
+    torch.cuda.synchronize()
+    op.sync_check()
+    rng = np.random.default_rng(22)
+    rows = np.unique(np.concatenate([
+        [0, 1, 15, 16, 255, 256, nr // 2, nr - 2, nr - 1],
+        rng.integers(0, nr, 190)])).astype(np.int64)
+    r_dev = torch.from_numpy(rows).to(cuda)
+    assert torch.equal(ip[r_dev], r_dev * G)
+    assert int(ip[-1]) == nz
+    pos = (r_dev[:, None] * G + torch.arange(G, device=cuda)[None, :]).reshape(-1)
+    cols = ij[pos].cpu().numpy().view(np.uint64).reshape(len(rows), G)
+    vals = dd[pos].cpu().numpy().reshape(len(rows), G)
+    cp = oracle.make_params(t.phase, t.coeff)
+    for k, r in enumerate(rows.tolist()):
+        oc, ov = oracle.make_row(t.x, t.z, cp, r)
+        assert np.array_equal(cols[k], oc), r
+        assert np.array_equal(_bits(vals[k]), _bits(ov)), r

@@ -72,3 +72,32 @@ def test_noalloc_rejects_beyond_capacity(cuda):
     rc = _call(L.qr_vdot_noalloc, n, _lib.QR_C128, a, a, ns, out)
     assert rc == _lib.QR_EINVAL
     assert "QR_VDOT_NOALLOC_MAX_PARTIALS" in _lib.last_error()
+
+
+@pytest.mark.parametrize("n,ns,dtype", [(18, 512, "c64"), (4, MAX_PARTIALS, "c128")])
+def test_noalloc_capped_block_count(cuda, n, ns, dtype):
+    """Many states: the per-state block count is cut so that nstates x blocks
+    fits the fixed array (n = 18, 512 states: 64 blocks per state cut to 32;
+    n = 4, 16,384 states: exactly QR_VDOT_NOALLOC_MAX_PARTIALS partial sums).
+    Only the summation order differs from qr_vdot."""
+    import torch
+    L = _lib.load()
+    g = torch.Generator(device=cuda).manual_seed(3)
+    tdt = torch.complex64 if dtype == "c64" else torch.complex128
+    rdt = torch.float32 if dtype == "c64" else torch.float64
+    code = _lib.QR_C64C if dtype == "c64" else _lib.QR_C128
+    N = 1 << n
+    a = torch.complex(torch.randn(ns * N, device=cuda, dtype=rdt, generator=g),
+                      torch.randn(ns * N, device=cuda, dtype=rdt, generator=g)).to(tdt)
+    b = torch.complex(torch.randn(ns * N, device=cuda, dtype=rdt, generator=g),
+                      torch.randn(ns * N, device=cuda, dtype=rdt, generator=g)).to(tdt)
+    want = torch.empty(ns, dtype=torch.complex128, device=cuda)
+    _lib.check(_call(L.qr_vdot, n, code, a, b, ns, want))
+    for _ in range(2):
+        got = torch.full((ns,), complex("nan"), dtype=torch.complex128, device=cuda)
+        _lib.check(_call(L.qr_vdot_noalloc, n, code, a, b, ns, got))
+        d = (got - want).abs()
+        assert bool(torch.all(torch.isfinite(got)))
+        assert float(d.max()) <= 1e-12 * float(want.abs().max()) * 10
+        assert float(torch.linalg.vector_norm(got - want)) <= 1e-12 * float(
+            torch.linalg.vector_norm(want))
