@@ -129,7 +129,9 @@ int qr_check(qr_op *op, void *stream);
  * staging buffer and applies.  When y is page-locked host memory
  * (cudaHostAlloc / cudaHostRegister) the kernel writes each output tile
  * straight into it, overlapping the write-back with the computation;
- * otherwise y goes to a device staging buffer and is copied back.  Staging
+ * otherwise y goes to a device staging buffer and is copied back.  With
+ * several states whose host ranges of psi and y do not overlap, the copy of
+ * state s + 1 runs on a second stream while state s is computed.  Staging
  * buffers are owned by the operator and reused across calls. */
 int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host,
                   int32_t nstates, int32_t adjoint);

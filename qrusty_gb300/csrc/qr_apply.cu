@@ -142,7 +142,7 @@ __device__ __forceinline__ Cplx<Real> cneg_if(const Cplx<Real> &d, uint32_t s) {
 // ---------------------------------------------------------------- apply kernel
 // Real = float (compensated) or double (plain).  AMPS amplitudes per thread.
 template <typename Real, int AMPS, bool COMP>
-__global__ void __launch_bounds__(COMP ? 512 : 256, 1) apply_tiled(const ApplyArgs a, int stages) {
+__global__ void __launch_bounds__(512, 1) apply_tiled(const ApplyArgs a, int stages) {
     using C = Cplx<Real>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t threads = blockDim.x;
@@ -1096,9 +1096,13 @@ static cudaError_t launch_c64c(const ApplyArgs &a, int threads, int nsm, cudaStr
 // run of sub-groups with equal key is one dispatch.  512 threads x 8
 // amplitudes; an operator with n < 12 has tiles of 2^n amplitudes, held by
 // threads t < tact and register indices m < mcount (the other lanes compute
-// on in-bounds shared memory and store nothing).  The lane that releases a
-// stage walks the work list kTabStages steps ahead to find the tile it
-// loads next.
+// on in-bounds shared memory and store nothing).  Every warp passes the
+// barrier at an item's start, so the item and its operator -- and the CTA's
+// next item -- are copied into shared memory there: the steady state reads
+// them with shared loads, and the lane that releases a stage finds the tile
+// it loads next, kTabStages steps ahead, by arithmetic on those copies (a
+// walk of the work list in global memory only when the lookahead crosses
+// more than one item).
 __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchArgs a) {
     constexpr int AMPS = 8;
     constexpr uint32_t kStageBytes = 4096u * 8u;
@@ -1120,6 +1124,10 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
     uint32_t *s_blk = s_run + kTabCap + 1;
     const uint32_t stride = gridDim.x;
     if (blockIdx.x >= a.nitems) return;
+    // [0]: the current item and its operator, [1]: the CTA's next item
+    __shared__ BatchOp s_op[2];
+    __shared__ BatchItem s_it[2];
+    __shared__ const float2 *s_src[2];
 
     // step cursor (work-list index, block of that item's operator) -> next step
     auto advance = [&](uint32_t &ik, uint32_t &j) {
@@ -1158,11 +1166,15 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
     float2 *mylo = s_lo + t;
     uint32_t ik = blockIdx.x, j = 0, s = 0, par = 0;
     uint32_t cidx = 0, cj0 = 0, next_j = 0;  // table chunk, its first block, the next's
+    const BatchOp &o = s_op[0];
+    const BatchItem &it = s_it[0];
+    // the current item's scalars, kept in registers from its first chunk on:
+    // tile, block count, x = 0 block, tile bits | threads used << 8 |
+    // amplitudes used << 20
+    uint64_t q = 0;
+    uint32_t nb = 1, geo = 0;
+    int dblk = -1;
     while (ik < a.nitems) {
-        const BatchItem it = a.items[ik];
-        const BatchOp &o = a.ops[it.op];
-        const uint64_t q = it.tile;
-        const uint32_t tact = (uint32_t)o.tact, mcount = (uint32_t)o.mcount;
         if (j == 0) {
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
@@ -1170,6 +1182,17 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
                 mylo[m * threads] = make_float2(0.f, 0.f);
             }
             cidx = 0;
+            // every warp is done with the last item (its releases included)
+            __syncthreads();
+            if (t < 2) {
+                const uint32_t ikx = ik + t * stride;
+                if (ikx < a.nitems) {
+                    const BatchItem itx = a.items[ikx];
+                    s_it[t] = itx;
+                    s_op[t] = a.ops[itx.op];
+                    s_src[t] = a.psi[itx.op] + (uint64_t)itx.state * a.ops[itx.op].N;
+                }
+            }
         }
         if (j == 0 || j == next_j) {
             // table, descriptors and run lists of the chunk starting at block
@@ -1185,18 +1208,24 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
                 s_run[i] = (o.run_g0[r] - c0.x) | (r < o.nruns ? o.run_key[r] << 16 : 0u);
             }
             for (uint32_t i = t; i <= c1.z - c0.z; i += threads) s_blk[i] = o.blk_r0[c0.z + i] - c0.y;
+            const uint64_t qt = it.tile;
             for (uint32_t gi = t; gi < c1.x - c0.x; gi += threads) {
                 const TileDataC64 &d = o.tdata[c0.x + gi];
-                const uint32_t uq = parity<false>(q, d.b0h) | (parity<false>(q, d.b1h) << 1);
-                const float sq = parity<false>(q, d.z0h) ? -1.f : 1.f;
+                const uint32_t uq = parity<false>(qt, d.b0h) | (parity<false>(qt, d.b1h) << 1);
+                const float sq = parity<false>(qt, d.z0h) ? -1.f : 1.f;
 #pragma unroll
                 for (uint32_t u = 0; u < 4; ++u) {
                     const float2 v = d.T[u ^ uq];
                     s_tab[gi * 4 + u] = make_float4(sq * v.x, sq * v.x, sq * v.y, sq * v.y);
                 }
             }
+            q = qt;
+            nb = o.nblocks;
+            dblk = o.diag_block;
+            geo = (uint32_t)o.b | ((uint32_t)o.tact << 8) | ((uint32_t)o.mcount << 20);
             __syncthreads();
         }
+        const uint32_t ob = geo & 0xffu, tact = (geo >> 8) & 0xfffu, mcount = geo >> 20;
         // an expired wait sets the abort flag; from then on every warp skips
         // waits and work but still reaches each chunk barrier
         bool skip = *s_abort != 0;
@@ -1210,8 +1239,8 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
         skip = __any_sync(0xffffffffu, skip);
         const uint32_t soff = s * kStageBytes;
 
-        if (!skip && (int)j == o.diag_block && o.diag != nullptr) {
-            const float2 *dg = o.diag + (q << o.b);
+        if (!skip && (int)j == dblk && o.diag != nullptr) {
+            const float2 *dg = o.diag + (q << ob);
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
                 if (t < tact && (uint32_t)m < mcount) {
@@ -1234,7 +1263,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
             rw = rn;
         }
 
-        const bool last = (j == o.nblocks - 1);
+        const bool last = (j == nb - 1);
         if (last || (j % kFlush) == kFlush - 1) {
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
@@ -1247,7 +1276,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
             }
         }
         if (last && t < tact) {
-            float2 *yo = a.y[it.op] + (uint64_t)it.state * o.N + (q << o.b);
+            float2 *yo = a.y[it.op] + (uint64_t)it.state * o.N + (q << ob);
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
                 if ((uint32_t)m < mcount) {
@@ -1265,11 +1294,30 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
             if (old == nwarps - 1) {
                 cnt[s] = 0;
                 if (*s_abort == 0) {
-                    uint32_t ik2 = ik, j2 = j;
-                    for (int k = 0; k < kTabStages && ik2 < a.nitems; ++k) advance(ik2, j2);
-                    if (ik2 < a.nitems) {
+                    // the step kTabStages ahead: in this item, in the next
+                    // one (shared copies), or further (walk the list)
+                    uint32_t jf = j + (uint32_t)kTabStages;
+                    int which = 0;
+                    if (jf >= nb) {
+                        jf -= nb;
+                        which = (ik + stride < a.nitems && jf < s_op[1].nblocks) ? 1 : -1;
+                    }
+                    if (which >= 0) {
+                        const BatchOp &fo = s_op[which];
+                        const uint32_t bytes = (1u << fo.b) * 8u;
+                        const float2 *src =
+                            s_src[which] + (((uint64_t)s_it[which].tile ^ fo.blk_hi[jf]) << fo.b);
                         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                        issue(ik2, j2, s);
+                        ++s_iss[s];
+                        mbar_expect_tx(&full[s], bytes);
+                        bulk_g2s(smem_raw + (size_t)s * kStageBytes, src, bytes, &full[s]);
+                    } else {
+                        uint32_t ik2 = ik, j2 = j;
+                        for (int k = 0; k < kTabStages && ik2 < a.nitems; ++k) advance(ik2, j2);
+                        if (ik2 < a.nitems) {
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                            issue(ik2, j2, s);
+                        }
                     }
                 }
             }
@@ -1278,7 +1326,10 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_batch(const BatchAr
             s = 0;
             par ^= 1u;
         }
-        advance(ik, j);
+        if (++j == nb) {  // the item's block count (register): no load per step
+            j = 0;
+            ik += stride;
+        }
     }
     // drain after an expired wait, as in apply_c64c_tab
     __syncthreads();

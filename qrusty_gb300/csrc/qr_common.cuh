@@ -36,6 +36,7 @@ struct alignas(16) TileDataC64 {
     uint64_t z0h, b0h, b1h, pad;
     float2 T[4];
 };
+static_assert(sizeof(TileDataC64) == 64, "TileDataC64 is read as four 16-byte words");
 
 struct ApplyArgs {
     const void *psi;

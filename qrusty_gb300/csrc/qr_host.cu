@@ -169,6 +169,8 @@ struct qr_op {
     DevBuf d_err;
     // host-call staging
     cudaStream_t hstream = nullptr;
+    cudaStream_t cstream = nullptr;  // host-call copies of states 1.. (overlap)
+    cudaEvent_t cev = nullptr;
     DevBuf stage_in, stage_out;
     // bumped by every host coefficient update: a qr_batch built on this
     // operator compares it with the value it recorded and rebuilds when they
@@ -531,7 +533,7 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     const int n = op->n;
     const bool f32 = dtype == QR_C64C;
     pl.b = tile_bits < 0 ? std::min(n, 12) : std::min(n, tile_bits);
-    const int tmax = !f32 ? 256 : (1 << kC64ThreadBits);
+    const int tmax = !f32 ? 512 : (1 << kC64ThreadBits);
     pl.threads = std::min(1 << pl.b, tmax);
     pl.amps = (1 << pl.b) / pl.threads;
     pl.tb = 0;
@@ -1080,6 +1082,8 @@ int qr_op_destroy(qr_op *op) {
     const int home = op->device;
     if (dev != home) cudaSetDevice(home);
     if (op->hstream) cudaStreamDestroy(op->hstream);
+    if (op->cstream) cudaStreamDestroy(op->cstream);
+    if (op->cev) cudaEventDestroy(op->cev);
     delete op;
     if (dev >= 0 && dev != home) cudaSetDevice(dev);
     return QR_OK;
@@ -1322,6 +1326,35 @@ int qr_apply_host(qr_op *op, int32_t dtype, const void *psi_host, void *y_host, 
     cudaGetLastError();  // a pageable pointer may leave a benign error behind
     if (!y_dev && op->stage_out.bytes < bytes)
         QR_CUDA(op->stage_out.alloc(bytes), "alloc y staging");
+    const char *pb = static_cast<const char *>(psi_host);
+    char *yb = static_cast<char *>(y_host);
+    if (nstates > 1 && (pb + bytes <= yb || yb + bytes <= pb)) {
+        // Several states, psi and y apart: state s + 1 is copied in on a
+        // second stream while the kernel works on state s (an event orders
+        // each state's kernel after its copy), so only the first copy is
+        // not hidden.
+        if (!op->cstream)
+            QR_CUDA(cudaStreamCreateWithFlags(&op->cstream, cudaStreamNonBlocking), "create stream");
+        if (!op->cev) QR_CUDA(cudaEventCreateWithFlags(&op->cev, cudaEventDisableTiming), "event");
+        const uint64_t b1 = op->N * esz;
+        char *in = static_cast<char *>(op->stage_in.p);
+        char *out = static_cast<char *>(y_dev ? y_dev : op->stage_out.p);
+        for (int32_t st = 0; st < nstates; ++st) {
+            QR_CUDA(cudaMemcpyAsync(in + st * b1, pb + st * b1, b1, cudaMemcpyHostToDevice,
+                                    op->cstream),
+                    "copy psi to device");
+            QR_CUDA(cudaEventRecord(op->cev, op->cstream), "record copy");
+            QR_CUDA(cudaStreamWaitEvent(op->hstream, op->cev, 0), "order apply after copy");
+            rc = qr_apply(op, dtype, in + st * b1, out + st * b1, 1, adjoint, op->hstream);
+            if (rc) return rc;
+            if (!y_dev)
+                QR_CUDA(cudaMemcpyAsync(yb + st * b1, out + st * b1, b1, cudaMemcpyDeviceToHost,
+                                        op->hstream),
+                        "copy y to host");
+        }
+        QR_CUDA(cudaStreamSynchronize(op->hstream), "apply_host sync");
+        return check_kernel_error(op);
+    }
     QR_CUDA(cudaMemcpyAsync(op->stage_in.p, psi_host, bytes, cudaMemcpyHostToDevice, op->hstream),
             "copy psi to device");
     rc = qr_apply(op, dtype, op->stage_in.p, y_dev ? y_dev : op->stage_out.p, nstates, adjoint,

@@ -225,6 +225,13 @@ def test_host_entry_matches_device(cuda):
     yh64 = op.apply(psi.astype(np.complex64))
     yd64 = op.apply(torch.from_numpy(psi).to(cuda).to(torch.complex64)).cpu().numpy()
     assert np.array_equal(yh64, yd64)
+    # three pageable states: per-state copies overlapped with the kernels
+    psi3 = W.random_state(np.random.default_rng(4), 1 << t.n, nstates=3).reshape(-1)
+    for dt in (np.complex128, np.complex64):
+        p = psi3.astype(dt)
+        yh3 = op.apply(p)
+        yd3 = op.apply(torch.from_numpy(p).to(cuda)).cpu().numpy()
+        assert np.array_equal(yh3, yd3)
 
 
 @pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
