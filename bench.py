@@ -658,7 +658,10 @@ def measure_batch(steps=3, warmup=3, per_op=True):
     out = {"workload": "256 operators, n ~ U{10..20}, T ~ U{50..5000} random letters (seed %d), "
                        "8 complex64 states each" % (W.SEED0 + 3),
            "ms_per_step": ms_b, "value": units / (ms_b / 1e3), "unit": UNIT,
-           "mode": "persistent work-list kernel" if b.mode == 0 else "graph of per-operator kernels",
+           "mode": {0: "persistent work-list kernel", 1: "graph of per-operator kernels",
+                    2: "persistent kernel for the small operators + per-operator kernels"}
+                   .get(b.mode, str(b.mode)),
+           "mode_code": b.mode,
            "tile_bits": b.tile_bits, "gpu_launches_per_step": launches,
            "roofline": _roof(alg, ms_b, hbm, peak_kind,
                              "sum over ops of (P+1)*states*2^n*8"),

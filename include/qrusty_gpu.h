@@ -246,10 +246,12 @@ int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32
  * qr_batch_apply: psi[i] / y[i] are device pointers to operator i's
  * nstates[i] complex64 states (back to back).  The first call times, on the
  * given buffers (y is overwritten), (a) one persistent kernel over a work list
- * of (operator, state, amplitude tile) items and (b) a graph of one apply
- * kernel per operator on four parallel branches, keeps the faster and
- * captures it into a CUDA graph; every call launches that graph on
- * `stream`.  A call whose pointers differ from the
+ * of (operator, state, amplitude tile) items, (b) a graph of one apply
+ * kernel per operator on four parallel branches and, when the batch has
+ * both, (c) the persistent kernel over the small operators (fewer work items
+ * than half the SMs) beside per-operator kernels for the large ones; it
+ * keeps the fastest, captured in a CUDA graph, and every call launches that
+ * graph on `stream`.  A call whose pointers differ from the
  * previous call's synchronises `stream` first (and, for (b), captures the
  * graph again). */
 typedef struct qr_batch qr_batch;
@@ -257,8 +259,9 @@ int qr_batch_create(int32_t nops, qr_op *const *ops, const int32_t *nstates, qr_
 int qr_batch_destroy(qr_batch *b);
 int qr_batch_apply(qr_batch *b, const void *const *psi, void *const *y, void *stream);
 /* Mode the first apply chose: 0 persistent work-list kernel, 1 graph of
- * per-operator kernels; -1 before the first apply.  qr_batch_set_mode fixes
- * it instead (-1 restores the choice by timing); only before the first apply. */
+ * per-operator kernels, 2 both (form (c) above); -1 before the first apply.
+ * qr_batch_set_mode fixes it instead (-1 restores the choice by timing);
+ * only before the first apply. */
 int qr_batch_mode(const qr_batch *b);
 int qr_batch_set_mode(qr_batch *b, int32_t mode);
 /* Tile width the autotuner chose (log2 amplitudes; 0 before the first apply). */

@@ -460,6 +460,35 @@ __device__ __forceinline__ void run_tab(float2 (&A)[AMPS], float2 (&B)[AMPS],
     if (g < g1) sub_tab_one<AMPS, ZM, XM, TV>(A, B, sm, soff, s_tab, tdesc, g, t, t8);
 }
 
+// A pair of key-0 sub-groups g, g+1 in halves 0 and 1 of the slot whose x
+// masks leave the partner tiles unpermuted: each has one factor for every
+// thread and amplitude (table entry u = 0), and amplitude m of thread t sits
+// at a fixed offset from t * 8 in its half -- no descriptor, no address
+// arithmetic.  Same products in the same order as two sub_tab_one calls.
+template <int AMPS>
+__device__ __forceinline__ void cheap_pair_lo0(float2 (&A)[AMPS], float2 (&B)[AMPS],
+                                               const unsigned char *sm, uint32_t base,
+                                               const float4 *s_tab, uint32_t g) {
+    const float4 Ta = s_tab[g * 4], Tb = s_tab[(g + 1) * 4];
+    const unsigned char *h0 = sm + base;
+    const unsigned char *h1 = h0 + 32768u;
+    float2 p[AMPS];
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) p[m] = *reinterpret_cast<const float2 *>(h0 + ((uint32_t)m << kMsh));
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        A[m] = __ffma2_rn(make_float2(Ta.x, Ta.y), p[m], A[m]);
+        B[m] = __ffma2_rn(make_float2(Ta.z, Ta.w), p[m], B[m]);
+    }
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) p[m] = *reinterpret_cast<const float2 *>(h1 + ((uint32_t)m << kMsh));
+#pragma unroll
+    for (int m = 0; m < AMPS; ++m) {
+        A[m] = __ffma2_rn(make_float2(Tb.x, Tb.y), p[m], A[m]);
+        B[m] = __ffma2_rn(make_float2(Tb.z, Tb.w), p[m], B[m]);
+    }
+}
+
 // Two sub-groups g, g+1 of one x group (same partner amplitudes) whose
 // register-bit sign patterns are ZM and ZM ^ (1 << BB): an x group split
 // because its terms' z differ on one register bit.  One set of partner loads
@@ -965,15 +994,21 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
             }
         }
 
-        // bit 31 of a pair's first run: exactly two sub-groups of key 0
+        // bit 31 of a pair's first run: exactly two sub-groups of key 0; bit
+        // 30: in halves 0 and 1, partner tiles unpermuted
         const uint32_t bw = s_blk[p];
-        const uint32_t rb = bw & 0x7fffffffu;
+        const uint32_t rb = bw & 0x3fffffffu;
         if (!skip && (bw >> 31) != 0) {
             const uint32_t g0 = s_run[rb] & 0xffffu;
-            sub_tab_one<AMPS, 0, false, false>(A, B, smem_raw, soff, s_tab, tdesc, g0, t, t8);
-            sub_tab_one<AMPS, 0, false, false>(A, B, smem_raw, soff, s_tab, tdesc, g0 + 1, t, t8);
+            if ((bw >> 30) & 1u) {
+                cheap_pair_lo0<AMPS>(A, B, smem_raw, soff | t8, s_tab, g0);
+            } else {
+                sub_tab_one<AMPS, 0, false, false>(A, B, smem_raw, soff, s_tab, tdesc, g0, t, t8);
+                sub_tab_one<AMPS, 0, false, false>(A, B, smem_raw, soff, s_tab, tdesc, g0 + 1, t,
+                                                   t8);
+            }
         } else {
-            const uint32_t r1 = skip ? 0u : (s_blk[p + 1] & 0x7fffffffu);
+            const uint32_t r1 = skip ? 0u : (s_blk[p + 1] & 0x3fffffffu);
             uint32_t rw = s_run[rb];
             for (uint32_t r = rb; r < r1; ++r) {
                 const uint32_t rn = s_run[r + 1];

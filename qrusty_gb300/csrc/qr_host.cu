@@ -904,11 +904,19 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         // pair plans: bit 31 of a pair's first run marks a pair of exactly two
         // sub-groups with key 0 (no sign pattern, no register-bit XOR, factor
         // constant over the threads), which the kernel runs without the run
-        // list
+        // list; bit 30 in addition when the two sit in halves 0 and 1 and
+        // neither permutes the partner tile (x & (tile - 1) == 0), so that
+        // their partner offsets are known at compile time
         if (pl.npairs) {
-            for (uint32_t j = 0; j < pl.npairs; ++j)
-                if (pg0[j + 1] - pg0[j] == 2 && pkey[pg0[j]] == 0 && pkey[pg0[j] + 1] == 0)
+            for (uint32_t j = 0; j < pl.npairs; ++j) {
+                const uint32_t a0 = pg0[j], a1 = pg0[j] + 1;
+                if (pg0[j + 1] - pg0[j] == 2 && pkey[a0] == 0 && pkey[a1] == 0) {
                     r0v[j] |= 0x80000000u;
+                    if (subs[ord[a0]].lo == 0 && subs[ord[a1]].lo == 0 && half[a0] == 0 &&
+                        half[a1] == 1)
+                        r0v[j] |= 0x40000000u;
+                }
+            }
         }
         QR_CUDA(pl.blk_r0.upload(r0v), "upload block runs");
         QR_CUDA(pl.run_g0.upload(rg0), "upload runs");
@@ -1634,8 +1642,13 @@ struct qr_batch {
     std::vector<qr_op *> ops;
     std::vector<int32_t> nstates;
     int tile_bits = 0;
-    int mode = 0;         // 0: one persistent work-list kernel, 1: graph of per-operator kernels
+    // 0: one persistent work-list kernel, 1: graph of per-operator kernels,
+    // 2: both in one graph -- the persistent kernel for the small operators
+    // (fewer work items than half the SMs), one kernel per large operator
+    int mode = 0;
     int force_mode = -1;  // -1: the autotuner chooses
+    std::vector<char> sel;    // operators in the persistent kernel's work list
+    std::vector<char> small;  // operators with fewer items than half the SMs
     DevBuf d_ops, d_items, d_ptrs, d_err;
     uint32_t nitems = 0;
     std::vector<const void *> cur_psi;
@@ -1657,6 +1670,7 @@ int batch_build(qr_batch *bt, int tb) {
     std::vector<BatchOp> bo(bt->ops.size());
     std::vector<std::pair<double, size_t>> cost;
     for (size_t i = 0; i < bt->ops.size(); ++i) {
+        if (!bt->sel[i]) continue;  // applied by its own kernel (modes 1, 2)
         qr_op *op = bt->ops[i];
         int rc = build_plan(op, QR_C64C, 0, tb);
         if (rc) return rc;
@@ -1742,27 +1756,37 @@ int batch_upload_ptrs(qr_batch *bt, const void *const *psi, void *const *y, cuda
     return QR_OK;
 }
 
-// Graph of one compensated-c64 apply per operator on the current pointers,
-// spread over kForks parallel branches so small operators overlap.  Plans
-// must already be built (an uncaptured apply per operator does that).
-int capture_per_op(qr_batch *bt, cudaGraph_t *graph) {
+// The batch's graph on the current pointers, on kForks parallel branches:
+// the persistent work-list kernel over the selected operators (branch 0)
+// and one compensated-c64 apply per other operator (round-robin over the
+// remaining branches, or all of them when nothing is selected).  The
+// selected operators' tables and work list (batch_build) and the other
+// operators' plans must already exist.
+int capture_graph(qr_batch *bt, cudaGraph_t *graph) {
     cudaStream_t cap = bt->cap;
+    bool any_sel = false;
+    for (char c : bt->sel) any_sel |= c != 0;
     QR_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed), "begin capture");
     cudaError_t e = cudaEventRecord(bt->fork_ev[qr_batch::kForks], cap);
     for (int k = 0; k < qr_batch::kForks && e == cudaSuccess; ++k)
         e = cudaStreamWaitEvent(bt->fork[k], bt->fork_ev[qr_batch::kForks], 0);
     int rc = QR_OK;
-    for (size_t i = 0; i < bt->ops.size() && e == cudaSuccess && !rc; ++i)
+    if (any_sel && e == cudaSuccess) e = launch_batch_c64c(batch_args(bt), bt->nsm, bt->fork[0]);
+    const int first = any_sel ? 1 : 0, nbr = qr_batch::kForks - first;
+    int k = 0;
+    for (size_t i = 0; i < bt->ops.size() && e == cudaSuccess && !rc; ++i) {
+        if (bt->sel[i]) continue;
         rc = apply_impl("qr_batch_apply", bt->ops[i], QR_C64C, bt->cur_psi[i], bt->cur_y[i],
-                        bt->nstates[i], 0, bt->fork[i % qr_batch::kForks], nullptr, nullptr,
+                        bt->nstates[i], 0, bt->fork[first + (k++ % nbr)], nullptr, nullptr,
                         nullptr);
-    for (int k = 0; k < qr_batch::kForks && e == cudaSuccess; ++k) {
-        e = cudaEventRecord(bt->fork_ev[k], bt->fork[k]);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(cap, bt->fork_ev[k], 0);
+    }
+    for (int f = 0; f < qr_batch::kForks && e == cudaSuccess; ++f) {
+        e = cudaEventRecord(bt->fork_ev[f], bt->fork[f]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(cap, bt->fork_ev[f], 0);
     }
     cudaError_t e2 = cudaStreamEndCapture(cap, graph);
     if (rc) return rc;
-    if (e != cudaSuccess) return cuda_fail(e, "per-operator graph capture");
+    if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
     if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
     return QR_OK;
 }
@@ -1774,25 +1798,31 @@ void drop_graph(qr_batch *bt) {
     bt->graph = nullptr;
 }
 
-int instantiate_per_op(qr_batch *bt) {
+// Select the operators of a mode, build what the graph needs (work list
+// and tables of the selected ones, plans of the others, uncaptured) and
+// capture and instantiate it.
+int instantiate_mode(qr_batch *bt, int mode) {
     drop_graph(bt);
-    int rc = capture_per_op(bt, &bt->graph);
+    for (size_t i = 0; i < bt->ops.size(); ++i)
+        bt->sel[i] = mode == 0 ? 1 : (mode == 1 ? 0 : bt->small[i]);
+    int rc = batch_build(bt, kBatchTileBits);
+    for (size_t i = 0; i < bt->ops.size() && !rc; ++i)
+        if (!bt->sel[i]) rc = build_plan(bt->ops[i], QR_C64C, 0);
+    if (!rc) rc = capture_graph(bt, &bt->graph);
     if (rc) return rc;
     QR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0), "graph instantiate");
+    bt->mode = mode;
     return QR_OK;
 }
 
-// Graph of the one persistent work-list launch (tables of batch_build).
-int instantiate_persistent(qr_batch *bt) {
-    drop_graph(bt);
-    BatchArgs a = batch_args(bt);
-    QR_CUDA(cudaStreamBeginCapture(bt->cap, cudaStreamCaptureModeRelaxed), "begin capture");
-    cudaError_t e = launch_batch_c64c(a, bt->nsm, bt->cap);
-    cudaError_t e2 = cudaStreamEndCapture(bt->cap, &bt->graph);
-    if (e != cudaSuccess) return cuda_fail(e, "batch launch under capture");
-    if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
-    QR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0), "graph instantiate");
-    return QR_OK;
+uint64_t graph_kernels(const qr_batch *bt) {
+    uint64_t k = 0;
+    bool any_sel = false;
+    for (size_t i = 0; i < bt->ops.size(); ++i) {
+        if (bt->sel[i]) any_sel = true;
+        else ++k;
+    }
+    return k + (any_sel ? 1 : 0);
 }
 
 void record_gens(qr_batch *bt) {
@@ -1808,14 +1838,7 @@ int refresh_after_coeffs(qr_batch *bt, cudaStream_t st) {
         stale = bt->gens[i] != bt->ops[i]->coef_gen;
     if (!stale) return QR_OK;
     QR_CUDA(cudaStreamSynchronize(st), "qr_batch_apply sync before plan rebuild");
-    int rc = QR_OK;
-    if (bt->mode == 1) {
-        for (size_t i = 0; i < bt->ops.size() && !rc; ++i) rc = build_plan(bt->ops[i], QR_C64C, 0);
-        if (!rc) rc = instantiate_per_op(bt);
-    } else {
-        rc = batch_build(bt, bt->tile_bits);
-        if (!rc) rc = instantiate_persistent(bt);
-    }
+    int rc = instantiate_mode(bt, bt->mode);
     if (!rc) record_gens(bt);
     return rc;
 }
@@ -1842,6 +1865,13 @@ int qr_batch_create(int32_t nops, qr_op *const *ops, const int32_t *nstates, qr_
     bt->ops.assign(ops, ops + nops);
     bt->nstates.assign(nstates, nstates + nops);
     cudaError_t e = cudaDeviceGetAttribute(&bt->nsm, cudaDevAttrMultiProcessorCount, dev);
+    bt->sel.assign(nops, 1);
+    bt->small.assign(nops, 0);
+    for (int32_t i = 0; i < nops; ++i) {
+        const int b = std::min(ops[i]->n, kBatchTileBits);
+        const uint64_t items = (ops[i]->N >> b) * (uint64_t)nstates[i];
+        bt->small[i] = 2 * items <= (uint64_t)bt->nsm ? 1 : 0;
+    }
     if (e == cudaSuccess) e = bt->d_ptrs.alloc(2 * (size_t)nops * sizeof(void *));
     if (e == cudaSuccess) e = bt->d_err.alloc(sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(bt->d_err.p, 0, sizeof(int));
@@ -1876,7 +1906,7 @@ int qr_batch_tile_bits(const qr_batch *bt) { return bt ? bt->tile_bits : 0; }
 int qr_batch_mode(const qr_batch *bt) { return bt && bt->exec ? bt->mode : -1; }
 
 int qr_batch_set_mode(qr_batch *bt, int32_t mode) {
-    if (!bt || mode < -1 || mode > 1) return fail(QR_EINVAL, "qr_batch_set_mode: bad arguments");
+    if (!bt || mode < -1 || mode > 2) return fail(QR_EINVAL, "qr_batch_set_mode: bad arguments");
     if (bt->exec) return fail(QR_ESTATE, "qr_batch_set_mode: the first apply has already chosen");
     bt->force_mode = mode;
     return QR_OK;
@@ -1894,69 +1924,62 @@ int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *s
         rc = refresh_after_coeffs(bt, st);
         if (rc) return rc;
     }
-    if (bt->exec && bt->mode == 1 && bt->ptrs_changed) {
+    if (bt->exec && bt->mode != 0 && bt->ptrs_changed) {
         // per-operator graph nodes carry the state pointers: capture again
-        rc = instantiate_per_op(bt);
+        rc = instantiate_mode(bt, bt->mode);
         if (rc) return rc;
     }
     bt->ptrs_changed = false;
     if (!bt->exec) {
-        // autotuner: time each candidate on these buffers -- the persistent
-        // work-list kernel (4096-amplitude tiles) and a graph of one
-        // per-operator kernel each
+        // autotuner: time each form on these buffers (one warm-up, three
+        // timed launches of its graph) -- the persistent work-list kernel,
+        // a graph of one kernel per operator, and, when the batch has both
+        // small and large operators, the persistent kernel for the small
+        // ones beside per-operator kernels for the large ones
+        bool any_small = false, any_large = false;
+        for (char c : bt->small) (c ? any_small : any_large) = true;
+        std::vector<int> cands;
+        if (bt->force_mode >= 0) cands.push_back(bt->force_mode);
+        else {
+            cands = {0, 1};
+            if (any_small && any_large) cands.push_back(2);
+        }
         int best = -1;
         float best_ms = 0.f;
         cudaEvent_t e0, e1;
         QR_CUDA(cudaEventCreate(&e0), "event");
         QR_CUDA(cudaEventCreate(&e1), "event");
-        auto timed = [&](auto &&launch, float *ms) -> cudaError_t {
-            cudaError_t e = launch();
+        for (int m : cands) {
+            rc = instantiate_mode(bt, m);
+            if (rc) break;
+            if (cands.size() == 1) {
+                best = m;
+                break;
+            }
+            cudaError_t e = cudaGraphLaunch(bt->exec, bt->cap);
             if (e == cudaSuccess) e = cudaEventRecord(e0, bt->cap);
-            for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = launch();
+            for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaGraphLaunch(bt->exec, bt->cap);
             if (e == cudaSuccess) e = cudaEventRecord(e1, bt->cap);
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-            if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
-            return e;
-        };
-        if (bt->force_mode != 1) {
-            rc = batch_build(bt, kBatchTileBits);
-            if (!rc) {
-                BatchArgs a = batch_args(bt);
-                float ms = 0.f;
-                cudaError_t e = timed([&] { return launch_batch_c64c(a, bt->nsm, bt->cap); }, &ms);
-                if (e != cudaSuccess) rc = cuda_fail(e, "qr_batch autotune");
-                best = kBatchTileBits;
-                best_ms = ms;
-            }
-        }
-        if (!rc && bt->force_mode != 0) {
-            for (size_t i = 0; i < bt->ops.size() && !rc; ++i)  // builds the plans
-                rc = apply_impl("qr_batch_apply", bt->ops[i], QR_C64C, bt->cur_psi[i],
-                                bt->cur_y[i], bt->nstates[i], 0, bt->cap, nullptr, nullptr,
-                                nullptr);
-            if (!rc) rc = instantiate_per_op(bt);
             float ms = 0.f;
-            if (!rc) {
-                cudaError_t e = timed([&] { return cudaGraphLaunch(bt->exec, bt->cap); }, &ms);
-                if (e != cudaSuccess) rc = cuda_fail(e, "qr_batch autotune");
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "qr_batch autotune");
+                break;
             }
-            if (!rc && (best < 0 || ms < best_ms)) {
-                best = 0;  // per-operator graph
+            if (best < 0 || ms < best_ms) {
+                best = m;
                 best_ms = ms;
             }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (rc) return rc;
-        if (best == 0) {
-            bt->mode = 1;
-            bt->tile_bits = 12;
-        } else {
-            bt->mode = 0;
-            rc = batch_build(bt, best);
-            if (!rc) rc = instantiate_persistent(bt);
+        if (bt->mode != best) {
+            rc = instantiate_mode(bt, best);
             if (rc) return rc;
         }
+        bt->tile_bits = kBatchTileBits;
         record_gens(bt);
         QR_CUDA(cudaStreamSynchronize(bt->cap), "autotune sync");
         int h = 0;
@@ -1968,7 +1991,7 @@ int qr_batch_apply(qr_batch *bt, const void *const *psi, void *const *y, void *s
         }
     }
     QR_CUDA(cudaGraphLaunch(bt->exec, st), "graph launch");
-    count_launch(bt->mode == 1 ? bt->ops.size() : 1);  // kernels the graph runs
+    count_launch(graph_kernels(bt));  // kernels the graph runs
     return QR_OK;
 }
 

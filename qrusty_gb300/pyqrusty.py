@@ -770,7 +770,8 @@ class Batch:
     @property
     def mode(self) -> int:
         """0: one persistent work-list kernel, 1: graph of per-operator
-        kernels (chosen by timing on the first apply); -1 before it."""
+        kernels, 2: both (the persistent kernel for the small operators);
+        chosen by timing on the first apply; -1 before it."""
         return int(_lib.load().qr_batch_mode(self._h))
 
     def set_mode(self, mode: int) -> None:

@@ -76,10 +76,10 @@ def check_against_c128(ops, psis, ys):
     return worst
 
 
-@pytest.mark.parametrize("mode", [-1, 0, 1])
+@pytest.mark.parametrize("mode", [-1, 0, 1, 2])
 def test_batch_uneven_small(cuda, mode):
-    """Both launch forms (persistent work-list kernel, graph of per-operator
-    kernels) and the timed choice between them."""
+    """Every launch form (persistent work-list kernel, graph of per-operator
+    kernels, both: persistent for the small operators) and the timed choice."""
     rng = np.random.default_rng(42)
     terms, nstates = [], []
     for k in range(24):
@@ -98,7 +98,7 @@ def test_batch_uneven_small(cuda, mode):
     b.set_mode(mode)
     b.apply(psis, ys)
     assert b.tile_bits in (10, 11, 12)
-    assert b.mode in ((0, 1) if mode == -1 else (mode,))
+    assert b.mode in ((0, 1, 2) if mode == -1 else (mode,))
     assert check_against_c128(ops, psis, ys) <= 1e-6
     # graph replay with the same buffers, then with new output buffers
     import torch
@@ -139,7 +139,7 @@ def test_batch_uneven_workload(cuda, oracle):
     assert check_against_c128(ops, psis, ys) <= 1e-6
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_batch_forms_vs_oracle(cuda, oracle, mode):
     """Each launch form, forced, on a dozen operators of the uneven workload
     (every qubit count) against the FP64 oracle, every state."""
@@ -154,7 +154,7 @@ def test_batch_forms_vs_oracle(cuda, oracle, mode):
     assert check_against_oracle(oracle, sub, psis, ys, range(len(sub))) <= 1e-6
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_batch_after_set_coeffs(cuda, oracle, mode):
     """A coefficient update of one operator reaches the batch's next apply."""
     import torch

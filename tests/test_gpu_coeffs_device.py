@@ -91,7 +91,7 @@ def test_device_update_then_host_update(cuda):
     assert torch.equal(op.apply(psi), PauliOperator(t.n, t.x, t.z, t.phase, c1).apply(psi))
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_batch_follows_device_update(cuda, mode):
     import torch
     rng = np.random.default_rng(2)
