@@ -139,18 +139,28 @@ __device__ __forceinline__ Cplx<Real> cneg_if(const Cplx<Real> &d, uint32_t s) {
     return r;
 }
 
-// ---------------------------------------------------------------- apply kernel
-// Real = float (compensated) or double (plain).  AMPS amplitudes per thread.
-template <typename Real, int AMPS, bool COMP>
-__global__ void __launch_bounds__(512, 1) apply_tiled(const ApplyArgs a, int stages) {
-    using C = Cplx<Real>;
+// ---------------------------------------------------------------- c128 kernel
+// Plain complex128: AMPS amplitudes per thread, one (amplitude, group) = 4
+// DFMA.  Warps run decoupled, as in the compensated-c64 kernels: each waits on
+// the stage's full mbarrier, applies the block's groups, and counts itself
+// out on a per-stage counter; the last warp out refills the stage with the
+// partner tile a ring length ahead.  No CTA-wide barrier sits between
+// partner blocks, so the FP64 pipe does not drain at every block.
+template <int AMPS>
+__global__ void __launch_bounds__(512, 1) apply_c128(const ApplyArgs a, int stages) {
+    using C = Cplx<double>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t threads = blockDim.x;
+    const uint32_t nwarps = threads >> 5;
     const uint32_t t = threadIdx.x;
+    const uint32_t lane = t & 31;
     const uint32_t tile = 1u << a.b;
     const uint32_t tile_bytes = tile * (uint32_t)sizeof(C);
     C *bufs = reinterpret_cast<C *>(smem_raw);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)stages * tile_bytes);
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kMaxStages);
+    volatile uint32_t *s_abort = cnt + kMaxStages;
+    uint32_t *s_iss = cnt + kMaxStages + 1;  // copies issued per stage (drain)
 
     const C *psi = static_cast<const C *>(a.psi);
     C *y = static_cast<C *>(a.y);
@@ -165,70 +175,67 @@ __global__ void __launch_bounds__(512, 1) apply_tiled(const ApplyArgs a, int sta
     const uint64_t total = my_items * nb;
     if (total == 0) return;
 
-    if (t == 0) {
-        for (int s = 0; s < stages; ++s) mbar_init(&full[s], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-
     auto issue = [&](uint64_t L) {
         const uint64_t k = L / nb;
         const uint32_t j = (uint32_t)(L - k * nb);
         const uint64_t item = first + k * gridDim.x;
         const uint64_t st = item / a.ntiles;
         const uint64_t q = item - st * a.ntiles;
-        const uint64_t src_tile = q ^ a.blk_hi[j];
-        const C *src = psi + st * a.N + (src_tile << a.b);
+        const C *src = psi + st * a.N + ((q ^ a.blk_hi[j]) << a.b);
         const int s = (int)(L % (uint64_t)stages);
         if (blockIdx.x == 0 && (int64_t)L == a.withhold) return;  // test hook: never issued
+        ++s_iss[s];
         mbar_expect_tx(&full[s], tile_bytes);
         bulk_g2s(bufs + (size_t)s * tile, src, tile_bytes, &full[s]);
     };
     if (t == 0) {
+        for (int s = 0; s < stages; ++s) {
+            mbar_init(&full[s], 1);
+            cnt[s] = 0;
+            s_iss[s] = 0;
+        }
+        *s_abort = 0;
+        mbar_fence_init();
         const uint64_t pro = total < (uint64_t)stages ? total : (uint64_t)stages;
         for (uint64_t L = 0; L < pro; ++L) issue(L);
     }
+    __syncthreads();
 
     C acc[AMPS];
-    C lo_acc[AMPS];
-    C bacc[AMPS];
     const uint32_t amask = AMPS - 1;
+    uint32_t j = 0, s = 0, par = 0;
+    uint64_t st = first / a.ntiles;
+    uint64_t q = first - st * a.ntiles;
 
     for (uint64_t L = 0; L < total; ++L) {
-        const uint64_t k = L / nb;
-        const uint32_t j = (uint32_t)(L - k * nb);
-        const uint64_t item = first + k * gridDim.x;
-        const uint64_t st = item / a.ntiles;
-        const uint64_t q = item - st * a.ntiles;
         const uint64_t rbase = (q << a.b) | t;
         if (j == 0) {
 #pragma unroll
-            for (int m = 0; m < AMPS; ++m) {
-                acc[m].re = acc[m].im = Real(0);
-                lo_acc[m].re = lo_acc[m].im = Real(0);
-            }
+            for (int m = 0; m < AMPS; ++m) acc[m].re = acc[m].im = 0.0;
         }
-        const int s = (int)(L % (uint64_t)stages);
-        const uint32_t par = (uint32_t)((L / (uint64_t)stages) & 1ull);
-        const bool ok = mbar_wait_bounded(&full[s], par, a.wait_ns);
+        // an expired wait sets the abort flag; from then on every warp skips
+        // waits and work
+        bool skip = *s_abort != 0;
+        if (!skip && !mbar_wait_bounded(&full[s], par, a.wait_ns)) {
+            if (lane == 0) {
+                atomicExch(a.err, kErrMbarTimeout);
+                *s_abort = 1;
+            }
+            skip = true;
+        }
+        skip = __any_sync(0xffffffffu, skip);
         const C *buf = bufs + (size_t)s * tile;
 
-        if constexpr (COMP) {
-#pragma unroll
-            for (int m = 0; m < AMPS; ++m) bacc[m].re = bacc[m].im = Real(0);
-        }
-        C *tgt = COMP ? bacc : acc;
-
-        if ((int)j == a.diag_block && diag != nullptr) {
+        if (!skip && (int)j == a.diag_block && diag != nullptr) {
             const C *dg = diag + (q << a.b);
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
                 const uint32_t rl = t + threads * (uint32_t)m;
-                cmac(tgt[m], dg[rl], buf[rl]);
+                cmac(acc[m], dg[rl], buf[rl]);
             }
         }
 
-        const uint32_t g1 = a.blk_g0[j + 1];
+        const uint32_t g1 = skip ? 0u : a.blk_g0[j + 1];
         for (uint32_t g = a.blk_g0[j]; g < g1; ++g) {
             const GroupDesc gd = a.groups[g];
             const uint32_t lo_t = gd.lo & (threads - 1);
@@ -260,7 +267,7 @@ __global__ void __launch_bounds__(512, 1) apply_tiled(const ApplyArgs a, int sta
                         C Dm;
                         Dm.re = sg ? Dn.re : D.re;
                         Dm.im = sg ? Dn.im : D.im;
-                        cmac(tgt[m], Dm, p);
+                        cmac(acc[m], Dm, p);
                     }
                 } else {
 #pragma unroll
@@ -271,7 +278,7 @@ __global__ void __launch_bounds__(512, 1) apply_tiled(const ApplyArgs a, int sta
                         const C D = tables[gd.off + um];
                         const C p = src[((uint32_t)m ^ lo_m) << a.tb];
                         const uint32_t sg = ((W0 >> m) ^ s0) & 1u;
-                        cmac(tgt[m], cneg_if(D, sg), p);
+                        cmac(acc[m], cneg_if(D, sg), p);
                     }
                 }
             } else {
@@ -279,7 +286,7 @@ __global__ void __launch_bounds__(512, 1) apply_tiled(const ApplyArgs a, int sta
                 for (int m = 0; m < AMPS; ++m) {
                     const uint64_t r = rbase | ((uint64_t)m << a.tb);
                     C D;
-                    D.re = D.im = Real(0);
+                    D.re = D.im = 0.0;
                     for (uint32_t kk = 0; kk < gd.cnt; ++kk) {
                         const uint64_t zk = a.fat_z[gd.off + kk];
                         const C ck = fat_c[gd.off + kk];
@@ -288,16 +295,8 @@ __global__ void __launch_bounds__(512, 1) apply_tiled(const ApplyArgs a, int sta
                         D.im += sg ? -ck.im : ck.im;
                     }
                     const C p = src[((uint32_t)m ^ lo_m) << a.tb];
-                    cmac(tgt[m], D, p);
+                    cmac(acc[m], D, p);
                 }
-            }
-        }
-
-        if constexpr (COMP) {
-#pragma unroll
-            for (int m = 0; m < AMPS; ++m) {
-                two_sum_into(acc[m].re, lo_acc[m].re, bacc[m].re);
-                two_sum_into(acc[m].im, lo_acc[m].im, bacc[m].im);
             }
         }
 
@@ -305,43 +304,51 @@ __global__ void __launch_bounds__(512, 1) apply_tiled(const ApplyArgs a, int sta
             C *yo = y + st * a.N + (q << a.b);
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
-                C o;
-                if constexpr (COMP) {
-                    o.re = acc[m].re + lo_acc[m].re;
-                    o.im = acc[m].im + lo_acc[m].im;
-                } else {
-                    o = acc[m];
-                }
+                C o = acc[m];
                 const uint32_t rl = t + threads * (uint32_t)m;
-                if constexpr (sizeof(Real) == 8) {
-                    if (a.v != nullptr) {  // fused y = alpha (H psi) + beta v
-                        const double2 vv = static_cast<const double2 *>(a.v)[st * a.N + (q << a.b) + rl];
-                        const double2 r = cx_axpby(a.ar, a.ai, make_double2(o.re, o.im), a.br, a.bi, vv);
-                        o.re = r.x;
-                        o.im = r.y;
-                    }
+                if (a.v != nullptr) {  // fused y = alpha (H psi) + beta v
+                    const double2 vv = static_cast<const double2 *>(a.v)[st * a.N + (q << a.b) + rl];
+                    const double2 r = cx_axpby(a.ar, a.ai, make_double2(o.re, o.im), a.br, a.bi, vv);
+                    o.re = r.x;
+                    o.im = r.y;
                 }
                 yo[rl] = o;
             }
         }
 
-        // All threads are done with stage s (and agree on the wait outcome).
-        if (__syncthreads_or(ok ? 0 : 1)) {
-            if (t == 0) {
-                atomicExch(a.err, kErrMbarTimeout);
-                // Drain the copies issued into this CTA's stages (steps L ..
-                // L + stages - 1; a withheld test step was never issued).  The
-                // drain keeps the full 2 s bound whatever a test set for the
-                // waits above: an issued copy always completes.
-                for (uint64_t L2 = L; L2 < total && L2 < L + (uint64_t)stages; ++L2) {
-                    if (blockIdx.x == 0 && (int64_t)L2 == a.withhold) continue;
-                    const int s2 = (int)(L2 % (uint64_t)stages);
-                    mbar_wait_bounded(&full[s2], (uint32_t)((L2 / stages) & 1ull), kWaitLimitNs);
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            const uint32_t old = atomicAdd(&cnt[s], 1u);
+            if (old == nwarps - 1) {
+                cnt[s] = 0;
+                if (L + (uint64_t)stages < total && *s_abort == 0) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue(L + (uint64_t)stages);
                 }
             }
-            return;
         }
-        if (t == 0 && L + (uint64_t)stages < total) issue(L + (uint64_t)stages);
+        if (++s == (uint32_t)stages) {
+            s = 0;
+            par ^= 1u;
+        }
+        if (++j == nb) {
+            j = 0;
+            q += gridDim.x;
+            while (q >= a.ntiles) {
+                q -= a.ntiles;
+                ++st;
+            }
+        }
+    }
+    // After an expired wait: every warp has left the loop (no copy is issued
+    // after the abort flag is set), then a bounded wait -- with the full 2 s,
+    // whatever a test set for the waits -- for the last copy issued into
+    // each stage, whose phase parity is (issues - 1) & 1.
+    __syncthreads();
+    if (t == 0 && *s_abort) {
+        for (int k = 0; k < stages; ++k)
+            if (s_iss[k] != 0) mbar_wait_bounded(&full[k], (s_iss[k] - 1u) & 1u, kWaitLimitNs);
     }
 }
 
@@ -1389,14 +1396,15 @@ cudaError_t launch_batch_c64c(const BatchArgs &a, int nsm, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-template <typename Real, int AMPS, bool COMP>
+template <int AMPS>
 static cudaError_t launch_one(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
-    const uint32_t tile_bytes = (1u << a.b) * (uint32_t)sizeof(Cplx<Real>);
+    const uint32_t tile_bytes = (1u << a.b) * (uint32_t)sizeof(Cplx<double>);
     int stages = (int)((200u * 1024u) / tile_bytes);
     if (stages > kMaxStages) stages = kMaxStages;
     if (stages < 2) stages = 2;
-    const size_t smem = (size_t)stages * tile_bytes + kMaxStages * sizeof(uint64_t);
-    auto kern = apply_tiled<Real, AMPS, COMP>;
+    // stages, then full barriers, stage counters, the abort flag and issue counts
+    const size_t smem = (size_t)stages * tile_bytes + kMaxStages * (sizeof(uint64_t) + 8u) + 8u;
+    auto kern = apply_c128<AMPS>;
     cudaError_t e = ensure_dyn_smem(reinterpret_cast<const void *>(kern), smem);
     if (e != cudaSuccess) return e;
     uint64_t grid = a.nitems < (uint64_t)nsm ? a.nitems : (uint64_t)nsm;
@@ -1406,22 +1414,21 @@ static cudaError_t launch_one(const ApplyArgs &a, int threads, int nsm, cudaStre
     return cudaGetLastError();
 }
 
-template <typename Real, bool COMP>
 static cudaError_t dispatch_amps(const ApplyArgs &a, int amps, int threads, int nsm,
                                  cudaStream_t st) {
     switch (amps) {
-        case 1: return launch_one<Real, 1, COMP>(a, threads, nsm, st);
-        case 2: return launch_one<Real, 2, COMP>(a, threads, nsm, st);
-        case 4: return launch_one<Real, 4, COMP>(a, threads, nsm, st);
-        case 8: return launch_one<Real, 8, COMP>(a, threads, nsm, st);
-        case 16: return launch_one<Real, 16, COMP>(a, threads, nsm, st);
+        case 1: return launch_one<1>(a, threads, nsm, st);
+        case 2: return launch_one<2>(a, threads, nsm, st);
+        case 4: return launch_one<4>(a, threads, nsm, st);
+        case 8: return launch_one<8>(a, threads, nsm, st);
+        case 16: return launch_one<16>(a, threads, nsm, st);
         default: return cudaErrorInvalidValue;
     }
 }
 
 cudaError_t launch_apply(int dtype, const ApplyArgs &a, int amps, int threads, int nsm,
                          cudaStream_t st) {
-    if (dtype == 0) return dispatch_amps<double, false>(a, amps, threads, nsm, st);
+    if (dtype == 0) return dispatch_amps(a, amps, threads, nsm, st);
     if (amps >= 2 && a.tb != kTb) return cudaErrorInvalidValue;
     switch (amps) {
         case 1: return launch_c64c<1>(a, threads, nsm, st);

@@ -90,8 +90,8 @@ def test_single_tile_table_kernel_withheld_copy(cuda):
 
 
 def test_complex128_kernel_withheld_copy(cuda):
-    """apply_tiled<double>: a CTA-wide vote on the wait, then the drain of
-    the steps already issued (the withheld one skipped)."""
+    """apply_c128 (decoupled warps, per-stage release counters): the abort
+    flag, then the drain of the copies issued into each stage."""
     import torch
     t = W.cfg2(n=16, npair=600, nz=200)
     op = PauliOperator(t.n, t.x, t.z, t.phase, t.coeff)
