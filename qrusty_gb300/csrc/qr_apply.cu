@@ -131,6 +131,15 @@ __device__ __forceinline__ void two_sum_into2(float2 &hi, float2 &lo, float2 b) 
     hi = s;
     lo = __fadd2_rn(lo, e);
 }
+// hi += b with the same error-free transformation; returns the error term
+// instead of accumulating it
+__device__ __forceinline__ float2 two_sum_carry2(float2 &hi, float2 b) {
+    const float2 s = __fadd2_rn(hi, b);
+    const float2 bb = sub2_rn(s, hi);
+    const float2 e = __fadd2_rn(sub2_rn(hi, sub2_rn(s, bb)), sub2_rn(b, bb));
+    hi = s;
+    return e;
+}
 template <typename Real>
 __device__ __forceinline__ Cplx<Real> cneg_if(const Cplx<Real> &d, uint32_t s) {
     Cplx<Real> r;
@@ -405,6 +414,12 @@ constexpr int kTabEnt = 4;  // per-tile table entries (float4) per sub-group
 // aligned
 constexpr size_t kTabBarBytes = ((size_t)kTabStages * 16u + 4u + 15u) & ~(size_t)15u;
 static_assert(kTabBarBytes % 16 == 0, "thread descriptors need 16-byte alignment");
+// paired kernel: up to three ring slots of two partner tiles; barriers,
+// counters, the abort flag and issue counts in 64 bytes
+constexpr uint32_t kMaxPairSlots = 3;
+constexpr size_t kPairBarBytes = 64;
+static_assert(kMaxPairSlots * 8 + kMaxPairSlots * 4 + 4 + kMaxPairSlots * 4 <= kPairBarBytes,
+              "pair barrier block");
 
 template <int AMPS, int ZM, bool XM, bool TV>
 __device__ __forceinline__ void sub_tab_one(float2 (&A)[AMPS], float2 (&B)[AMPS],
@@ -869,19 +884,20 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     const uint32_t t = threadIdx.x;
     const uint32_t lane = t & 31;
     const uint32_t tile_bytes = (1u << a.b) * 8u;
-    const uint32_t tabn = a.nsub < kTabCap ? a.nsub : kTabCap;
-    float4 *s_tab = reinterpret_cast<float4 *>(smem_raw + (size_t)kTabStages * tile_bytes);
-    float2 *s_lo = reinterpret_cast<float2 *>(s_tab + kTabEnt * (size_t)tabn);
-    uint64_t *full = reinterpret_cast<uint64_t *>(s_lo + (size_t)AMPS * threads);
-    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kTabStages);
-    volatile uint32_t *s_abort = cnt + kTabStages;
-    // copies issued into each stage: the drain after an expired wait waits
+    // layout (pair_smem_bytes): ring of nsl slots of two tiles, factor table,
+    // barriers / counters (64 bytes), thread descriptors, run list, pair list
+    const uint32_t nsl = a.pair_slots;
+    const uint32_t tabn = a.nsub;  // a pair plan has at most kTabCap sub-groups
+    float4 *s_tab = reinterpret_cast<float4 *>(smem_raw + (size_t)nsl * 2u * tile_bytes);
+    uint64_t *full = reinterpret_cast<uint64_t *>(s_tab + kTabEnt * (size_t)tabn);
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(full + kMaxPairSlots);
+    volatile uint32_t *s_abort = cnt + kMaxPairSlots;
+    // copies issued into each slot: the drain after an expired wait waits
     // for the last one's phase, so no copy is in flight when the CTA exits
-    uint32_t *s_iss = cnt + kTabStages + 1;
-    uint4 *s_td = reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(s_lo) +
-                                            (size_t)AMPS * threads * 8u + kTabBarBytes);
-    uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + kTabCap);
-    uint32_t *s_blk = s_run + kTabCap + 1;
+    uint32_t *s_iss = cnt + kMaxPairSlots + 1;
+    uint4 *s_td = reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(full) + kPairBarBytes);
+    uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + tabn);
+    uint32_t *s_blk = s_run + a.nruns + 1;
     const uint32_t np = a.npairs, nb = a.nblocks;
     for (uint32_t i = t; i < a.nsub; i += threads) s_td[i] = a.tdesc[i];
     for (uint32_t i = t; i <= a.nruns; i += threads)
@@ -919,17 +935,17 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     uint64_t st = first / a.ntiles;
     uint64_t q = first - st * a.ntiles;
     if (t == 0) {
-        for (int s = 0; s < 2; ++s) {
+        for (uint32_t s = 0; s < nsl; ++s) {
             mbar_init(&full[s], 1);
             cnt[s] = 0;
             s_iss[s] = 0;
         }
         *s_abort = 0;
         mbar_fence_init();
-        // prologue: steps 0 and 1
+        // prologue: steps 0 .. nsl - 1
         uint32_t p1 = 0;
         uint64_t q1 = q, st1 = st;
-        for (uint64_t L = 0; L < total && L < 2; ++L) {
+        for (uint64_t L = 0; L < total && L < nsl; ++L) {
             issue_pair(L, (uint32_t)L, p1, st1, q1);
             if (++p1 == np) {
                 p1 = 0;
@@ -943,21 +959,19 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     }
     __syncthreads();
 
+    // y = A + iB is the FP32 sum of the current window of pairs; every 16
+    // pairs it is folded into hi with an error-free two-sum, and the error of
+    // that addition is carried into the next window (A starts from it: the
+    // compensated summation of Kahan, with no separate low word to keep);
+    // the last fold's error is added at the store
     float2 A[AMPS], B[AMPS], hi[AMPS];
-    float2 *mylo = s_lo + t;
     uint32_t p = 0, s = 0, par = 0;
-    // compensated fold every 16 pairs (32 partner tiles): a quarter of the
-    // fold work of kFlush; relative error 2.45e-7 on the 26-qubit
-    // Jordan-Wigner operator (2.0e-7 folding every 8 pairs, 1 % slower)
     constexpr uint32_t kFlushPairs = 16;
 
     for (uint64_t L = 0; L < total; ++L) {
         if (p == 0) {
 #pragma unroll
-            for (int m = 0; m < AMPS; ++m) {
-                A[m] = B[m] = hi[m] = make_float2(0.f, 0.f);
-                mylo[m * threads] = make_float2(0.f, 0.f);
-            }
+            for (int m = 0; m < AMPS; ++m) A[m] = B[m] = hi[m] = make_float2(0.f, 0.f);
             // table of the new output tile: every warp has finished the last one
             __syncthreads();
             for (uint32_t gi = t; gi < a.nsub; gi += threads) {
@@ -1031,10 +1045,8 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
             for (int m = 0; m < AMPS; ++m) {
                 const float2 yv =
                     make_float2(__fsub_rn(A[m].x, B[m].y), __fadd_rn(A[m].y, B[m].x));
-                float2 lm = mylo[m * threads];
-                two_sum_into2(hi[m], lm, yv);
-                mylo[m * threads] = lm;
-                A[m] = B[m] = make_float2(0.f, 0.f);
+                A[m] = two_sum_carry2(hi[m], yv);  // the error opens the next window
+                B[m] = make_float2(0.f, 0.f);
             }
         }
         if (last) {
@@ -1043,9 +1055,8 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
                                    : nullptr;
 #pragma unroll
             for (int m = 0; m < AMPS; ++m) {
-                const float2 lm = mylo[m * threads];
                 const uint32_t rl = t + threads * (uint32_t)m;
-                float2 o = make_float2(__fadd_rn(hi[m].x, lm.x), __fadd_rn(hi[m].y, lm.y));
+                float2 o = make_float2(__fadd_rn(hi[m].x, A[m].x), __fadd_rn(hi[m].y, A[m].y));
                 if (vo)  // fused y = alpha (H psi) + beta v, in FP32
                     o = cx_axpby((float)a.ar, (float)a.ai, o, (float)a.br, (float)a.bi, vo[rl]);
                 yo[rl] = o;
@@ -1058,10 +1069,10 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
             const uint32_t old = atomicAdd(&cnt[s], 1u);
             if (old == nwarps - 1) {
                 cnt[s] = 0;
-                if (L + 2 < total && *s_abort == 0) {
+                if (L + nsl < total && *s_abort == 0) {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    // two pairs ahead of (st, q, p), stepped with adds
-                    uint32_t p2 = p + 2;
+                    // nsl pairs ahead of (st, q, p), stepped with adds
+                    uint32_t p2 = p + nsl;
                     uint64_t q2 = q, st2 = st;
                     while (p2 >= np) {
                         p2 -= np;
@@ -1071,12 +1082,14 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
                             ++st2;
                         }
                     }
-                    issue_pair(L + 2, s, p2, st2, q2);
+                    issue_pair(L + nsl, s, p2, st2, q2);
                 }
             }
         }
-        s ^= 1u;
-        if (s == 0) par ^= 1u;
+        if (++s == nsl) {
+            s = 0;
+            par ^= 1u;
+        }
         if (++p == np) {
             p = 0;
             q += gridDim.x;
@@ -1089,7 +1102,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     // drain after an expired wait, as in apply_c64c_tab
     __syncthreads();
     if (t == 0 && *s_abort) {
-        for (int k = 0; k < 2; ++k)
+        for (uint32_t k = 0; k < nsl; ++k)
             if (s_iss[k] != 0) mbar_wait_bounded(&full[k], (s_iss[k] - 1u) & 1u, kWaitLimitNs);
     }
 }
@@ -1103,14 +1116,28 @@ static size_t tab_smem_bytes(const ApplyArgs &a, int threads) {
            (size_t)kTabCap * sizeof(uint4) + (2u * (size_t)kTabCap + 3u) * 4u;
 }
 
+// shared memory of the paired kernel with nsl ring slots (exact sizes of the
+// table, descriptors and lists of this plan)
+static size_t pair_smem_bytes(const ApplyArgs &a, uint32_t nsl) {
+    const size_t tile_bytes = ((size_t)1 << a.b) * 8u;
+    return (size_t)nsl * 2u * tile_bytes + (size_t)a.nsub * 16u * kTabEnt + kPairBarBytes +
+           (size_t)a.nsub * sizeof(uint4) + ((size_t)a.nruns + 1 + a.npairs + 1) * 4u;
+}
+
 template <int AMPS, bool WIDE>
-static cudaError_t launch_c64c_tab(const ApplyArgs &a, int threads, int nsm, cudaStream_t st) {
-    const size_t smem = tab_smem_bytes<AMPS>(a, threads);
+static cudaError_t launch_c64c_tab(const ApplyArgs &a_in, int threads, int nsm, cudaStream_t st) {
+    ApplyArgs a = a_in;
+    size_t smem = tab_smem_bytes<AMPS>(a, threads);
     // one chunk (operators of up to 512 sub-groups): no chunk bookkeeping;
-    // with a pair plan, partner blocks two at a time
+    // with a pair plan, partner blocks two at a time, in a ring of three
+    // slots when the plan's tables leave room for it, else two
     auto kern = a.nchunks > 1 ? apply_c64c_tab<AMPS, WIDE, true> : apply_c64c_tab<AMPS, WIDE, false>;
     if constexpr (AMPS == 8)
-        if (a.npairs > 0 && a.nchunks <= 1) kern = apply_c64c_pair<AMPS, WIDE>;
+        if (a.npairs > 0 && a.nchunks <= 1) {
+            kern = apply_c64c_pair<AMPS, WIDE>;
+            a.pair_slots = pair_smem_bytes(a, kMaxPairSlots) <= kMaxSmemPerBlock ? kMaxPairSlots : 2u;
+            smem = pair_smem_bytes(a, a.pair_slots);
+        }
     cudaError_t e = ensure_dyn_smem(reinterpret_cast<const void *>(kern), smem);
     if (e != cudaSuccess) return e;
     uint64_t grid = a.nitems < (uint64_t)nsm ? a.nitems : (uint64_t)nsm;

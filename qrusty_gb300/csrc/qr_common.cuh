@@ -90,6 +90,8 @@ struct ApplyArgs {
     int64_t withhold;
     // 64-bit row words (the n > 32 instantiations) forced at any n (test hook)
     int wide;
+    // paired kernel: ring slots of two partner tiles (set by the launcher)
+    uint32_t pair_slots;
 };
 
 
