@@ -547,8 +547,6 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
 // entries four at a time (independent loads in flight), then combine their
 // partial sums with a butterfly over the S lanes.
 // Replaces spmat_dot_densevec (qrusty/src/accel.rs:338-370).
-constexpr int kSpmvUnroll = 8;
-
 template <int S>
 __global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, uint64_t ncols,
                                                        const uint64_t *__restrict__ indptr,
@@ -562,28 +560,34 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, uint64_t 
          r += groups) {
         const uint64_t j0 = indptr[r], j1 = indptr[r + 1];
         double sr = 0.0, si = 0.0, tr = 0.0, ti = 0.0;
-        // U entries per lane per step, all loads issued before the first FMA
-        // (predicated: the short rows of a Pauli-sum CSR -- G entries, ~6 per
-        // lane at G = 44 -- take one step with every load in flight)
-        for (uint64_t j = j0 + sl; j < j1; j += (uint64_t)kSpmvUnroll * S) {
-            uint64_t c[kSpmvUnroll];
-            double2 d[kSpmvUnroll];
+        uint64_t j = j0 + sl;
+        // four entries per lane per step: their loads are in flight together
+        for (; j + 3 * S < j1; j += 4 * S) {
+            uint64_t c[4];
+            double2 d[4];
 #pragma unroll
-            for (int u = 0; u < kSpmvUnroll; ++u) {  // the matrix streams once: evict-first loads
-                const uint64_t jj = j + (uint64_t)u * S;
-                c[u] = jj < j1 ? __ldcs(indices + jj) : ncols;
-                d[u] = jj < j1 ? __ldcs(data + jj) : make_double2(0.0, 0.0);
+            for (int u = 0; u < 4; ++u) {  // the matrix streams once: evict-first loads
+                c[u] = __ldcs(indices + j + u * S);
+                d[u] = __ldcs(data + j + u * S);
             }
-            double2 x[kSpmvUnroll];
+            double2 x[4];
 #pragma unroll
-            for (int u = 0; u < kSpmvUnroll; ++u)
-                x[u] = c[u] < ncols ? __ldg(v + c[u]) : make_double2(0.0, 0.0);
+            for (int u = 0; u < 4; ++u) x[u] = c[u] < ncols ? __ldg(v + c[u]) : make_double2(0.0, 0.0);
 #pragma unroll
-            for (int u = 0; u < kSpmvUnroll; ++u) {
-                if (c[u] >= ncols) continue;  // out-of-range columns (and padding) are skipped
+            for (int u = 0; u < 4; ++u) {
+                if (c[u] >= ncols) continue;  // out-of-range columns are skipped
                 double &ar = (u & 1) ? tr : sr, &ai = (u & 1) ? ti : si;
                 ar = fma(d[u].x, x[u].x, fma(-d[u].y, x[u].y, ar));
                 ai = fma(d[u].x, x[u].y, fma(d[u].y, x[u].x, ai));
+            }
+        }
+        for (; j < j1; j += S) {
+            const uint64_t c = indices[j];  // out-of-range columns are skipped
+            if (c < ncols) {
+                const double2 d = data[j];
+                const double2 x = v[c];
+                sr = fma(d.x, x.x, fma(-d.y, x.y, sr));
+                si = fma(d.x, x.y, fma(d.y, x.x, si));
             }
         }
         sr += tr;
