@@ -721,11 +721,20 @@ def measure_grad(steps=10, warmup=3):
     yref = O.apply(t.n, t.x, t.z, cp, ph)
     yh = y.detach().cpu().numpy().astype(np.complex128)
     N = 1 << t.n
+    # where a step goes: the pieces on their own clocks
+    op = terms.operator(c.detach())
+    pd = p.detach()
+    ms_fwd = _events_time(lambda: op.apply(pd), 10, 3, stream)
+    ms_adj = _events_time(lambda: op.apply(wd, adjoint=True), 10, 3, stream)
+    ms_tg = _events_time(lambda: op.term_grad(pd, wd), 10, 3, stream)
+    ms_cu = _events_time(lambda: op.set_coeffs_device(c.detach()), 10, 3, stream)
     return {"workload": "n=%d, %d random-letter terms, real c, complex64 psi, L = Re<H(c)psi, w> "
                         "(seed %d)" % (t.n, t.T, W.SEED0 + 4),
             "step": "forward + backward (grad_c, grad_psi) + SGD update of c",
             "ms_per_step": ms, "value": t.T * N / (ms / 1e3), "unit": UNIT,
             "gpu_launches_per_step": launches,
+            "breakdown_ms": {"forward_apply": ms_fwd, "adjoint_apply": ms_adj,
+                             "term_grad": ms_tg, "device_coefficient_update": ms_cu},
             "rel_err_vs_oracle": {
                 "forward_y": float(np.linalg.norm(yh - yref) / np.linalg.norm(yref)),
                 "grad_c": float(np.linalg.norm(gc - tg) / np.linalg.norm(tg))}}
@@ -859,7 +868,8 @@ def run_grad(args):
                      r["value"], UNIT, r["ms_per_step"], "c64c forward / adjoint, fp64 reductions",
                      {"workload": r["workload"], "step": r["step"],
                       "l2": "state 8 MiB: L2-resident"},
-                     rel_err=r["rel_err_vs_oracle"], gpu_launches=r["gpu_launches_per_step"])
+                     rel_err=r["rel_err_vs_oracle"], gpu_launches=r["gpu_launches_per_step"],
+                     breakdown_ms=r["breakdown_ms"])
     print(json.dumps(out), flush=True)
 
 
