@@ -67,7 +67,8 @@ typedef struct {
 /* Create an operator from T terms (replaces SparsePauliOp::new,
  * qrusty/src/lib.rs:354-376, plus make_params, qrusty/src/accel.rs:141-157).
  * Validates 1 <= n <= 63, T >= 1, masks within n bits, phase <= 3.
- * Uploads the term tables to the current CUDA device (synchronous). */
+ * Uploads the terms to the current CUDA device and groups them there
+ * (qr_op_get_groups); synchronous. */
 int qr_op_create(int32_t n, uint64_t nterms, const uint64_t *x, const uint64_t *z,
                  const uint8_t *phase, const double *coeff, qr_op **out);
 
@@ -75,6 +76,20 @@ int qr_op_create(int32_t n, uint64_t nterms, const uint64_t *x, const uint64_t *
 int qr_op_destroy(qr_op *op);
 
 int qr_op_get_info(const qr_op *op, qr_op_info *info);
+
+/* The operator's term grouping, computed on the device at creation by a
+ * stable radix sort on x (replaces the per-row sort by x of make_row,
+ * qrusty/src/accel.rs:188-208, and the merging of equal (x, z) strings of
+ * the FP64 simplification).  *ngroups receives the number of groups; the
+ * host buffers, each may be NULL (a first call with all NULL sizes them):
+ *   gx[ngroups]       distinct x masks, ascending (the CSR column groups);
+ *   goff[ngroups + 1] group g is order[goff[g] .. goff[g + 1]);
+ *   order[nterms]     input index of each term, stably sorted by x;
+ *   mmap[nterms]      merged (x, z) string of each input term, the strings
+ *                     numbered in order of first occurrence.
+ * Synchronous. */
+int qr_op_get_groups(const qr_op *op, uint64_t *ngroups, uint64_t *gx, uint32_t *goff,
+                     uint32_t *order, uint32_t *mmap);
 
 /* CSR size of the operator's matrix (replaces the nnz pass of
  * make_unsafe_vectors_chunked, qrusty/src/accel.rs:309-319):

@@ -31,7 +31,7 @@ EXPORTS = (
     "qr_batch_apply", "qr_batch_tile_bits", "qr_batch_mode", "qr_batch_set_mode", "qr_axpby", "qr_axpy", "qr_ax", "qr_precond2",
     "qr_csr_diagonal", "qr_op_diagonal", "qr_apply_axpby", "qr_rawio_info", "qr_rawio_read", "qr_rawio_write",
     "qr_mm_write", "qr_mm_open", "qr_mm_fetch", "qr_mm_close", "qr_last_error", "qr_launch_count",
-    "qr_op_set_test_hooks", "qr_op_set_coeffs_device",
+    "qr_op_set_test_hooks", "qr_op_set_coeffs_device", "qr_op_get_groups",
 )
 
 QR_TEST_FORCE_WIDE = 1
@@ -80,6 +80,7 @@ def load(build_if_missing: bool = True):
     L.qr_op_create.argtypes = [i32, u64, vp, vp, vp, vp, C.POINTER(vp)]
     L.qr_op_destroy.argtypes = [vp]
     L.qr_op_get_info.argtypes = [vp, C.POINTER(OpInfo)]
+    L.qr_op_get_groups.argtypes = [vp, C.POINTER(u64), vp, vp, vp, vp]
     L.qr_csr_size.argtypes = [vp, C.POINTER(u64), C.POINTER(u64)]
     L.qr_csr_build.argtypes = [vp, vp, vp, vp, i32, vp]
     L.qr_apply.argtypes = [vp, i32, vp, vp, i32, i32, vp]

@@ -18,7 +18,8 @@ OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libqrusty_gpu.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
-SOURCES = ["qr_host.cu", "qr_apply.cu", "qr_csr.cu", "qr_reduce.cu", "qr_vec.cu", "qr_coef.cu"]
+SOURCES = ["qr_host.cu", "qr_apply.cu", "qr_csr.cu", "qr_reduce.cu", "qr_vec.cu", "qr_coef.cu",
+           "qr_group.cu"]
 HOST_SOURCES = ["qr_io.cpp"]  # host-only C++ (file formats), compiled by the host compiler
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",

@@ -23,18 +23,12 @@ __global__ void __launch_bounds__(256) merge_coeffs_kernel(uint32_t M, const uin
         double2 v = make_double2(0.0, 0.0);
         for (uint32_t t = mm_off[i]; t < mm_off[i + 1]; ++t) {
             const uint32_t k = mm_terms[t];
-            const double2 b = coeff[k];
-            // m(phase) = (1, -i, -1, +i)[phase]; (ar br - ai bi, ar bi + ai br)
-            const uint32_t ph = phase[k] & 3u;
-            const double ar = ph == 0 ? 1.0 : (ph == 2 ? -1.0 : 0.0);
-            const double ai = ph == 1 ? -1.0 : (ph == 3 ? 1.0 : 0.0);
-            const double cr = __dsub_rn(__dmul_rn(ar, b.x), __dmul_rn(ai, b.y));
-            const double ci = __dadd_rn(__dmul_rn(ar, b.y), __dmul_rn(ai, b.x));
+            const double2 c = make_param(coeff[k], phase[k]);
             if (t == mm_off[i]) {
-                v = make_double2(cr, ci);
+                v = c;
             } else {
-                v.x = __dadd_rn(v.x, cr);
-                v.y = __dadd_rn(v.y, ci);
+                v.x = __dadd_rn(v.x, c.x);
+                v.y = __dadd_rn(v.y, c.y);
             }
         }
         mc[i] = v;

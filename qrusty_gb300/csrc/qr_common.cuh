@@ -147,6 +147,17 @@ cudaError_t launch_coef_program(const CoefSlot *slots, uint32_t nslots, const ui
                                 const uint8_t *coord, const double2 *mc, const uint8_t *madj,
                                 int adjoint, cudaStream_t st);
 
+// c'_k = m(phase_k) * c_k (make_params, qrusty/src/accel.rs:141-157):
+// m = (1, -i, -1, +i)[phase], num-complex's product (ar br - ai bi,
+// ar bi + ai br) with every operation rounded on its own (no FMA).
+__device__ __forceinline__ double2 make_param(double2 b, uint32_t phase) {
+    const uint32_t ph = phase & 3u;
+    const double ar = ph == 0 ? 1.0 : (ph == 2 ? -1.0 : 0.0);
+    const double ai = ph == 1 ? -1.0 : (ph == 3 ? 1.0 : 0.0);
+    return make_double2(__dsub_rn(__dmul_rn(ar, b.x), __dmul_rn(ai, b.y)),
+                        __dadd_rn(__dmul_rn(ar, b.y), __dmul_rn(ai, b.x)));
+}
+
 // Device error codes written to the error word.
 enum : int { kErrNone = 0, kErrMbarTimeout = 1, kErrCsrPos = 2 };
 
@@ -240,6 +251,50 @@ struct CsrArgs {
     int wide;                 // 64-bit row words (the n > 32 kernels) forced (test hook)
 };
 cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st);
+
+// qr_group.cu: term grouping on the device.  Buffers sized for T terms (the
+// group counts are bounded by T).
+struct TermGroupsOut {
+    uint32_t *order;     // T: input index of each term, stably sorted by x (CSR order)
+    uint64_t *tz;        // T: z of the terms in CSR order
+    uint64_t *gx;        // G: distinct x, ascending
+    uint32_t *goff;      // G + 1: CSR group g = terms [goff[g], goff[g + 1]) in CSR order
+    uint32_t *mmap;      // T: merged string of each input term
+    uint32_t *mm_off;    // M + 1: merged string m folds terms mm_terms[mm_off[m] ..]
+    uint32_t *mm_terms;  // T: input indices, per merged string in input order
+    uint64_t *mx, *mz;   // M: merged strings, first-occurrence order
+    uint8_t *madj;       // M: popc(x & z) & 1 (adjoint sign)
+    uint32_t *ag_off;    // Ga + 1: x-groups of the merged strings (first-occurrence order)
+    uint32_t *ag_mem;    // M: merged indices per x-group, ascending
+};
+struct TermGroupCounts {
+    uint64_t G = 0, M = 0, Ga = 0;
+};
+// Synchronises st; returns the counts.
+cudaError_t group_terms(int n, uint64_t T, const uint64_t *x, const uint64_t *z,
+                        const TermGroupsOut &o, TermGroupCounts *cnt, cudaStream_t st);
+
+struct CsrStructOut {
+    uint64_t *pmask;  // G
+    int32_t *sig;     // G x n
+    CsrGroup *grp;    // G
+    uint16_t *coord;  // T: span coordinates of each term (CSR order)
+    uint32_t *fold;   // <= G: fold-mode groups
+    uint64_t *pbeta;  // <= G x kCsrPrefixRank
+};
+struct CsrStructCounts {
+    uint64_t nctab = 0, nptab = 0;
+    uint32_t nfold = 0;
+};
+// Mask-only CSR tables; synchronises st and returns the table sizes.
+cudaError_t csr_structure(int n, uint64_t G, const uint64_t *gx, const uint32_t *goff,
+                          const uint64_t *tz, const CsrStructOut &o, CsrStructCounts *cnt,
+                          cudaStream_t st);
+// Coefficient-dependent CSR tables (tc, zero-part flags, class and prefix
+// tables) from the raw coefficients: stream-ordered, no synchronisation.
+cudaError_t csr_values(uint64_t G, uint64_t T, const uint32_t *order, const double2 *coef,
+                       const uint8_t *phase, double2 *tc, CsrGroup *grp, const uint16_t *coord,
+                       double2 *ctab, double2 *ptab, cudaStream_t st);
 cudaError_t launch_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
                             const uint64_t *indices, const double *data, const double *v,
                             double *y, int nsm, cudaStream_t st);

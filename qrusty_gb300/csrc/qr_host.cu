@@ -18,7 +18,6 @@
 #include <map>
 #include <mutex>
 #include <string>
-#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -141,28 +140,26 @@ struct qr_op {
     uint64_t N = 0, T = 0;
     int device = 0;
     int nsm = 0;
-    // input terms (input order)
-    std::vector<uint64_t> x, z;
-    std::vector<cd> cp;  // c'_k
-    // CSR tables: groups by x ascending, terms stable within group
-    uint64_t G = 0;
-    std::vector<uint64_t> gx;
-    std::vector<uint32_t> goff;
-    std::vector<uint64_t> tz;
-    std::vector<cd> tc;
-    std::vector<uint64_t> pmask;        // per group: bits with a nonzero sigma
-    std::vector<int32_t> sig;           // G x n: sigma_{g,b}
-    bool csr_uploaded = false;
-    uint32_t nfold = 0, nctab = 0;
-    DevBuf d_gx, d_goff, d_tz, d_tc, d_pmask, d_sig, d_grp, d_ctab, d_fold, d_pbeta, d_ptab, d_fv;
-    // merged terms (FP64 simplification) for qr_apply; mmap[k] = merged index
-    std::vector<uint64_t> mx, mz;
+    // input terms on the device: masks, phases and the last coefficients
+    // (input order); every table below is derived from them on the device
+    DevBuf d_x, d_z, d_ph, d_coef;
+    // grouping on the device (qr_group.cu): CSR order and the ascending x
+    // groups, the merged strings (FP64 simplification, first-occurrence
+    // order) with each one's input terms, the apply plan's x-groups
+    uint64_t G = 0, M = 0, Ga = 0;
+    DevBuf d_order, d_tz, d_gx, d_goff, d_mmap, d_mm_off, d_mm_terms, d_mx, d_mz, d_madj;
+    DevBuf d_ag_off, d_ag_mem, d_mc;
+    // host copies of the grouping, read by the apply plan builder and the
+    // operator diagonal; mc is refetched from d_mc while host_coef_stale
+    std::vector<uint64_t> gx, mx, mz;
+    std::vector<uint32_t> goff, ag_off, ag_mem;
     std::vector<cd> mc;
-    std::vector<uint32_t> mmap;
-    std::vector<uint8_t> ph;            // input phases
-    std::vector<uint64_t> csr_order;    // input index of CSR term i
-    DevBuf d_mx, d_mz, d_mmap, d_ph;    // term-gradient tables (lazy)
-    bool grad_uploaded = false;
+    bool host_coef_stale = false;
+    // CSR tables, built on the device on first use; their coefficient parts
+    // follow every coefficient update on the device
+    bool csr_ready = false;
+    uint32_t nfold = 0, nctab = 0;
+    DevBuf d_tc, d_pmask, d_sig, d_grp, d_coord, d_ctab, d_fold, d_pbeta, d_ptab, d_fv;
     DevBuf expect_y;                    // H psi buffer of qr_expect
     Plan plans[2][2];  // [dtype][adjoint]
     Plan bplans[13];   // compensated-c64 plans with an explicit tile width (batched launches)
@@ -176,13 +173,6 @@ struct qr_op {
     // operator compares it with the value it recorded and rebuilds when they
     // differ (device updates rewrite the built tables in place instead)
     uint64_t coef_gen = 0;
-    // device coefficient updates (qr_op_set_coeffs_device): the last input,
-    // the merged-string fold lists, merged coefficients, adjoint signs and
-    // input phases on the device; host_coef_stale while cp / mc / tc on the
-    // host are older than d_coef
-    DevBuf d_coef, d_mc, d_mm_off, d_mm_terms, d_madj, d_cphase;
-    bool dev_coef_ready = false;
-    bool host_coef_stale = false;
     // test hooks (qr_op_set_test_hooks): mbarrier wait bound (0 = default),
     // withheld ring step (-1 = none), 64-bit row words forced
     uint64_t test_wait_ns = 0;
@@ -192,63 +182,6 @@ struct qr_op {
 
 namespace {
 
-// ---------------------------------------------------------------- CSR trie
-// Recursive split of the ascending x masks [lo, hi) at bit `bit`: records,
-// for every element, its sibling-subtree size at each branching bit.
-void build_trie(const std::vector<uint64_t> &gx, size_t lo, size_t hi, int bit,
-                std::vector<std::vector<std::pair<uint8_t, int64_t>>> &ent) {
-    while (bit >= 0 && hi - lo > 1) {
-        const uint64_t m = 1ull << bit;
-        // first index in [lo, hi) with bit set (sorted ascending, common prefix above bit)
-        size_t mid = lo;
-        while (mid < hi && !(gx[mid] & m)) ++mid;
-        if (mid > lo && mid < hi) {
-            const int64_t s0 = (int64_t)(mid - lo), s1 = (int64_t)(hi - mid);
-            for (size_t i = lo; i < mid; ++i) ent[i].push_back({(uint8_t)bit, +s1});
-            for (size_t i = mid; i < hi; ++i) ent[i].push_back({(uint8_t)bit, -s0});
-            build_trie(gx, lo, mid, bit - 1, ent);
-            lo = mid;  // continue with the 1-side iteratively
-        }
-        --bit;
-    }
-}
-
-int prepare_csr_tables(qr_op *op) {
-    const uint64_t T = op->T;
-    std::vector<uint64_t> order(T);
-    for (uint64_t k = 0; k < T; ++k) order[k] = k;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](uint64_t a, uint64_t b) { return op->x[a] < op->x[b]; });
-    op->gx.clear();
-    op->goff.clear();
-    op->tz.resize(T);
-    op->tc.resize(T);
-    for (uint64_t i = 0; i < T; ++i) {
-        const uint64_t k = order[i];
-        if (i == 0 || op->x[k] != op->gx.back()) {
-            op->gx.push_back(op->x[k]);
-            op->goff.push_back((uint32_t)i);
-        }
-        op->tz[i] = op->z[k];
-        op->tc[i] = op->cp[k];
-    }
-    op->goff.push_back((uint32_t)T);
-    op->G = op->gx.size();
-    op->csr_order = order;
-    std::vector<std::vector<std::pair<uint8_t, int64_t>>> ent(op->G);
-    build_trie(op->gx, 0, op->G, op->n - 1, ent);
-    if (op->G >= (1ull << 31)) return fail(QR_EINVAL, "qr_op_create: too many distinct x masks");
-    op->pmask.assign(op->G, 0);
-    op->sig.assign(op->G * (uint64_t)op->n, 0);
-    for (uint64_t g = 0; g < op->G; ++g) {
-        for (auto &e : ent[g]) {
-            op->pmask[g] |= 1ull << e.first;
-            op->sig[g * op->n + e.first] = (int32_t)e.second;
-        }
-    }
-    return QR_OK;
-}
-
 struct Span {
     std::vector<uint64_t> basis;
     std::vector<uint64_t> coord;  // per term
@@ -257,184 +190,62 @@ struct Span {
 };
 Span gf2_span(const std::vector<uint64_t> &zs, size_t dmax);
 
-// Per group: position-formula range and either the class table (the
-// term-order fold of +-c'_k for every sign class; same additions in the same
-// order as make_row, so the same bits) or the term range for a per-row fold.
-// Term-order fold of terms [k0, k0 + m) for every sign class of a span
-// (class bit 0: parity against z0, bit j+1: against basis j): the additions
-// of make_row, in its order, once per class.
-void fold_classes(const qr_op *op, uint32_t k0, size_t m, const Span &sp, std::vector<cd> &out) {
-    const uint32_t ncls = 2u << sp.basis.size();
-    for (uint32_t c = 0; c < ncls; ++c) {
-        cd v{0.0, 0.0};
-        for (uint32_t k = k0; k < k0 + m; ++k) {
-            const uint64_t sel = 1ull | (sp.coord[k - k0] << 1);
-            const bool neg = (__builtin_popcountll(c & sel) & 1) != 0;
-            const cd t = neg ? cd{-op->tc[k].re, -op->tc[k].im} : op->tc[k];
-            if (k == k0) v = t;
-            else v = cd{v.re + t.re, v.im + t.im};
-        }
-        out.push_back(v);
-    }
-}
-
-void build_csr_groups(const qr_op *op, std::vector<CsrGroup> &grp, std::vector<cd> &ctab,
-                      std::vector<uint32_t> &fold, std::vector<uint64_t> &pbeta,
-                      std::vector<cd> &ptab) {
-    grp.assign(op->G, CsrGroup{});
-    ctab.clear();
-    fold.clear();
-    pbeta.clear();
-    ptab.clear();
-    for (uint64_t g = 0; g < op->G; ++g) {
-        CsrGroup &d = grp[g];
-        const uint32_t k0 = op->goff[g], k1 = op->goff[g + 1];
-        d.k0 = k0;
-        d.k1 = k1;
-        d.z0 = op->tz[k0];
-        std::vector<uint64_t> zs(op->tz.begin() + k0, op->tz.begin() + k1);
-        Span sp = gf2_span(zs, kCsrMaxRank);
-        if (sp.overflow) {
-            d.d = kCsrFold;
-            d.tab = 0;
-            // a part whose every coefficient is +-0 folds to a zero whose sign
-            // the kernel derives without FP64 additions
-            bool rz = true, iz = true;
-            for (uint32_t k = k0; k < k1; ++k) {
-                rz = rz && op->tc[k].re == 0.0;
-                iz = iz && op->tc[k].im == 0.0;
-            }
-            d.zparts = (rz ? 1u : 0u) | (iz ? 2u : 0u);
-            // leading terms of rank <= kCsrPrefixRank: one table read per row
-            const Span pp = gf2_span(zs, kCsrPrefixRank);
-            const size_t m = pp.used;
-            d.pre = 0;
-            if (m >= 2) {
-                d.tab = (uint32_t)ptab.size();
-                d.pre = (uint32_t)m | ((uint32_t)pp.basis.size() << 24);
-                fold_classes(op, k0, m, pp, ptab);
-            }
-            for (int j = 0; j < kCsrPrefixRank; ++j)
-                pbeta.push_back(j < (int)pp.basis.size() ? pp.basis[j] : 0ull);
-            fold.push_back((uint32_t)g);
-            continue;
-        }
-        d.d = (uint32_t)sp.basis.size();
-        for (uint32_t j = 0; j < d.d; ++j) d.beta[j] = sp.basis[j];
-        d.tab = (uint32_t)ctab.size();
-        fold_classes(op, k0, k1 - k0, sp, ctab);
-    }
-}
-
-int sync_host_coeffs(qr_op *op);
-
-int upload_csr_tables(qr_op *op) {
-    if (op->csr_uploaded) return QR_OK;
-    {
-        const int rc = sync_host_coeffs(op);
-        if (rc) return rc;
-        if (op->csr_uploaded) return QR_OK;
-    }
-    std::vector<CsrGroup> grp;
-    std::vector<cd> ctab;
-    std::vector<uint32_t> fold;
-    std::vector<uint64_t> pbeta;
-    std::vector<cd> ptab;
-    build_csr_groups(op, grp, ctab, fold, pbeta, ptab);
-    if (ctab.size() > 0xffffffffull) return fail(QR_EINVAL, "qr_csr_build: class tables too large");
-    QR_CUDA(op->d_gx.upload(op->gx), "upload gx");
-    QR_CUDA(op->d_goff.upload(op->goff), "upload goff");
-    QR_CUDA(op->d_tz.upload(op->tz), "upload tz");
-    QR_CUDA(op->d_tc.upload(op->tc), "upload tc");
-    QR_CUDA(op->d_pmask.upload(op->pmask), "upload position masks");
-    QR_CUDA(op->d_sig.upload(op->sig), "upload position table");
-    QR_CUDA(op->d_grp.upload(grp), "upload group descriptors");
-    QR_CUDA(op->d_ctab.upload(ctab), "upload class tables");
-    op->nctab = (uint32_t)ctab.size();
-    QR_CUDA(op->d_fold.upload(fold), "upload fold groups");
-    if (pbeta.empty()) pbeta.push_back(0);
-    if (ptab.empty()) ptab.push_back(cd{0.0, 0.0});
-    QR_CUDA(op->d_pbeta.upload(pbeta), "upload prefix bases");
-    QR_CUDA(op->d_ptab.upload(ptab), "upload prefix tables");
-    op->nfold = (uint32_t)fold.size();
-    op->csr_uploaded = true;
-    return QR_OK;
-}
-
-// ---------------------------------------------------------------- merging
-void merge_terms(qr_op *op) {
-    struct H {
-        size_t operator()(const std::pair<uint64_t, uint64_t> &p) const {
-            return std::hash<uint64_t>()(p.first * 0x9E3779B97F4A7C15ull ^ p.second);
-        }
-    };
-    std::unordered_map<std::pair<uint64_t, uint64_t>, size_t, H> idx;
-    idx.reserve(op->T * 2);
-    op->mx.clear();
-    op->mz.clear();
-    op->mc.clear();
-    op->mmap.assign(op->T, 0);
-    for (uint64_t k = 0; k < op->T; ++k) {
-        auto key = std::make_pair(op->x[k], op->z[k]);
-        auto it = idx.find(key);
-        if (it == idx.end()) {
-            op->mmap[k] = (uint32_t)op->mx.size();
-            idx.emplace(key, op->mx.size());
-            op->mx.push_back(op->x[k]);
-            op->mz.push_back(op->z[k]);
-            op->mc.push_back(op->cp[k]);
-        } else {
-            op->mmap[k] = (uint32_t)it->second;
-            cd &c = op->mc[it->second];
-            c.re += op->cp[k].re;
-            c.im += op->cp[k].im;
-        }
-    }
-}
-
-// c'_k = m(phase_k) * c_k (make_params, qrusty/src/accel.rs:141-157: the
-// num-complex product, no FMA), the CSR-ordered copy, and the merged sums
-// (first term, then additions in input order, as merge_terms forms them).
-// Built plans are left as they are.
-void apply_host_coeffs(qr_op *op, const double *coeff) {
-    static const cd m[4] = {{1.0, 0.0}, {0.0, -1.0}, {-1.0, 0.0}, {0.0, 1.0}};
-    for (uint64_t k = 0; k < op->T; ++k) {
-        const cd a = m[op->ph[k] & 3];
-        const cd b{coeff[2 * k], coeff[2 * k + 1]};
-        op->cp[k].re = a.re * b.re - a.im * b.im;
-        op->cp[k].im = a.re * b.im + a.im * b.re;
-    }
-    for (uint64_t i = 0; i < op->T; ++i) op->tc[i] = op->cp[op->csr_order[i]];
-    op->csr_uploaded = false;
-    if (!op->mx.empty()) {
-        for (auto &c : op->mc) c = cd{0.0, 0.0};
-        std::vector<bool> seen(op->mx.size(), false);
-        for (uint64_t k = 0; k < op->T; ++k) {
-            const uint32_t mi = op->mmap[k];
-            if (!seen[mi]) {
-                op->mc[mi] = op->cp[k];
-                seen[mi] = true;
-            } else {
-                op->mc[mi].re += op->cp[k].re;
-                op->mc[mi].im += op->cp[k].im;
-            }
-        }
-    }
-}
-
-// After a device coefficient update the host copies (cp, tc, mc) are older
-// than the device ones: fetch the last device input (synchronous) before any
-// host-side use -- a plan built later, the CSR tables, the diagonal.
+// ---------------------------------------------------------------- coefficients
+// After a device coefficient update the host copy of the merged coefficients
+// is older than d_mc: fetch it (synchronous) before a plan is built.
 int sync_host_coeffs(qr_op *op) {
     if (!op->host_coef_stale) return QR_OK;
     // the update ran on the caller's stream, which may not be ordered with
     // the legacy stream: wait for the device
-    QR_CUDA(cudaDeviceSynchronize(), "fetch device coefficients: sync");
-    std::vector<double> c(2 * op->T);
-    QR_CUDA(cudaMemcpy(c.data(), op->d_coef.p, c.size() * sizeof(double), cudaMemcpyDeviceToHost),
-            "fetch device coefficients");
-    apply_host_coeffs(op, c.data());
+    QR_CUDA(cudaDeviceSynchronize(), "fetch merged coefficients: sync");
+    op->mc.resize(op->M);
+    QR_CUDA(cudaMemcpy(op->mc.data(), op->d_mc.p, op->M * sizeof(cd), cudaMemcpyDeviceToHost),
+            "fetch merged coefficients");
     op->host_coef_stale = false;
+    return QR_OK;
+}
+
+// Coefficient-dependent CSR tables from d_coef, on stream st.
+int refresh_csr_values(qr_op *op, cudaStream_t st) {
+    QR_CUDA(csr_values(op->G, op->T, op->d_order.as<uint32_t>(), op->d_coef.as<double2>(),
+                       op->d_ph.as<uint8_t>(), op->d_tc.as<double2>(), op->d_grp.as<CsrGroup>(),
+                       op->d_coord.as<uint16_t>(), op->d_ctab.as<double2>(),
+                       op->d_ptab.as<double2>(), st),
+            "CSR coefficient tables");
+    return QR_OK;
+}
+
+// CSR tables on the device, once per operator (qr_group.cu): the position
+// trie, group spans and descriptors, then the coefficient parts.
+int upload_csr_tables(qr_op *op) {
+    if (op->csr_ready) return QR_OK;
+    // d_coef may have been written on another stream
+    QR_CUDA(cudaDeviceSynchronize(), "CSR tables: sync");
+    const uint64_t G = op->G, T = op->T;
+    QR_CUDA(op->d_pmask.alloc(G * sizeof(uint64_t)), "alloc position masks");
+    QR_CUDA(op->d_sig.alloc(G * op->n * sizeof(int32_t)), "alloc position table");
+    QR_CUDA(op->d_grp.alloc(G * sizeof(CsrGroup)), "alloc group descriptors");
+    QR_CUDA(op->d_coord.alloc(T * sizeof(uint16_t)), "alloc span coordinates");
+    QR_CUDA(op->d_fold.alloc(G * sizeof(uint32_t)), "alloc fold groups");
+    QR_CUDA(op->d_pbeta.alloc(G * kCsrPrefixRank * sizeof(uint64_t)), "alloc prefix bases");
+    QR_CUDA(op->d_tc.alloc(T * sizeof(cd)), "alloc CSR coefficients");
+    CsrStructOut o{op->d_pmask.as<uint64_t>(), op->d_sig.as<int32_t>(), op->d_grp.as<CsrGroup>(),
+                   op->d_coord.as<uint16_t>(), op->d_fold.as<uint32_t>(),
+                   op->d_pbeta.as<uint64_t>()};
+    CsrStructCounts cnt;
+    QR_CUDA(csr_structure(op->n, G, op->d_gx.as<uint64_t>(), op->d_goff.as<uint32_t>(),
+                          op->d_tz.as<uint64_t>(), o, &cnt, nullptr),
+            "CSR tables");
+    if (cnt.nctab > 0xffffffffull || cnt.nptab > 0xffffffffull)
+        return fail(QR_EINVAL, "qr_csr_build: class tables too large");
+    QR_CUDA(op->d_ctab.alloc(cnt.nctab * sizeof(cd)), "alloc class tables");
+    QR_CUDA(op->d_ptab.alloc(cnt.nptab * sizeof(cd)), "alloc prefix tables");
+    op->nctab = (uint32_t)cnt.nctab;
+    op->nfold = cnt.nfold;
+    int rc = refresh_csr_values(op, nullptr);
+    if (rc) return rc;
+    QR_CUDA(cudaStreamSynchronize(nullptr), "CSR tables: sync");
+    op->csr_ready = true;
     return QR_OK;
 }
 
@@ -509,7 +320,6 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         const int rc = sync_host_coeffs(op);
         if (rc) return rc;
     }
-    if (op->mx.empty()) merge_terms(op);
     pl.dtype = dtype;
     pl.adjoint = adjoint;
     // coefficient program (see CoefSlot): members packed per slot
@@ -553,20 +363,13 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
             }
         }
     }
-    // groups by x in first-occurrence order
-    std::vector<uint64_t> gxs;
-    std::unordered_map<uint64_t, size_t> gid;
-    std::vector<std::vector<size_t>> members;
-    for (size_t k = 0; k < M; ++k) {
-        auto it = gid.find(op->mx[k]);
-        if (it == gid.end()) {
-            gid.emplace(op->mx[k], gxs.size());
-            gxs.push_back(op->mx[k]);
-            members.emplace_back();
-            members.back().push_back(k);
-        } else {
-            members[it->second].push_back(k);
-        }
+    // x-groups of the merged strings in first-occurrence order (grouped on
+    // the device at creation)
+    std::vector<uint64_t> gxs(op->Ga);
+    std::vector<std::vector<size_t>> members(op->Ga);
+    for (size_t g = 0; g < op->Ga; ++g) {
+        members[g].assign(op->ag_mem.begin() + op->ag_off[g], op->ag_mem.begin() + op->ag_off[g + 1]);
+        gxs[g] = op->mx[members[g][0]];
     }
     // The compensated-c64 kernel keeps a sub-group's factor thread-constant
     // up to a Walsh sign over the register bits [tb, tb + log2 amps): split
@@ -998,6 +801,70 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
 // bound of every mbarrier wait of the apply kernels
 constexpr uint64_t kDefaultWaitNs = 2000000000ull;
 
+// Creation: upload the terms once, then group them on the device
+// (qr_group.cu) -- CSR order and groups, merged strings, the apply plan's
+// x-groups -- and fold the merged coefficients (merge_coeffs_kernel).  The
+// host keeps copies of what the apply plan builder reads.
+int create_tables(qr_op *op, const uint64_t *x, const uint64_t *z, const uint8_t *phase,
+                  const double *coeff) {
+    const uint64_t T = op->T;
+    QR_CUDA(op->d_err.alloc(sizeof(int)), "qr_op_create: device allocation");
+    QR_CUDA(cudaMemset(op->d_err.p, 0, sizeof(int)), "qr_op_create: clear error word");
+    QR_CUDA(op->d_x.alloc(T * 8), "alloc x masks");
+    QR_CUDA(op->d_z.alloc(T * 8), "alloc z masks");
+    QR_CUDA(op->d_ph.alloc(T), "alloc phases");
+    QR_CUDA(op->d_coef.alloc(T * sizeof(cd)), "alloc coefficients");
+    QR_CUDA(cudaMemcpy(op->d_x.p, x, T * 8, cudaMemcpyHostToDevice), "upload x masks");
+    QR_CUDA(cudaMemcpy(op->d_z.p, z, T * 8, cudaMemcpyHostToDevice), "upload z masks");
+    QR_CUDA(cudaMemcpy(op->d_ph.p, phase, T, cudaMemcpyHostToDevice), "upload phases");
+    QR_CUDA(cudaMemcpy(op->d_coef.p, coeff, T * sizeof(cd), cudaMemcpyHostToDevice),
+            "upload coefficients");
+    DevBuf *u32s[] = {&op->d_order, &op->d_mmap, &op->d_mm_terms, &op->d_ag_mem};
+    for (DevBuf *b : u32s) QR_CUDA(b->alloc(T * 4), "alloc grouping tables");
+    DevBuf *offs[] = {&op->d_goff, &op->d_mm_off, &op->d_ag_off};
+    for (DevBuf *b : offs) QR_CUDA(b->alloc((T + 1) * 4), "alloc grouping offsets");
+    DevBuf *u64s[] = {&op->d_tz, &op->d_gx, &op->d_mx, &op->d_mz};
+    for (DevBuf *b : u64s) QR_CUDA(b->alloc(T * 8), "alloc grouping masks");
+    QR_CUDA(op->d_madj.alloc(T), "alloc adjoint signs");
+    TermGroupsOut o{op->d_order.as<uint32_t>(), op->d_tz.as<uint64_t>(), op->d_gx.as<uint64_t>(),
+                    op->d_goff.as<uint32_t>(), op->d_mmap.as<uint32_t>(),
+                    op->d_mm_off.as<uint32_t>(), op->d_mm_terms.as<uint32_t>(),
+                    op->d_mx.as<uint64_t>(), op->d_mz.as<uint64_t>(), op->d_madj.as<uint8_t>(),
+                    op->d_ag_off.as<uint32_t>(), op->d_ag_mem.as<uint32_t>()};
+    TermGroupCounts cnt;
+    QR_CUDA(group_terms(op->n, T, op->d_x.as<uint64_t>(), op->d_z.as<uint64_t>(), o, &cnt,
+                        nullptr),
+            "qr_op_create: grouping terms");
+    op->G = cnt.G;
+    op->M = cnt.M;
+    op->Ga = cnt.Ga;
+    QR_CUDA(op->d_mc.alloc(op->M * sizeof(cd)), "alloc merged coefficients");
+    QR_CUDA(launch_merge_coeffs((uint32_t)op->M, op->d_mm_off.as<uint32_t>(),
+                                op->d_mm_terms.as<uint32_t>(), op->d_coef.as<double2>(),
+                                op->d_ph.as<uint8_t>(), op->d_mc.as<double2>(), nullptr),
+            "merge coefficients");
+    op->gx.resize(op->G);
+    op->goff.resize(op->G + 1);
+    op->mx.resize(op->M);
+    op->mz.resize(op->M);
+    op->mc.resize(op->M);
+    op->ag_off.resize(op->Ga + 1);
+    op->ag_mem.resize(op->M);
+    QR_CUDA(cudaMemcpy(op->gx.data(), op->d_gx.p, op->G * 8, cudaMemcpyDeviceToHost), "fetch gx");
+    QR_CUDA(cudaMemcpy(op->goff.data(), op->d_goff.p, (op->G + 1) * 4, cudaMemcpyDeviceToHost),
+            "fetch group offsets");
+    QR_CUDA(cudaMemcpy(op->mx.data(), op->d_mx.p, op->M * 8, cudaMemcpyDeviceToHost), "fetch mx");
+    QR_CUDA(cudaMemcpy(op->mz.data(), op->d_mz.p, op->M * 8, cudaMemcpyDeviceToHost), "fetch mz");
+    QR_CUDA(cudaMemcpy(op->mc.data(), op->d_mc.p, op->M * sizeof(cd), cudaMemcpyDeviceToHost),
+            "fetch merged coefficients");
+    QR_CUDA(cudaMemcpy(op->ag_off.data(), op->d_ag_off.p, (op->Ga + 1) * 4,
+                       cudaMemcpyDeviceToHost),
+            "fetch x-group offsets");
+    QR_CUDA(cudaMemcpy(op->ag_mem.data(), op->d_ag_mem.p, op->M * 4, cudaMemcpyDeviceToHost),
+            "fetch x-group members");
+    return QR_OK;
+}
+
 int check_device(const qr_op *op) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -1048,19 +915,6 @@ int qr_op_create(int32_t n, uint64_t nterms, const uint64_t *x, const uint64_t *
     op->n = n;
     op->N = 1ull << n;
     op->T = nterms;
-    op->x.assign(x, x + nterms);
-    op->z.assign(z, z + nterms);
-    op->ph.assign(phase, phase + nterms);
-    op->cp.resize(nterms);
-    // make_params (qrusty/src/accel.rs:141-157): c' = m(phase) * c, with
-    // num-complex's product (ar*br - ai*bi, ar*bi + ai*br), no FMA.
-    static const cd m[4] = {{1.0, 0.0}, {0.0, -1.0}, {-1.0, 0.0}, {0.0, 1.0}};
-    for (uint64_t k = 0; k < nterms; ++k) {
-        const cd a = m[phase[k] & 3];
-        const cd b{coeff[2 * k], coeff[2 * k + 1]};
-        op->cp[k].re = a.re * b.re - a.im * b.im;
-        op->cp[k].im = a.re * b.im + a.im * b.re;
-    }
     cudaError_t e = cudaGetDevice(&op->device);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&op->nsm, cudaDevAttrMultiProcessorCount, op->device);
@@ -1068,16 +922,10 @@ int qr_op_create(int32_t n, uint64_t nterms, const uint64_t *x, const uint64_t *
         delete op;
         return cuda_fail(e, "qr_op_create: no usable CUDA device");
     }
-    int rc = prepare_csr_tables(op);
+    const int rc = create_tables(op, x, z, phase, coeff);
     if (rc) {
         delete op;
         return rc;
-    }
-    e = op->d_err.alloc(sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(op->d_err.p, 0, sizeof(int));
-    if (e != cudaSuccess) {
-        delete op;
-        return cuda_fail(e, "qr_op_create: device allocation");
     }
     *out = op;
     return QR_OK;
@@ -1119,12 +967,30 @@ int qr_op_get_info(const qr_op *op_c, qr_op_info *info) {
     info->tile_bits = pl.b;
     info->nterms = op->T;
     info->ngroups = op->G;
-    info->nmerged = op->mx.size();
+    info->nmerged = op->M;
     info->nblocks = pl.nblocks;
     info->nfat = op->plans[QR_C128][0].nfat;
     info->nsub = pl.nsub;
     info->has_diag = pl.has_diag ? 1 : 0;
     info->device = op->device;
+    return QR_OK;
+}
+
+int qr_op_get_groups(const qr_op *op, uint64_t *ngroups, uint64_t *gx, uint32_t *goff,
+                     uint32_t *order, uint32_t *mmap) {
+    if (!op || !ngroups) return fail(QR_EINVAL, "qr_op_get_groups: null argument");
+    int rc = check_device(op);
+    if (rc) return rc;
+    *ngroups = op->G;
+    QR_CUDA(cudaDeviceSynchronize(), "qr_op_get_groups sync");
+    if (gx) std::memcpy(gx, op->gx.data(), op->G * sizeof(uint64_t));
+    if (goff) std::memcpy(goff, op->goff.data(), (op->G + 1) * sizeof(uint32_t));
+    if (order)
+        QR_CUDA(cudaMemcpy(order, op->d_order.p, op->T * 4, cudaMemcpyDeviceToHost),
+                "fetch term order");
+    if (mmap)
+        QR_CUDA(cudaMemcpy(mmap, op->d_mmap.p, op->T * 4, cudaMemcpyDeviceToHost),
+                "fetch merged-string map");
     return QR_OK;
 }
 
@@ -1463,13 +1329,26 @@ int qr_op_diagonal(qr_op *op, int32_t dtype, void *out, void *stream) {
     return QR_OK;
 }
 
+// Merged coefficients and the built CSR tables from d_coef, on stream st.
+static int recompute_coeffs(qr_op *op, cudaStream_t st) {
+    QR_CUDA(launch_merge_coeffs((uint32_t)op->M, op->d_mm_off.as<uint32_t>(),
+                                op->d_mm_terms.as<uint32_t>(), op->d_coef.as<double2>(),
+                                op->d_ph.as<uint8_t>(), op->d_mc.as<double2>(), st),
+            "merge coefficients");
+    if (op->csr_ready) return refresh_csr_values(op, st);
+    return QR_OK;
+}
+
 int qr_op_set_coeffs(qr_op *op, const double *coeff) {
     if (!op || !coeff) return fail(QR_EINVAL, "qr_op_set_coeffs: null argument");
     int rc = check_device(op);
     if (rc) return rc;
     QR_CUDA(cudaDeviceSynchronize(), "qr_op_set_coeffs sync");
-    apply_host_coeffs(op, coeff);
-    op->host_coef_stale = false;
+    QR_CUDA(cudaMemcpy(op->d_coef.p, coeff, op->T * sizeof(cd), cudaMemcpyHostToDevice),
+            "upload coefficients");
+    rc = recompute_coeffs(op, nullptr);
+    if (rc) return rc;
+    op->host_coef_stale = true;  // plans built below fetch the new merged sums
     for (int d = 0; d < 2; ++d)
         for (int j = 0; j < 2; ++j) op->plans[d][j].built = false;
     // plans are rebuilt on next use into the buffers they already hold
@@ -1483,34 +1362,11 @@ int qr_op_set_coeffs_device(qr_op *op, const double *coeff, void *stream) {
     int rc = check_device(op);
     if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (!op->dev_coef_ready) {
-        // one-time (synchronous) upload of the fold structure: per merged
-        // string its input terms in input order, the adjoint sign
-        // parity(x & z), and the input phases
-        if (op->mx.empty()) merge_terms(op);
-        const size_t M = op->mx.size();
-        std::vector<uint32_t> off(M + 1, 0), terms(op->T);
-        for (uint64_t k = 0; k < op->T; ++k) ++off[op->mmap[k] + 1];
-        for (size_t i = 0; i < M; ++i) off[i + 1] += off[i];
-        std::vector<uint32_t> fill(off.begin(), off.end() - 1);
-        for (uint64_t k = 0; k < op->T; ++k) terms[fill[op->mmap[k]]++] = (uint32_t)k;
-        std::vector<uint8_t> adj(M);
-        for (size_t i = 0; i < M; ++i) adj[i] = __builtin_popcountll(op->mx[i] & op->mz[i]) & 1;
-        QR_CUDA(op->d_mm_off.upload(off), "upload merge offsets");
-        QR_CUDA(op->d_mm_terms.upload(terms), "upload merge terms");
-        QR_CUDA(op->d_madj.upload(adj), "upload adjoint signs");
-        QR_CUDA(op->d_cphase.upload(op->ph), "upload phases");
-        QR_CUDA(op->d_coef.alloc(op->T * 2 * sizeof(double)), "alloc device coefficients");
-        QR_CUDA(op->d_mc.alloc(M * sizeof(double2)), "alloc merged coefficients");
-        op->dev_coef_ready = true;
-    }
-    QR_CUDA(cudaMemcpyAsync(op->d_coef.p, coeff, op->T * 2 * sizeof(double),
-                            cudaMemcpyDeviceToDevice, st),
+    QR_CUDA(cudaMemcpyAsync(op->d_coef.p, coeff, op->T * sizeof(cd), cudaMemcpyDeviceToDevice,
+                            st),
             "copy device coefficients");
-    QR_CUDA(launch_merge_coeffs((uint32_t)op->mx.size(), op->d_mm_off.as<uint32_t>(),
-                                op->d_mm_terms.as<uint32_t>(), op->d_coef.as<double2>(),
-                                op->d_cphase.as<uint8_t>(), op->d_mc.as<double2>(), st),
-            "merge coefficients");
+    rc = recompute_coeffs(op, st);
+    if (rc) return rc;
     auto refresh = [&](Plan &pl) -> int {
         if (!pl.built) return QR_OK;
         QR_CUDA(launch_coef_program(pl.cslots.as<CoefSlot>(), pl.nslots, pl.cmem.as<uint32_t>(),
@@ -1534,7 +1390,6 @@ int qr_op_set_coeffs_device(qr_op *op, const double *coeff, void *stream) {
         if (rc) return rc;
     }
     op->host_coef_stale = true;
-    op->csr_uploaded = false;
     return QR_OK;
 }
 
@@ -1599,16 +1454,8 @@ int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32
     if (op->n > 40) return fail(QR_EINVAL, "qr_term_grad: n=%d too large", op->n);
     int rc = check_device(op);
     if (rc) return rc;
-    if (op->mx.empty()) merge_terms(op);
-    if (!op->grad_uploaded) {
-        QR_CUDA(op->d_mx.upload(op->mx), "upload merged x");
-        QR_CUDA(op->d_mz.upload(op->mz), "upload merged z");
-        QR_CUDA(op->d_mmap.upload(op->mmap), "upload term map");
-        QR_CUDA(op->d_ph.upload(op->ph), "upload phases");
-        op->grad_uploaded = true;
-    }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const uint32_t nstr = (uint32_t)op->mx.size();
+    const uint32_t nstr = (uint32_t)op->M;
     // blocks take 4 strings each: enough chunks for ~8 blocks per SM
     const uint64_t nbatch = (nstr + 3) / 4;
     uint64_t nchunk = ((uint64_t)op->nsm * 8 + nbatch - 1) / nbatch;

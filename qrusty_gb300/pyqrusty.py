@@ -180,6 +180,23 @@ class PauliOperator:
         check(_lib.load().qr_op_get_info(self._h, C.byref(inf)))
         return {f: getattr(inf, f) for f, _ in inf._fields_}
 
+    def groups(self) -> dict:
+        """The term grouping made on the device at creation: ``gx`` (distinct
+        x, ascending), ``goff`` (group offsets into ``order``), ``order``
+        (input index of each term, stably sorted by x) and ``mmap`` (merged
+        (x, z) string of each input term, first-occurrence numbering)."""
+        L = _lib.load()
+        ng = C.c_uint64()
+        check(L.qr_op_get_groups(self._h, C.byref(ng), None, None, None, None))
+        G, T = ng.value, self.nterms
+        gx = np.empty(G, dtype=np.uint64)
+        goff = np.empty(G + 1, dtype=np.uint32)
+        order = np.empty(T, dtype=np.uint32)
+        mmap = np.empty(T, dtype=np.uint32)
+        check(L.qr_op_get_groups(self._h, C.byref(ng), gx.ctypes.data, goff.ctypes.data,
+                                 order.ctypes.data, mmap.ctypes.data))
+        return {"gx": gx, "goff": goff, "order": order, "mmap": mmap}
+
     def csr_size(self):
         nr, nz = C.c_uint64(), C.c_uint64()
         check(_lib.load().qr_csr_size(self._h, C.byref(nr), C.byref(nz)))
