@@ -316,5 +316,14 @@ cudaError_t launch_term_grad(int dtype, uint64_t N, int nstates, const uint64_t 
                              double2 *partial, uint32_t nchunk, uint64_t chunk, double2 *R,
                              uint64_t T, const uint32_t *map, const uint8_t *phase, double2 *out,
                              cudaStream_t st);
+// Tiled complex64 term gradients (n >= 12): strings sorted by partner tile
+// x >> 12 (sx, sz; perm = merged index of each), batches of <= 8 strings of
+// one partner tile as (first, count); partial holds nstr x nchunk entries.
+cudaError_t launch_term_grad_tiles(uint64_t N, int nstates, const uint64_t *sx, const uint64_t *sz,
+                                   const uint32_t *perm, const uint2 *batches, uint32_t nbatch,
+                                   uint32_t nstr, const void *psi, const void *g,
+                                   double2 *partial, uint32_t nchunk, double2 *R, uint64_t T,
+                                   const uint32_t *map, const uint8_t *phase, double2 *out,
+                                   int nsm, cudaStream_t st);
 
 }  // namespace qr

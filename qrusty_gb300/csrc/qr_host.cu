@@ -160,6 +160,11 @@ struct qr_op {
     bool csr_ready = false;
     uint32_t nfold = 0, nctab = 0;
     DevBuf d_tc, d_pmask, d_sig, d_grp, d_coord, d_ctab, d_fold, d_pbeta, d_ptab, d_fv;
+    // term-gradient batches (complex64, n >= 12): merged strings sorted by
+    // partner tile x >> 12, batches of <= 8 strings of one partner tile
+    bool tg_ready = false;
+    uint32_t tg_nbatch = 0;
+    DevBuf d_tg_x, d_tg_z, d_tg_perm, d_tg_bat;
     DevBuf expect_y;                    // H psi buffer of qr_expect
     Plan plans[2][2];  // [dtype][adjoint]
     Plan bplans[13];   // compensated-c64 plans with an explicit tile width (batched launches)
@@ -1456,6 +1461,55 @@ int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32
     if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const uint32_t nstr = (uint32_t)op->M;
+    if (dtype == QR_C64C && op->n >= 12) {
+        if (!op->tg_ready) {
+            // strings by partner tile, input order kept within one; batches
+            // of <= 8 never span two partner tiles, largest first
+            std::vector<uint32_t> ord(nstr);
+            for (uint32_t i = 0; i < nstr; ++i) ord[i] = i;
+            std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) {
+                return (op->mx[a] >> 12) < (op->mx[b] >> 12);
+            });
+            std::vector<uint64_t> sx(nstr), sz(nstr);
+            for (uint32_t i = 0; i < nstr; ++i) {
+                sx[i] = op->mx[ord[i]];
+                sz[i] = op->mz[ord[i]];
+            }
+            std::vector<uint2> bat;
+            for (uint32_t i = 0; i < nstr;) {
+                uint32_t j = i + 1;
+                while (j < nstr && j - i < 8 && (sx[j] >> 12) == (sx[i] >> 12)) ++j;
+                bat.push_back(make_uint2(i, j - i));
+                i = j;
+            }
+            std::stable_sort(bat.begin(), bat.end(),
+                             [](const uint2 &a, const uint2 &b) { return a.y > b.y; });
+            QR_CUDA(op->d_tg_x.upload(sx), "upload gradient strings");
+            QR_CUDA(op->d_tg_z.upload(sz), "upload gradient strings");
+            QR_CUDA(op->d_tg_perm.upload(ord), "upload gradient order");
+            QR_CUDA(op->d_tg_bat.upload(bat), "upload gradient batches");
+            op->tg_nbatch = (uint32_t)bat.size();
+            op->tg_ready = true;
+        }
+        const uint64_t TT = (op->N >> 12) * (uint64_t)nstates;
+        uint64_t nchunk = ((uint64_t)op->nsm * 4 + op->tg_nbatch - 1) / op->tg_nbatch;
+        if (nchunk > TT / 8) nchunk = TT / 8;
+        if (nchunk < 1) nchunk = 1;
+        void *scratch = nullptr;
+        const size_t pbytes = (size_t)nstr * nchunk * sizeof(double2);
+        QR_CUDA(cudaMallocAsync(&scratch, pbytes + (size_t)nstr * sizeof(double2), st),
+                "term-grad scratch");
+        double2 *partial = static_cast<double2 *>(scratch);
+        double2 *R = partial + (size_t)nstr * nchunk;
+        cudaError_t e = launch_term_grad_tiles(
+            op->N, nstates, op->d_tg_x.as<uint64_t>(), op->d_tg_z.as<uint64_t>(),
+            op->d_tg_perm.as<uint32_t>(), op->d_tg_bat.as<uint2>(), op->tg_nbatch, nstr, psi, g,
+            partial, (uint32_t)nchunk, R, op->T, op->d_mmap.as<uint32_t>(), op->d_ph.as<uint8_t>(),
+            reinterpret_cast<double2 *>(out), op->nsm, st);
+        cudaFreeAsync(scratch, st);
+        if (e != cudaSuccess) return cuda_fail(e, "term-grad launch");
+        return QR_OK;
+    }
     // blocks take 4 strings each: enough chunks for ~8 blocks per SM
     const uint64_t nbatch = (nstr + 3) / 4;
     uint64_t nchunk = ((uint64_t)op->nsm * 8 + nbatch - 1) / nbatch;

@@ -231,6 +231,290 @@ __global__ void __launch_bounds__(kRedThreads) term_grad_scatter_kernel(uint64_t
     }
 }
 
+// ---------------------------------------------------------------- term grads, tiled (complex64)
+// The merged strings are sorted by partner tile h = x >> 12 and cut into
+// batches of <= kTgB strings with one h.  A work item is (batch, chunk of
+// output tiles); per output tile (4,096 rows of one state) the CTA stages
+// the tile of g and the batch's partner tile of psi (tile ^ h) in shared
+// memory (cp.async, kTgStages stages), and thread i takes rows i + 512 j
+// (j < 8).  For string (x, z), row r = tile * 4096 + i + 512 j:
+//   psi[r ^ x] = partner row (i ^ (x & 511)) + 512 (j ^ l),  l = (x >> 9) & 7,
+//   (-1)^popc(r & z) = (-1)^popc(tile & (z >> 12)) (-1)^popc(i & z & 511)
+//                      (-1)^popc(j & w),                     w = (z >> 9) & 7,
+// so l is a compile-time case (shared-memory loads at immediate offsets) and
+// the register-bit signs are one three-level butterfly.  Packed FP32:
+// A = sum s gx p, B = sum s gy p with p = (px, py) give conj(p) g summed as
+// (A.x + B.y, B.x - A.y).  Every kTgFlush tiles a warp transpose-reduce sums
+// the 8 strings' FP32 values over the warp's lanes (16 shuffles for 16
+// values) and lane 2m adds value m to its FP64 sum; at the item's end the 16
+// warps' sums are added in warp order.  Deterministic: fixed order
+// everywhere, one partial per (string, chunk).
+constexpr int kTgThreads = 512;
+constexpr int kTgStages = 3;
+constexpr int kTgB = 8;        // strings per batch
+constexpr int kTgFlush = 4;    // tiles per FP32 window (32 rows per thread)
+constexpr uint32_t kTgTileBytes = 4096 * 8;
+constexpr uint32_t kTgStageBytes = 2 * kTgTileBytes;
+constexpr uint32_t kTgAlign = 32768;
+constexpr size_t kTgSmem = (size_t)kTgStages * kTgStageBytes + kTgAlign;
+
+__device__ __forceinline__ uint32_t tg_saddr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void tg_cp16(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void tg_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int K>
+__device__ __forceinline__ void tg_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(K) : "memory");
+}
+constexpr int tg_par3(int v) { return (v ^ (v >> 1) ^ (v >> 2)) & 1; }
+
+__device__ __forceinline__ float2 tg_lds(uint32_t a) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+    return v;
+}
+
+// Row J of g into the plus or minus chain of a string whose register-bit z
+// pattern is W: plus rows (even popc(J & W)) start at J = 0, minus rows at
+// the lowest set bit of W.  q = shared address of the string's partner row
+// for J = 0 with the partner tile 32 KB-aligned, so row J is at q ^ (J << 12).
+template <int J, int W>
+__device__ __forceinline__ void tg_row(uint32_t q, const float2 (&GX)[8], const float2 (&GY)[8],
+                                       float2 &aP, float2 &bP, float2 &aM, float2 &bM) {
+    const float2 p = tg_lds(q ^ (uint32_t)(J << 12));
+    if constexpr (tg_par3(J & W) == 0) {
+        if constexpr (J == 0) {
+            aP = __fmul2_rn(GX[J], p);
+            bP = __fmul2_rn(GY[J], p);
+        } else {
+            aP = __ffma2_rn(GX[J], p, aP);
+            bP = __ffma2_rn(GY[J], p, bP);
+        }
+    } else {
+        if constexpr (J == (W & -W)) {
+            aM = __fmul2_rn(GX[J], p);
+            bM = __fmul2_rn(GY[J], p);
+        } else {
+            aM = __ffma2_rn(GX[J], p, aM);
+            bM = __ffma2_rn(GY[J], p, bM);
+        }
+    }
+}
+
+// One string on one staged tile; sg = (tile sign, tile sign, -tile sign,
+// -tile sign).  The thread's own sign (-1)^popc(i & z & 511) is applied at
+// the flush.
+template <int W>
+__device__ __forceinline__ void tg_string(uint32_t q, const float2 (&GX)[8],
+                                          const float2 (&GY)[8], float4 sg, float2 &accA,
+                                          float2 &accB) {
+    float2 aP, bP, aM, bM;
+    tg_row<0, W>(q, GX, GY, aP, bP, aM, bM);
+    tg_row<1, W>(q, GX, GY, aP, bP, aM, bM);
+    tg_row<2, W>(q, GX, GY, aP, bP, aM, bM);
+    tg_row<3, W>(q, GX, GY, aP, bP, aM, bM);
+    tg_row<4, W>(q, GX, GY, aP, bP, aM, bM);
+    tg_row<5, W>(q, GX, GY, aP, bP, aM, bM);
+    tg_row<6, W>(q, GX, GY, aP, bP, aM, bM);
+    tg_row<7, W>(q, GX, GY, aP, bP, aM, bM);
+    const float2 ST = make_float2(sg.x, sg.y);
+    accA = __ffma2_rn(ST, aP, accA);
+    accB = __ffma2_rn(ST, bP, accB);
+    if constexpr (W != 0) {
+        const float2 NST = make_float2(sg.z, sg.w);
+        accA = __ffma2_rn(NST, aM, accA);
+        accB = __ffma2_rn(NST, bM, accB);
+    }
+}
+
+// Sum of v[m] over the warp's 32 lanes for m < 16, by recursive halving:
+// returns the sum of value (lane >> 1) & 15.
+__device__ __forceinline__ float tg_transpose_reduce(float (&v)[16]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int h = 8, o = 16; h >= 1; h >>= 1, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int q = 0; q < h; ++q) {
+            const float send = up ? v[q] : v[q + h];
+            const float keep = up ? v[q + h] : v[q];
+            v[q] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+__global__ void __launch_bounds__(kTgThreads, 1) term_grad_tiles_kernel(
+    uint64_t ntiles, int tbits, int nstates, const uint64_t *sx, const uint64_t *sz,
+    const uint32_t *perm, const uint2 *batches, uint32_t nbatch, const float2 *psi,
+    const float2 *g, uint32_t nchunk, uint64_t chunk_tiles, double *partial) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t s_x[kTgB], s_z[kTgB];
+    __shared__ float4 s_sign[2][kTgB];  // per tile parity: (s, s, -s, -s), two tiles in flight
+    __shared__ double s_red[kTgThreads / 32][16];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // stages from the first 32 KB boundary of the dynamic window (kTgAlign
+    // bytes of slack), so that a partner row's address has the row's
+    // register bits at bits 12-14 alone
+    const uint32_t raw = tg_saddr(smem_raw);
+    const uint32_t sbase = (raw + kTgAlign - 1) & ~(kTgAlign - 1);
+    unsigned char *const smem = smem_raw + (sbase - raw);
+    const uint64_t TT = ntiles * (uint64_t)nstates;
+    const uint64_t nitems = (uint64_t)nbatch * nchunk;
+    for (uint64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const uint32_t bi = (uint32_t)(item % nbatch), c = (uint32_t)(item / nbatch);
+        const uint2 bt = batches[bi];
+        const uint32_t kv = bt.y;
+        const uint64_t t0 = (uint64_t)c * chunk_tiles;
+        const uint64_t t1 = t0 + chunk_tiles < TT ? t0 + chunk_tiles : TT;
+        if (tid < kTgB) {
+            s_x[tid] = (uint32_t)tid < kv ? sx[bt.x + tid] : 0ull;
+            s_z[tid] = (uint32_t)tid < kv ? sz[bt.x + tid] : 0ull;
+        }
+        __syncthreads();
+        const uint64_t hpart = s_x[0] >> 12;  // one partner tile for the batch
+        // per string: offset of its partner row for j = 0 within the 32 KB
+        // partner tile, (i ^ (x & 511)) * 8 | ((x >> 9) & 7) << 12 (bits
+        // 0-14), and w = (z >> 9) & 7 (bits 15-17); per thread the parities
+        // of i & z & 511
+        uint32_t info[kTgB], tpar = 0;
+#pragma unroll
+        for (int k = 0; k < kTgB; ++k) {
+            const uint32_t x = (uint32_t)s_x[k], z = (uint32_t)s_z[k];
+            info[k] = ((((uint32_t)tid ^ x) & 511u) << 3) | (((x >> 9) & 7u) << 12) |
+                      (((z >> 9) & 7u) << 15);
+            tpar |= (__popc((uint32_t)tid & z & 511u) & 1u) << k;
+        }
+        auto issue = [&](uint64_t gt, int stage) {
+            const uint64_t st = gt >> tbits, t = gt & (ntiles - 1);
+            const unsigned char *gsrc = reinterpret_cast<const unsigned char *>(g + (gt << 12));
+            const unsigned char *psrc =
+                reinterpret_cast<const unsigned char *>(psi + (((st << tbits) | (t ^ hpart)) << 12));
+            const uint32_t dst = tg_saddr(smem + (size_t)stage * kTgStageBytes);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t off = (uint32_t)(q * kTgThreads + tid) * 16u;
+                tg_cp16(dst + off, psrc + off);
+                tg_cp16(dst + kTgTileBytes + off, gsrc + off);
+            }
+        };
+#pragma unroll
+        for (int q = 0; q < kTgStages - 1; ++q) {
+            if (t0 + q < t1) issue(t0 + q, q);
+            tg_commit();
+        }
+        float2 accA[kTgB], accB[kTgB];
+#pragma unroll
+        for (int k = 0; k < kTgB; ++k) accA[k] = accB[k] = make_float2(0.f, 0.f);
+        double acc64 = 0.0;
+        int win = 0, stage = 0;
+        for (uint64_t gt = t0; gt < t1; ++gt) {
+            if (tid < kTgB) {
+                // (-1)^popc(tile & (z >> 12)) of string tid for this tile; the
+                // entry written two tiles ago was last read before the
+                // previous barrier
+                const float sgn =
+                    (__popcll((gt & (ntiles - 1)) & (s_z[tid] >> 12)) & 1) ? -1.f : 1.f;
+                s_sign[gt & 1][tid] = make_float4(sgn, sgn, -sgn, -sgn);
+            }
+            tg_wait<kTgStages - 2>();
+            __syncthreads();  // tile gt staged by every thread; the oldest stage is free
+            {
+                const uint64_t nx = gt + kTgStages - 1;
+                if (nx < t1) issue(nx, (stage + kTgStages - 1) % kTgStages);
+                tg_commit();
+            }
+            const unsigned char *sb = smem + (size_t)stage * kTgStageBytes;
+            float2 GX[8], GY[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float2 gv =
+                    *reinterpret_cast<const float2 *>(sb + kTgTileBytes + (tid + 512 * j) * 8);
+                GX[j] = make_float2(gv.x, gv.x);
+                GY[j] = make_float2(gv.y, gv.y);
+            }
+            const uint32_t qs = tg_saddr(sb);  // 32 KB-aligned partner tile
+#pragma unroll
+            for (int k = 0; k < kTgB; ++k) {
+                if ((uint32_t)k < kv) {
+                    const uint32_t inf = info[k];
+                    const float4 sg = s_sign[gt & 1][k];
+                    const uint32_t q = qs | (inf & 0x7fffu);
+                    switch ((inf >> 15) & 7u) {
+                        case 0: tg_string<0>(q, GX, GY, sg, accA[k], accB[k]); break;
+                        case 1: tg_string<1>(q, GX, GY, sg, accA[k], accB[k]); break;
+                        case 2: tg_string<2>(q, GX, GY, sg, accA[k], accB[k]); break;
+                        case 3: tg_string<3>(q, GX, GY, sg, accA[k], accB[k]); break;
+                        case 4: tg_string<4>(q, GX, GY, sg, accA[k], accB[k]); break;
+                        case 5: tg_string<5>(q, GX, GY, sg, accA[k], accB[k]); break;
+                        case 6: tg_string<6>(q, GX, GY, sg, accA[k], accB[k]); break;
+                        default: tg_string<7>(q, GX, GY, sg, accA[k], accB[k]); break;
+                    }
+                }
+            }
+            stage = (stage + 1) % kTgStages;
+            if (++win == kTgFlush || gt + 1 == t1) {
+                float v[16];
+#pragma unroll
+                for (int k = 0; k < kTgB; ++k) {
+                    const float re = accA[k].x + accB[k].y, im = accB[k].x - accA[k].y;
+                    const bool neg = (tpar >> k) & 1u;
+                    v[2 * k] = neg ? -re : re;
+                    v[2 * k + 1] = neg ? -im : im;
+                    accA[k] = accB[k] = make_float2(0.f, 0.f);
+                }
+                acc64 += (double)tg_transpose_reduce(v);
+                win = 0;
+            }
+        }
+        tg_wait<0>();
+        if (!(lane & 1)) s_red[warp][lane >> 1] = acc64;
+        __syncthreads();
+        if (tid < 16) {
+            double v = 0.0;
+            for (int w = 0; w < kTgThreads / 32; ++w) v += s_red[w][tid];
+            const uint32_t k = (uint32_t)tid >> 1;
+            if (k < kv) partial[2 * ((uint64_t)perm[bt.x + k] * nchunk + c) + (tid & 1)] = v;
+        }
+        __syncthreads();  // s_x, s_z, s_red and the stages are reused by the next item
+    }
+}
+
+cudaError_t launch_term_grad_tiles(uint64_t N, int nstates, const uint64_t *sx, const uint64_t *sz,
+                                   const uint32_t *perm, const uint2 *batches, uint32_t nbatch,
+                                   uint32_t nstr, const void *psi, const void *g,
+                                   double2 *partial, uint32_t nchunk, double2 *R, uint64_t T,
+                                   const uint32_t *map, const uint8_t *phase, double2 *out,
+                                   int nsm, cudaStream_t st) {
+    const uint64_t ntiles = N >> 12;
+    int tbits = 0;
+    while ((1ull << tbits) < ntiles) ++tbits;
+    const uint64_t TT = ntiles * (uint64_t)nstates;
+    const uint64_t chunk = (TT + nchunk - 1) / nchunk;
+    cudaError_t e = ensure_dyn_smem(reinterpret_cast<const void *>(term_grad_tiles_kernel), kTgSmem);
+    if (e != cudaSuccess) return e;
+    const uint64_t nitems = (uint64_t)nbatch * nchunk;
+    const unsigned grid = (unsigned)(nitems < (uint64_t)nsm ? nitems : (uint64_t)nsm);
+    term_grad_tiles_kernel<<<grid, kTgThreads, kTgSmem, st>>>(
+        ntiles, tbits, nstates, sx, sz, perm, batches, nbatch, static_cast<const float2 *>(psi),
+        static_cast<const float2 *>(g), nchunk, chunk, reinterpret_cast<double *>(partial));
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    sum_partials_kernel<<<nstr, kRedThreads, 0, st>>>(partial, nchunk, R);
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    uint64_t gb = (T + kRedThreads - 1) / kRedThreads;
+    if (gb > 4096) gb = 4096;
+    term_grad_scatter_kernel<<<(unsigned)gb, kRedThreads, 0, st>>>(T, map, phase, R, out);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_term_grad(int dtype, uint64_t N, int nstates, const uint64_t *sx,
                              const uint64_t *sz, uint32_t nstr, const void *psi, const void *g,
                              double2 *partial, uint32_t nchunk, uint64_t chunk, double2 *R,

@@ -74,6 +74,47 @@ def test_term_grad_vs_oracle(cuda, oracle, n, T):
     assert rel(got64, want) <= 1e-5
 
 
+def _jw_like(rng, n, T):
+    """Hopping-like strings X_i Z..Z X_j / Y_i Z..Z Y_j plus random letters:
+    x masks with bits on every row position (partner rows permuted by bits
+    0-8, 9-11 and the partner tile), z with bits 9-11 set and clear."""
+    t = W.random_letters_op(rng, n, T // 2)
+    xs, zs, ph = [t.x], [t.z], [t.phase]
+    i = rng.integers(0, n - 1, T - T // 2)
+    j = np.minimum(i + 1 + rng.integers(0, n - 1, len(i)), n - 1)
+    x = (np.uint64(1) << i.astype(np.uint64)) | (np.uint64(1) << j.astype(np.uint64))
+    between = ((np.uint64(1) << j.astype(np.uint64)) - np.uint64(1)) & ~(
+        (np.uint64(2) << i.astype(np.uint64)) - np.uint64(1))
+    xs.append(x)
+    zs.append(between | np.where(rng.random(len(i)) < 0.5, x, np.uint64(0)))
+    ph.append(rng.integers(0, 4, len(i)).astype(np.uint8))
+    c = rng.standard_normal(T).astype(np.complex128)
+    return (np.concatenate(xs), np.concatenate(zs), np.concatenate(ph), c)
+
+
+@pytest.mark.parametrize("n,T,ns", [(12, 300, 1), (13, 500, 2), (16, 900, 3), (18, 2000, 1)])
+def test_term_grad_tiles_c64(cuda, oracle, n, T, ns):
+    """The tiled complex64 gradient kernel (n >= 12: strings batched by
+    partner tile, staged tiles, sign butterfly, FP64 warp sums) against the
+    oracle on the same complex64 values, summed over several states, and
+    bit-identical when called again (fixed summation order)."""
+    import torch
+    rng = np.random.default_rng(200 + n)
+    x, z, ph, c = _jw_like(rng, n, T)
+    op = PauliOperator(n, x, z, ph, c)
+    psi = W.random_state(rng, 1 << n, nstates=ns).astype(np.complex64).reshape(ns, -1)
+    g = W.random_state(rng, 1 << n, nstates=ns).astype(np.complex64).reshape(ns, -1)
+    want = sum(oracle.term_grad(n, x, z, ph, psi[s].astype(np.complex128),
+                                g[s].astype(np.complex128)) for s in range(ns))
+    pt = torch.from_numpy(psi.reshape(-1)).to(cuda)
+    gt = torch.from_numpy(g.reshape(-1)).to(cuda)
+    got = op.term_grad(pt, gt)
+    again = op.term_grad(pt, gt)
+    assert torch.equal(torch.view_as_real(got), torch.view_as_real(again))
+    err = np.abs(got.cpu().numpy() - want).max() / np.abs(want).max()
+    assert err <= 1e-6, err
+
+
 def test_set_coeffs(cuda, oracle):
     import torch
     t, psi = W.cfg0()
