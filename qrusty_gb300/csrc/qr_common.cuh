@@ -318,12 +318,13 @@ cudaError_t launch_term_grad(int dtype, uint64_t N, int nstates, const uint64_t 
                              cudaStream_t st);
 // Tiled complex64 term gradients (n >= 12): strings sorted by partner tile
 // x >> 12 (sx, sz; perm = merged index of each), batches of <= 8 strings of
-// one partner tile as (first, count); partial holds nstr x nchunk entries.
+// one partner tile as (first, count), largest first; partial holds nstr x
+// nchunk entries; counter: 8 bytes of device scratch (the work counter).
 cudaError_t launch_term_grad_tiles(uint64_t N, int nstates, const uint64_t *sx, const uint64_t *sz,
                                    const uint32_t *perm, const uint2 *batches, uint32_t nbatch,
                                    uint32_t nstr, const void *psi, const void *g,
                                    double2 *partial, uint32_t nchunk, double2 *R, uint64_t T,
                                    const uint32_t *map, const uint8_t *phase, double2 *out,
-                                   int nsm, cudaStream_t st);
+                                   unsigned long long *counter, int nsm, cudaStream_t st);
 
 }  // namespace qr

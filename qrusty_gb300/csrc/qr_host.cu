@@ -1491,21 +1491,23 @@ int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32
             op->tg_nbatch = (uint32_t)bat.size();
             op->tg_ready = true;
         }
+        // about 8 work items per SM, chunks of at least 16 tiles
         const uint64_t TT = (op->N >> 12) * (uint64_t)nstates;
-        uint64_t nchunk = ((uint64_t)op->nsm * 4 + op->tg_nbatch - 1) / op->tg_nbatch;
-        if (nchunk > TT / 8) nchunk = TT / 8;
+        uint64_t nchunk = ((uint64_t)op->nsm * 8 + op->tg_nbatch - 1) / op->tg_nbatch;
+        if (nchunk > TT / 16) nchunk = TT / 16;
         if (nchunk < 1) nchunk = 1;
         void *scratch = nullptr;
         const size_t pbytes = (size_t)nstr * nchunk * sizeof(double2);
-        QR_CUDA(cudaMallocAsync(&scratch, pbytes + (size_t)nstr * sizeof(double2), st),
+        QR_CUDA(cudaMallocAsync(&scratch, pbytes + (size_t)nstr * sizeof(double2) + 16, st),
                 "term-grad scratch");
         double2 *partial = static_cast<double2 *>(scratch);
         double2 *R = partial + (size_t)nstr * nchunk;
+        auto *counter = reinterpret_cast<unsigned long long *>(R + nstr);
         cudaError_t e = launch_term_grad_tiles(
             op->N, nstates, op->d_tg_x.as<uint64_t>(), op->d_tg_z.as<uint64_t>(),
             op->d_tg_perm.as<uint32_t>(), op->d_tg_bat.as<uint2>(), op->tg_nbatch, nstr, psi, g,
             partial, (uint32_t)nchunk, R, op->T, op->d_mmap.as<uint32_t>(), op->d_ph.as<uint8_t>(),
-            reinterpret_cast<double2 *>(out), op->nsm, st);
+            reinterpret_cast<double2 *>(out), counter, op->nsm, st);
         cudaFreeAsync(scratch, st);
         if (e != cudaSuccess) return cuda_fail(e, "term-grad launch");
         return QR_OK;

@@ -350,11 +350,13 @@ __device__ __forceinline__ float tg_transpose_reduce(float (&v)[16]) {
 __global__ void __launch_bounds__(kTgThreads, 1) term_grad_tiles_kernel(
     uint64_t ntiles, int tbits, int nstates, const uint64_t *sx, const uint64_t *sz,
     const uint32_t *perm, const uint2 *batches, uint32_t nbatch, const float2 *psi,
-    const float2 *g, uint32_t nchunk, uint64_t chunk_tiles, double *partial) {
+    const float2 *g, uint32_t nchunk, uint64_t chunk_tiles, double *partial,
+    unsigned long long *next_item) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ uint64_t s_x[kTgB], s_z[kTgB];
     __shared__ float4 s_sign[2][kTgB];  // per tile parity: (s, s, -s, -s), two tiles in flight
     __shared__ double s_red[kTgThreads / 32][16];
+    __shared__ unsigned long long s_item;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // stages from the first 32 KB boundary of the dynamic window (kTgAlign
     // bytes of slack), so that a partner row's address has the row's
@@ -364,8 +366,15 @@ __global__ void __launch_bounds__(kTgThreads, 1) term_grad_tiles_kernel(
     unsigned char *const smem = smem_raw + (sbase - raw);
     const uint64_t TT = ntiles * (uint64_t)nstates;
     const uint64_t nitems = (uint64_t)nbatch * nchunk;
-    for (uint64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const uint32_t bi = (uint32_t)(item % nbatch), c = (uint32_t)(item / nbatch);
+    // items = (batch, chunk), batch-major with the batches largest first:
+    // taken from a counter, so the CTAs stay balanced whatever the batch sizes
+    // (each item's sums are formed in a fixed order, whichever CTA runs it)
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(next_item, 1ull);
+        __syncthreads();
+        const uint64_t item = s_item;
+        if (item >= nitems) break;
+        const uint32_t bi = (uint32_t)(item / nchunk), c = (uint32_t)(item % nchunk);
         const uint2 bt = batches[bi];
         const uint32_t kv = bt.y;
         const uint64_t t0 = (uint64_t)c * chunk_tiles;
@@ -488,7 +497,7 @@ cudaError_t launch_term_grad_tiles(uint64_t N, int nstates, const uint64_t *sx, 
                                    uint32_t nstr, const void *psi, const void *g,
                                    double2 *partial, uint32_t nchunk, double2 *R, uint64_t T,
                                    const uint32_t *map, const uint8_t *phase, double2 *out,
-                                   int nsm, cudaStream_t st) {
+                                   unsigned long long *counter, int nsm, cudaStream_t st) {
     const uint64_t ntiles = N >> 12;
     int tbits = 0;
     while ((1ull << tbits) < ntiles) ++tbits;
@@ -498,9 +507,12 @@ cudaError_t launch_term_grad_tiles(uint64_t N, int nstates, const uint64_t *sx, 
     if (e != cudaSuccess) return e;
     const uint64_t nitems = (uint64_t)nbatch * nchunk;
     const unsigned grid = (unsigned)(nitems < (uint64_t)nsm ? nitems : (uint64_t)nsm);
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
     term_grad_tiles_kernel<<<grid, kTgThreads, kTgSmem, st>>>(
         ntiles, tbits, nstates, sx, sz, perm, batches, nbatch, static_cast<const float2 *>(psi),
-        static_cast<const float2 *>(g), nchunk, chunk, reinterpret_cast<double *>(partial));
+        static_cast<const float2 *>(g), nchunk, chunk, reinterpret_cast<double *>(partial),
+        counter);
     count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
