@@ -899,10 +899,14 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
     uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + tabn);
     uint32_t *s_blk = s_run + a.nruns + 1;
     const uint32_t np = a.npairs, nb = a.nblocks;
+    uint64_t *s_bhi = reinterpret_cast<uint64_t *>(
+        (reinterpret_cast<uintptr_t>(s_blk + np + 1) + 7u) & ~(uintptr_t)7u);
     for (uint32_t i = t; i < a.nsub; i += threads) s_td[i] = a.tdesc[i];
     for (uint32_t i = t; i <= a.nruns; i += threads)
         s_run[i] = a.run_g0[i] | (i < a.nruns ? a.run_key[i] << 16 : 0u);
     for (uint32_t i = t; i <= np; i += threads) s_blk[i] = a.blk_r0[i];
+    for (uint32_t i = t; i < nb; i += threads) s_bhi[i] = a.blk_hi[i];
+    __syncthreads();  // the prologue reads s_bhi
     const uint4 *tdesc = s_td;
 
     const float2 *psi = static_cast<const float2 *>(a.psi);
@@ -927,7 +931,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_pair(const ApplyArg
         ++s_iss[s];
         mbar_expect_tx(&full[s], ntl * tile_bytes);
         for (uint32_t h = 0; h < ntl; ++h) {
-            const float2 *src = psi + st * a.N + ((q ^ a.blk_hi[j0 + h]) << a.b);
+            const float2 *src = psi + st * a.N + ((q ^ s_bhi[j0 + h]) << a.b);
             bulk_g2s(smem_raw + (size_t)s * slot_bytes + (size_t)h * tile_bytes, src, tile_bytes,
                      &full[s]);
         }
@@ -1121,7 +1125,8 @@ static size_t tab_smem_bytes(const ApplyArgs &a, int threads) {
 static size_t pair_smem_bytes(const ApplyArgs &a, uint32_t nsl) {
     const size_t tile_bytes = ((size_t)1 << a.b) * 8u;
     return (size_t)nsl * 2u * tile_bytes + (size_t)a.nsub * 16u * kTabEnt + kPairBarBytes +
-           (size_t)a.nsub * sizeof(uint4) + ((size_t)a.nruns + 1 + a.npairs + 1) * 4u;
+           (size_t)a.nsub * sizeof(uint4) + ((size_t)a.nruns + 1 + a.npairs + 1) * 4u + 8u +
+           (size_t)a.nblocks * 8u;
 }
 
 template <int AMPS, bool WIDE>

@@ -526,6 +526,59 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         bhi.swap(vh);
         bg0.swap(vg);
     }
+    // pair plans: partner blocks with one sub-group are cheap to consume and
+    // a ring of three pairs cannot hide the refill behind a run of them, so
+    // the blocks are paired heavy with heavy and light with light and the
+    // heavy pairs are spread evenly among the light ones (the same order for
+    // every output tile)
+    if (f32 && tile_bits < 0 && ord.size() <= (size_t)kTabCap && bhi.size() >= 4 &&
+        pl.amps == 8) {
+        const size_t nbk = bhi.size();
+        std::vector<uint32_t> heavy, light;
+        for (uint32_t j = 0; j < nbk; ++j)
+            ((bg0[j + 1] - bg0[j] > 1 || bhi[j] == 0) ? heavy : light).push_back(j);
+        std::vector<std::vector<uint32_t>> hp, lp;
+        for (size_t i = 0; i < heavy.size(); i += 2)
+            hp.push_back(i + 1 < heavy.size() ? std::vector<uint32_t>{heavy[i], heavy[i + 1]}
+                                              : std::vector<uint32_t>{heavy[i]});
+        // an odd heavy block takes a light partner
+        size_t l0 = 0;
+        if (!hp.empty() && hp.back().size() == 1 && !light.empty()) hp.back().push_back(light[l0++]);
+        for (size_t i = l0; i < light.size(); i += 2)
+            lp.push_back(i + 1 < light.size() ? std::vector<uint32_t>{light[i], light[i + 1]}
+                                              : std::vector<uint32_t>{light[i]});
+        // a single-block pair can only be the last one
+        std::vector<uint32_t> tail;
+        if (!lp.empty() && lp.back().size() == 1) {
+            tail = lp.back();
+            lp.pop_back();
+        } else if (!hp.empty() && hp.back().size() == 1) {
+            tail = hp.back();
+            hp.pop_back();
+        }
+        std::vector<std::vector<uint32_t>> seq;
+        const size_t nh = hp.size(), tot = hp.size() + lp.size();
+        size_t ih = 0, il = 0;
+        for (size_t k = 0; k < tot; ++k) {
+            // heavy pair ih goes at position floor(ih * tot / nh)
+            if (ih < nh && (il >= lp.size() || k >= ih * tot / nh)) seq.push_back(hp[ih++]);
+            else seq.push_back(lp[il++]);
+        }
+        if (!tail.empty()) seq.push_back(tail);
+        std::vector<size_t> nord;
+        std::vector<uint64_t> nbhi;
+        std::vector<uint32_t> nbg0;
+        for (const auto &pr : seq)
+            for (uint32_t j : pr) {
+                nbhi.push_back(bhi[j]);
+                nbg0.push_back((uint32_t)nord.size());
+                for (uint32_t g = bg0[j]; g < bg0[j + 1]; ++g) nord.push_back(ord[g]);
+            }
+        nbg0.push_back((uint32_t)nord.size());
+        ord.swap(nord);
+        bhi.swap(nbhi);
+        bg0.swap(nbg0);
+    }
     pl.nblocks = (uint32_t)bhi.size();
     pl.ngroups = ord.size();
     pl.diag_block = -1;
