@@ -529,8 +529,10 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
     // pair plans: partner blocks with one sub-group are cheap to consume and
     // a ring of three pairs cannot hide the refill behind a run of them, so
     // the blocks are paired heavy with heavy and light with light and the
-    // heavy pairs are spread evenly among the light ones (the same order for
-    // every output tile)
+    // heavy pairs are spread evenly among the light ones, each closing a run
+    // of light pairs (the tile's last pair is heavy, so the ring refills
+    // across the table rebuild and the next tile starts on light pairs); the
+    // same order for every output tile
     if (f32 && tile_bits < 0 && ord.size() <= (size_t)kTabCap && bhi.size() >= 4 &&
         pl.amps == 8) {
         const size_t nbk = bhi.size();
@@ -560,8 +562,9 @@ int build_plan(qr_op *op, int dtype, int adjoint, int tile_bits = -1) {
         const size_t nh = hp.size(), tot = hp.size() + lp.size();
         size_t ih = 0, il = 0;
         for (size_t k = 0; k < tot; ++k) {
-            // heavy pair ih goes at position floor(ih * tot / nh)
-            if (ih < nh && (il >= lp.size() || k >= ih * tot / nh)) seq.push_back(hp[ih++]);
+            // heavy pair ih goes at position floor((ih + 1) * tot / nh) - 1
+            if (ih < nh && (il >= lp.size() || k >= (ih + 1) * tot / nh - 1))
+                seq.push_back(hp[ih++]);
             else seq.push_back(lp[il++]);
         }
         if (!tail.empty()) seq.push_back(tail);
