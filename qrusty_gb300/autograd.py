@@ -8,6 +8,9 @@ hand-written backward:
 * grad_c_k = <P_k psi, g>    -- one FP64-accumulated reduction per term
   (``qr_term_grad``); its real part for real coefficients.
 
+When both are needed the two run on two streams at once (they read the
+same psi / g and write different outputs).
+
 Here P_k is term k without its coefficient, (1, -i, -1, +i)[phase_k] X^x Z^z,
 and <a, b> = sum conj(a) b.  complex64 states run the compensated-c64
 kernels, complex128 states the plain c128 kernels.
@@ -41,6 +44,14 @@ class PauliTerms:
         self._cur = None
         self._dev_ref = None
         self._dev_ver = -1
+        self._side = {}
+
+    def side_stream(self, device) -> "torch.cuda.Stream":
+        """A second stream per device for the backward's term gradients."""
+        key = torch.device(device).index
+        if key not in self._side:
+            self._side[key] = torch.cuda.Stream(device=device)
+        return self._side[key]
 
     def _ensure(self, c_host=None) -> PauliOperator:
         if self._op is None:
@@ -93,9 +104,26 @@ class _PauliApply(torch.autograd.Function):
         op = ctx.terms.operator(coeffs)
         gy = gy.contiguous()
         grad_c = grad_psi = None
-        if ctx.needs_input_grad[1]:
+        need_c, need_psi = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if need_c and need_psi and gy.is_cuda:
+            # The two halves are independent: the term gradients run on a
+            # side stream beside the adjoint apply, so the reduction's CTAs
+            # (which take work items from a counter) fill the SMs that the
+            # apply's last wave of output tiles leaves idle.
+            main = torch.cuda.current_stream(gy.device)
+            side = ctx.terms.side_stream(gy.device)
+            p = psi.contiguous()
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                tg = op.term_grad(p, gy)
             grad_psi = op.apply(gy, adjoint=True)
-        if ctx.needs_input_grad[0]:
+            main.wait_stream(side)
+            tg.record_stream(main)  # allocated on the side stream, read on main
+            grad_c = (tg.real if ctx.real else tg).to(device=ctx.cdevice, dtype=ctx.cdtype)
+            return grad_c, grad_psi, None
+        if need_psi:
+            grad_psi = op.apply(gy, adjoint=True)
+        if need_c:
             tg = op.term_grad(psi.contiguous(), gy)
             grad_c = (tg.real if ctx.real else tg).to(device=ctx.cdevice, dtype=ctx.cdtype)
         return grad_c, grad_psi, None
