@@ -543,51 +543,43 @@ cudaError_t launch_csr_fill(const CsrArgs &a, int nsm, cudaStream_t st) {
     return launch_csr_fold(b, nsm, st);
 }
 
-// y = A v, complex128.  S lanes per row: the lanes of a row stride its
-// entries four at a time (independent loads in flight), then combine their
-// partial sums with a butterfly over the S lanes.
+// y = A v, complex128.  S lanes per row, U entries per lane per step with
+// the step's tail predicated, so that a row of up to S * U entries costs one
+// round of dependent loads (index, then the gathered v); the lanes' partial
+// sums meet in a butterfly over the S lanes.  The GB300's FP64 rate is the
+// bound: a step whose S * U slots match the row length wastes no DFMA slot.
 // Replaces spmat_dot_densevec (qrusty/src/accel.rs:338-370).
-template <int S>
-__global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, uint64_t ncols,
-                                                       const uint64_t *__restrict__ indptr,
-                                                       const uint64_t *__restrict__ indices,
-                                                       const double2 *__restrict__ data,
-                                                       const double2 *__restrict__ v,
-                                                       double2 *__restrict__ y) {
+template <int S, int U>
+__device__ __forceinline__ void spmv_rows(uint64_t nrows, uint64_t ncols,
+                                          const uint64_t *__restrict__ indptr,
+                                          const uint64_t *__restrict__ indices,
+                                          const double2 *__restrict__ data,
+                                          const double2 *__restrict__ v, double2 *__restrict__ y) {
     const uint32_t sl = threadIdx.x & (S - 1);
     const uint64_t groups = (uint64_t)gridDim.x * (blockDim.x / S);
     for (uint64_t r = blockIdx.x * (uint64_t)(blockDim.x / S) + (threadIdx.x / S); r < nrows;
          r += groups) {
         const uint64_t j0 = indptr[r], j1 = indptr[r + 1];
         double sr = 0.0, si = 0.0, tr = 0.0, ti = 0.0;
-        uint64_t j = j0 + sl;
-        // four entries per lane per step: their loads are in flight together
-        for (; j + 3 * S < j1; j += 4 * S) {
-            uint64_t c[4];
-            double2 d[4];
+        for (uint64_t j = j0 + sl; j < j1; j += (uint64_t)U * S) {
+            uint64_t c[U];
+            double2 d[U];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {  // the matrix streams once: evict-first loads
-                c[u] = __ldcs(indices + j + u * S);
-                d[u] = __ldcs(data + j + u * S);
+            for (int u = 0; u < U; ++u) {  // the matrix streams once: evict-first loads
+                const bool ok = j + (uint64_t)u * S < j1;
+                c[u] = ok ? __ldcs(indices + j + u * S) : ncols;
+                d[u] = ok ? __ldcs(data + j + u * S) : make_double2(0.0, 0.0);
             }
-            double2 x[4];
+            double2 x[U];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) x[u] = c[u] < ncols ? __ldg(v + c[u]) : make_double2(0.0, 0.0);
+            for (int u = 0; u < U; ++u)
+                x[u] = c[u] < ncols ? __ldg(v + c[u]) : make_double2(0.0, 0.0);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (c[u] >= ncols) continue;  // out-of-range columns are skipped
+            for (int u = 0; u < U; ++u) {
+                if (c[u] >= ncols) continue;  // out-of-range columns (and the tail) are skipped
                 double &ar = (u & 1) ? tr : sr, &ai = (u & 1) ? ti : si;
                 ar = fma(d[u].x, x[u].x, fma(-d[u].y, x[u].y, ar));
                 ai = fma(d[u].x, x[u].y, fma(d[u].y, x[u].x, ai));
-            }
-        }
-        for (; j < j1; j += S) {
-            const uint64_t c = indices[j];  // out-of-range columns are skipped
-            if (c < ncols) {
-                const double2 d = data[j];
-                const double2 x = v[c];
-                sr = fma(d.x, x.x, fma(-d.y, x.y, sr));
-                si = fma(d.x, x.y, fma(d.y, x.x, si));
             }
         }
         sr += tr;
@@ -601,21 +593,45 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, uint64_t 
     }
 }
 
+constexpr int kSpmvLanes = 4;   // lanes per row
+constexpr int kSpmvMaxStep = 16;  // entries per lane per step, at most
+
+// The step depth U is chosen from the first row's length (every row of a
+// Pauli-sum CSR holds G entries; any CSR is handled at any depth).
+__global__ void __launch_bounds__(256) csr_spmv_kernel(uint64_t nrows, uint64_t ncols,
+                                                       const uint64_t *__restrict__ indptr,
+                                                       const uint64_t *__restrict__ indices,
+                                                       const double2 *__restrict__ data,
+                                                       const double2 *__restrict__ v,
+                                                       double2 *__restrict__ y) {
+    constexpr int S = kSpmvLanes;
+    const uint64_t len0 = indptr[1] - indptr[0];
+    const uint64_t want = (len0 + S - 1) / S;
+    const int u = want < 1 ? 1 : (want > (uint64_t)kSpmvMaxStep ? kSpmvMaxStep : (int)want);
+#define QR_SPMV_CASE(k) \
+    case k: spmv_rows<S, k>(nrows, ncols, indptr, indices, data, v, y); break;
+    switch (u) {
+        QR_SPMV_CASE(1) QR_SPMV_CASE(2) QR_SPMV_CASE(3) QR_SPMV_CASE(4)
+        QR_SPMV_CASE(5) QR_SPMV_CASE(6) QR_SPMV_CASE(7) QR_SPMV_CASE(8)
+        QR_SPMV_CASE(9) QR_SPMV_CASE(10) QR_SPMV_CASE(11) QR_SPMV_CASE(12)
+        QR_SPMV_CASE(13) QR_SPMV_CASE(14) QR_SPMV_CASE(15)
+        default: spmv_rows<S, kSpmvMaxStep>(nrows, ncols, indptr, indices, data, v, y); break;
+    }
+#undef QR_SPMV_CASE
+}
+
 cudaError_t launch_csr_spmv(uint64_t nrows, uint64_t ncols, const uint64_t *indptr,
                             const uint64_t *indices, const double *data, const double *v,
                             double *y, int nsm, cudaStream_t st) {
     if (nrows == 0) return cudaSuccess;
-    // 8 lanes per row: rows of a Pauli-sum CSR hold G entries (tens to a few
-    // hundred), about 6 per lane at G = 44; no host read of nnz, so the call
-    // stays asynchronous
-    constexpr int S = 8;
-    const uint64_t rows_per_block = 256 / S;
+    // no host read of nnz or row lengths: the call stays asynchronous
+    const uint64_t rows_per_block = 256 / kSpmvLanes;
     uint64_t g = (nrows + rows_per_block - 1) / rows_per_block;
     if (g > (uint64_t)nsm * 16) g = (uint64_t)nsm * 16;
-    csr_spmv_kernel<S><<<(unsigned)g, 256, 0, st>>>(nrows, ncols, indptr, indices,
-                                                    reinterpret_cast<const double2 *>(data),
-                                                    reinterpret_cast<const double2 *>(v),
-                                                    reinterpret_cast<double2 *>(y));
+    csr_spmv_kernel<<<(unsigned)g, 256, 0, st>>>(nrows, ncols, indptr, indices,
+                                                 reinterpret_cast<const double2 *>(data),
+                                                 reinterpret_cast<const double2 *>(v),
+                                                 reinterpret_cast<double2 *>(y));
     count_launch();
     return cudaGetLastError();
 }

@@ -283,6 +283,34 @@ def test_spmv_skips_out_of_range_columns(cuda):
     assert np.allclose(got, want, rtol=1e-12, atol=1e-12)
 
 
+@pytest.mark.parametrize("first_len", [0, 1, 7, 44, 64, 65, 300])
+def test_spmv_ragged_rows(cuda, first_len):
+    """The step depth of qr_csr_spmv follows the first row's length; every
+    other row length (empty, shorter, longer, many steps) must come out the
+    same as scipy's product, with several rows per warp in flight."""
+    import scipy.sparse as sps
+    import torch
+    from qrusty_gb300 import _lib
+    rng = np.random.default_rng(first_len + 11)
+    nrows, ncols = 1000, 700
+    lens = rng.integers(0, 200, nrows)
+    lens[rng.random(nrows) < 0.1] = 0
+    lens[0] = first_len
+    indptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    nnz = int(indptr[-1])
+    indices = rng.integers(0, ncols, nnz).astype(np.int64)
+    data = rng.standard_normal(nnz) + 1j * rng.standard_normal(nnz)
+    v = rng.standard_normal(ncols) + 1j * rng.standard_normal(ncols)
+    want = sps.csr_matrix((data, indices, indptr), shape=(nrows, ncols)) @ v
+    d = lambda a: torch.from_numpy(a).to(cuda)
+    ip, ij, dd, vd = d(indptr), d(indices), d(data), d(v)
+    y = torch.empty(nrows, dtype=torch.complex128, device=cuda)
+    _lib.check(_lib.load().qr_csr_spmv(nrows, ncols, ip.data_ptr(), ij.data_ptr(), dd.data_ptr(),
+                                       vd.data_ptr(), y.data_ptr(), None))
+    got = y.cpu().numpy()
+    assert np.abs(got - want).max() <= 1e-12 * max(1.0, np.abs(want).max())
+
+
 def test_chain22_sampled_rows_vs_make_row(cuda, oracle):
     """The chain at its benchmark size, n = 22 (G = 44, 1.85e8 stored
     entries, built on the device by the staged bulk-store kernel with the
