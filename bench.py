@@ -675,6 +675,14 @@ def measure_batch(steps=3, warmup=3, per_op=True):
         ms_64 = _events_time(per_op_apply, 2, 1, stream)
         out["per_op_c64c_ms"] = ms_64
         out["speedup_vs_per_op_c64c"] = ms_64 / ms_b
+        # every launch form on its own clock (the autotuner keeps the fastest)
+        forms = {}
+        for m, name in ((0, "persistent"), (1, "per_operator_graph"), (2, "hybrid")):
+            bm = Batch(ops, [ns] * len(ops))
+            bm.set_mode(m)
+            forms[name] = _events_time(lambda: bm.apply(psis, ys), 2, 1, stream)
+            del bm
+        out["forms_ms"] = forms
     return out, (ops, psis, ys, terms, b)
 
 
@@ -856,8 +864,8 @@ def run_batch(args):
                      roofline=r["roofline"], rel_err=r["rel_err_vs_oracle"],
                      per_op_c128={"ms_per_step": ms_128, "launches_per_step": len(ops)},
                      speedup_vs_per_op_c128=ms_128 / r["ms_per_step"],
-                     per_op_c64c_ms=r.get("per_op_c64c_ms"), setup_s=r["setup_s"],
-                     gpu_launches=r["gpu_launches_per_step"])
+                     per_op_c64c_ms=r.get("per_op_c64c_ms"), forms_ms=r.get("forms_ms"),
+                     setup_s=r["setup_s"], gpu_launches=r["gpu_launches_per_step"])
     print(json.dumps(out), flush=True)
 
 
