@@ -74,6 +74,29 @@ def test_device_grouping_matches_numpy(cuda, n, T, xb, zb):
         assert inf["ngroups"] == len(gx) and inf["nmerged"] == M
 
 
+def test_device_grouping_millions_of_terms(cuda):
+    """4.5 million terms: the scans run several top-level chunks and the
+    radix sort thousands of tiles; checked with vectorised numpy."""
+    rng = np.random.default_rng(4242)
+    T, n = 4_500_000, 40
+    x = rng.integers(0, 1 << 14, T, dtype=np.uint64) << np.uint64(20)
+    z = rng.integers(0, 1 << 6, T, dtype=np.uint64) | (x >> np.uint64(3))
+    ph = rng.integers(0, 4, T).astype(np.uint8)
+    c = rng.standard_normal(T).astype(np.complex128)
+    op = PauliOperator(n, x, z, ph, c)
+    got = op.groups()
+    assert np.array_equal(got["order"], np.argsort(x, kind="stable").astype(np.uint32))
+    gx, counts = np.unique(x, return_counts=True)
+    assert np.array_equal(got["gx"], gx)
+    assert np.array_equal(got["goff"], np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32))
+    # merged strings numbered by first occurrence
+    keys = np.stack([x, z], axis=1)
+    _, first, inv = np.unique(keys, axis=0, return_index=True, return_inverse=True)
+    rank = np.empty(len(first), dtype=np.int64)
+    rank[np.argsort(first, kind="stable")] = np.arange(len(first))
+    assert np.array_equal(got["mmap"], rank[inv.reshape(-1)].astype(np.uint32))
+
+
 def _check_csr(oracle, op, t, c):
     ip, ij, d = op.csr_host()
     oi, oj, od = oracle.csr_build(t.n, t.x, t.z, oracle.make_params(t.phase, c), step=1024)
