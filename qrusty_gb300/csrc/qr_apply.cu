@@ -409,6 +409,7 @@ __device__ __forceinline__ uint32_t parity(uint64_t r, uint64_t m) {
 constexpr int kTabStages = 4;  // partner-tile ring depth (timed best of 3, 4, 5)
 constexpr size_t kMaxSmemPerBlock = 227u * 1024u;  // sm_100-family opt-in limit
 constexpr int kTabEnt = 4;  // per-tile table entries (float4) per sub-group
+constexpr uint32_t kTabBhiCap = 1024;  // partner blocks whose XORs are staged in shared memory
 // full barriers, stage counters, the abort flag and per-stage issue counts,
 // rounded to 16 bytes so that the 16-byte thread descriptors after them stay
 // aligned
@@ -658,6 +659,14 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
                                             (size_t)AMPS * threads * 8u + kTabBarBytes);
     uint32_t *s_run = reinterpret_cast<uint32_t *>(s_td + kTabCap);
     uint32_t *s_blk = s_run + kTabCap + 1;
+    // partner-tile XORs in shared memory (up to kTabBhiCap blocks): a refill
+    // needs no global load first
+    uint64_t *s_bhi = reinterpret_cast<uint64_t *>(
+        (reinterpret_cast<uintptr_t>(s_blk + kTabCap + 2) + 7u) & ~(uintptr_t)7u);
+    const bool bhi_smem = a.nblocks <= kTabBhiCap;
+    if (bhi_smem)
+        for (uint32_t i = t; i < a.nblocks; i += threads) s_bhi[i] = a.blk_hi[i];
+    const uint64_t *bhi = bhi_smem ? s_bhi : a.blk_hi;
     if constexpr (!MULTI) {
         for (uint32_t i = t; i < a.nsub; i += threads) s_td[i] = a.tdesc[i];
         for (uint32_t i = t; i <= a.nruns; i += threads)
@@ -684,13 +693,14 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
         const uint64_t item = first + k * gridDim.x;
         const uint64_t st = item / a.ntiles;
         const uint64_t q = item - st * a.ntiles;
-        const float2 *src = psi + st * a.N + ((q ^ a.blk_hi[j]) << a.b);
+        const float2 *src = psi + st * a.N + ((q ^ bhi[j]) << a.b);
         const int s = (int)(L % (uint64_t)kTabStages);
         if (blockIdx.x == 0 && (int64_t)L == a.withhold) return;  // test hook: never issued
         ++s_iss[s];
         mbar_expect_tx(&full[s], tile_bytes);
         bulk_g2s(smem_raw + (size_t)s * tile_bytes, src, tile_bytes, &full[s]);
     };
+    __syncthreads();  // the prologue reads s_bhi
     if (t == 0) {
         for (int s = 0; s < kTabStages; ++s) {
             mbar_init(&full[s], 1);
@@ -834,7 +844,7 @@ __global__ void __launch_bounds__(kC64Threads, 1) apply_c64c_tab(const ApplyArgs
                             ++st2;
                         }
                     }
-                    const float2 *src = psi + st2 * a.N + ((q2 ^ a.blk_hi[j2]) << a.b);
+                    const float2 *src = psi + st2 * a.N + ((q2 ^ bhi[j2]) << a.b);
                     if (blockIdx.x != 0 || (int64_t)(L + kTabStages) != a.withhold) {
                         ++s_iss[s];
                         mbar_expect_tx(&full[s], tile_bytes);
@@ -1117,7 +1127,8 @@ static size_t tab_smem_bytes(const ApplyArgs &a, int threads) {
     const uint32_t tabn = a.nsub < kTabCap ? a.nsub : kTabCap;
     return (size_t)kTabStages * tile_bytes + (size_t)tabn * 16u * kTabEnt +
            (size_t)AMPS * threads * 8u + kTabBarBytes +
-           (size_t)kTabCap * sizeof(uint4) + (2u * (size_t)kTabCap + 3u) * 4u;
+           (size_t)kTabCap * sizeof(uint4) + (2u * (size_t)kTabCap + 3u) * 4u + 8u +
+           (a.nblocks <= kTabBhiCap ? (size_t)a.nblocks * 8u : 0u);
 }
 
 // shared memory of the paired kernel with nsl ring slots (exact sizes of the
