@@ -244,7 +244,9 @@ int qr_expect(qr_op *op, int32_t dtype, const void *psi, int32_t nstates, double
  * pointer), where P_k = (1, -i, -1, +i)[phase_k] X^x_k Z^z_k is the term
  * without its coefficient and g the upstream gradient.  For real
  * coefficients the gradient is Re(out[k]).  FP32 products for QR_C64C,
- * FP64 accumulation across threads and tiles.  New: no reference
+ * FP64 accumulation across threads and tiles, every sum in a fixed order
+ * (repeated calls and graph replays give the same bits).  Scratch is taken
+ * from the stream-ordered allocator on `stream`.  New: no reference
  * counterpart (used by the autograd backward). */
 int qr_term_grad(qr_op *op, int32_t dtype, const void *psi, const void *g, int32_t nstates,
                  double *out, void *stream);
