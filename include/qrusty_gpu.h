@@ -68,7 +68,10 @@ typedef struct {
  * qrusty/src/lib.rs:354-376, plus make_params, qrusty/src/accel.rs:141-157).
  * Validates 1 <= n <= 63, T >= 1, masks within n bits, phase <= 3.
  * Uploads the terms to the current CUDA device and groups them there
- * (qr_op_get_groups); synchronous. */
+ * (qr_op_get_groups); synchronous.  The grouping kernels run on the legacy
+ * default stream with scratch from the stream-ordered allocator, so, like
+ * cudaMalloc, this is not to be called while a stream of the device is
+ * being captured into a CUDA graph. */
 int qr_op_create(int32_t n, uint64_t nterms, const uint64_t *x, const uint64_t *z,
                  const uint8_t *phase, const double *coeff, qr_op **out);
 
